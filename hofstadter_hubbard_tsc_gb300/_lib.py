@@ -1,0 +1,119 @@
+"""ctypes binding of ``libhh_dmrg.so`` (the C ABI declared in include/hh_dmrg.h).
+
+This is the same binding a Python caller of the reference's hot path would
+write; it loads the in-tree library and raises if it is missing: there is no
+CPU fallback for any entry point.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhh_dmrg.so")
+
+HH_OK = 0
+HH_PREC_FP64 = 0
+HH_PREC_BF16X3 = 1
+
+STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
+          -4: "quantum number mismatch", -5: "bounded device wait timed out",
+          -6: "numerical failure", -7: "unsupported"}
+
+# term kinds (enum hh_term_kind)
+BLOCK_VEC_DIA = 1
+VEC_BLOCK_DIA = 2
+SITE_VEC_SITE_DIA = 3
+SITE_VEC_SITE_NDIA = 4
+BLOCK_SITE_VEC_NDIA = 5
+VEC_BLOCK_SITE_NDIA = 6
+BLOCK_VEC_SITE_NDIA = 7
+SITE_VEC_BLOCK_NDIA = 8
+BLOCK_VEC_BLOCK_NDIA = 9
+BLOCK_SITE_VEC_DIA = 10
+VEC_BLOCK_SITE_DIA = 11
+BLOCK_VEC_SITE_DIA = 12
+SITE_VEC_BLOCK_DIA = 13
+BLOCK_VEC_BLOCK_DIA = 14
+
+
+class HHTerm(C.Structure):
+    _fields_ = [("kind", C.c_int), ("flag0", C.c_int), ("flag1", C.c_int),
+                ("trans0", C.c_int), ("trans1", C.c_int),
+                ("op0", C.c_void_p), ("op1", C.c_void_p),
+                ("coef_re", C.c_double), ("coef_im", C.c_double)]
+
+
+P = C.c_void_p
+PP = C.POINTER(C.c_void_p)
+I = C.c_int
+D = C.c_double
+IP = C.POINTER(C.c_int)
+DP = C.POINTER(C.c_double)
+LLP = C.POINTER(C.c_longlong)
+
+# name -> (restype, argtypes); every symbol declared in include/hh_dmrg.h
+SIGNATURES = {
+    "hh_init": (I, [I, PP]),
+    "hh_finalize": (I, [P]),
+    "hh_last_error": (C.c_char_p, [P]),
+    "hh_status_string": (C.c_char_p, [I]),
+    "hh_ctx_stream": (I, [P, PP]),
+    "hh_ctx_sync": (I, [P]),
+    "hh_version": (I, []),
+    "hh_block_create": (I, [P, I, I, I, I, IP, DP, PP]),
+    "hh_block_zeros": (I, [P, I, I, I, I, IP, PP]),
+    "hh_block_info": (I, [P, IP, IP, IP, IP, LLP]),
+    "hh_block_qn": (I, [P, IP]),
+    "hh_block_download": (I, [P, DP]),
+    "hh_block_free": (I, [P]),
+    "hh_block_add": (I, [P, DP, P]),
+    "hh_basis_create": (I, [P, I, I, IP, IP, PP]),
+    "hh_basis_free": (I, [P]),
+    "hh_wave_create": (I, [P, I, I, I, IP, I, PP]),
+    "hh_wave_info": (I, [P, LLP, IP]),
+    "hh_wave_upload": (I, [P, DP]),
+    "hh_wave_download": (I, [P, DP]),
+    "hh_wave_copy": (I, [P, P]),
+    "hh_wave_free": (I, [P]),
+    "hh_wave_dot": (I, [P, P, DP]),
+    "hh_wave_norm": (I, [P, DP]),
+    "hh_wave_normalize": (I, [P]),
+    "hh_plan_create": (I, [P, P, P, P, I, C.POINTER(HHTerm), PP]),
+    "hh_plan_stats": (I, [P, DP]),
+    "hh_plan_free": (I, [P]),
+    "hh_matvec": (I, [P, P, P, I]),
+    "hh_matvec_host": (I, [P, DP, DP, I]),
+    "hh_lanczos": (I, [P, P, D, I, I, DP, IP]),
+}
+
+_lib = None
+
+
+class HHError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"{STATUS.get(status, status)} ({status}): {msg}")
+        self.status = status
+
+
+def load(path=LIB_PATH):
+    """Load the library once; raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with hofstadter_hubbard_tsc_gb300.build.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status, ctx=None):
+    if status != HH_OK:
+        msg = ""
+        if ctx is not None and _lib is not None:
+            m = _lib.hh_last_error(ctx)
+            msg = m.decode() if m else ""
+        raise HHError(status, msg)

@@ -1,0 +1,343 @@
+// Grouped segment GEMM in complex FP64 and the wave-vector kernels.
+//
+// One CTA owns one 64x64 output tile and accumulates every segment of its
+// tile (c_s * opP(P_s) * opQ(Q_s), or c_s * P_s for copies) in registers before
+// a single store: the sum over terms that the reference performs with
+// successive ZGEMM(beta=1) calls on the same output sub-block is done here
+// without atomics and in a fixed order.
+#include "hh_internal.h"
+
+namespace hh {
+
+namespace {
+
+constexpr int TM = 64, TN = 64, TK = 16, NT = 256;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ const double2* resolve(long long off, int base, const double2* bin,
+                                                  const double2* bscr, const double2* bout) {
+  switch (base) {
+    case HH_BASE_IN: return bin + off;
+    case HH_BASE_SCR: return bscr + off;
+    case HH_BASE_OUT: return bout + off;
+    default: return reinterpret_cast<const double2*>(off);
+  }
+}
+
+__global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __restrict__ tiles,
+                                                          const hh_seg* __restrict__ segs,
+                                                          const double2* __restrict__ bin,
+                                                          double2* __restrict__ bscr,
+                                                          double2* __restrict__ bout,
+                                                          long long sin, long long sscr, long long sout) {
+  __shared__ double2 Ps[TK][TM + 1];
+  __shared__ double2 Qs[TK][TN + 1];
+  const hh_tile t = tiles[blockIdx.x];
+  const int b = blockIdx.y;
+  const double2* in = bin + (long long)b * sin;
+  double2* scr = bscr + (long long)b * sscr;
+  double2* out = bout + (long long)b * sout;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int mrem = min(TM, t.M - t.m0), nrem = min(TN, t.N - t.n0);
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+
+  for (int si = 0; si < t.nseg; ++si) {
+    const hh_seg s = segs[t.seg0 + si];
+    const double2 c = make_double2(s.cre, s.cim);
+    const double2* P = resolve(s.poff, s.pbase, in, scr, out);
+    if (s.kind == HH_SEG_COPY) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          int r = ty * 4 + i, q = tx * 4 + j;
+          if (r < mrem && q < nrem) {
+            double2 v = P[(long long)(t.m0 + r) + (long long)(t.n0 + q) * s.ldp];
+            double2 cv = cmul(c, v);
+            acc[i][j].x += cv.x;
+            acc[i][j].y += cv.y;
+          }
+        }
+      continue;
+    }
+    const double2* Q = resolve(s.qoff, s.qbase, in, scr, out);
+    for (int k0 = 0; k0 < s.K; k0 += TK) {
+      const int krem = min(TK, s.K - k0);
+      // stage the P tile (TM x TK), scaled by the segment coefficient
+#pragma unroll
+      for (int r = 0; r < (TM * TK) / NT; ++r) {
+        int e = tid + r * NT;
+        int m, kk;
+        if (s.opP == HH_OP_N) { m = e % TM; kk = e / TM; } else { kk = e % TK; m = e / TK; }
+        double2 v = make_double2(0.0, 0.0);
+        if (m < mrem && kk < krem) {
+          if (s.opP == HH_OP_N) {
+            v = P[(long long)(t.m0 + m) + (long long)(k0 + kk) * s.ldp];
+          } else {
+            v = P[(long long)(k0 + kk) + (long long)(t.m0 + m) * s.ldp];
+            if (s.opP == HH_OP_C) v.y = -v.y;
+          }
+          v = cmul(c, v);
+        }
+        Ps[kk][m] = v;
+      }
+#pragma unroll
+      for (int r = 0; r < (TN * TK) / NT; ++r) {
+        int e = tid + r * NT;
+        int n, kk;
+        if (s.opQ == HH_OP_N) { kk = e % TK; n = e / TK; } else { n = e % TN; kk = e / TN; }
+        double2 v = make_double2(0.0, 0.0);
+        if (n < nrem && kk < krem) {
+          if (s.opQ == HH_OP_N) {
+            v = Q[(long long)(k0 + kk) + (long long)(t.n0 + n) * s.ldq];
+          } else {
+            v = Q[(long long)(t.n0 + n) + (long long)(k0 + kk) * s.ldq];
+            if (s.opQ == HH_OP_C) v.y = -v.y;
+          }
+        }
+        Qs[kk][n] = v;
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int kk = 0; kk < TK; ++kk) {
+        double2 a[4], bb[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = Ps[kk][ty * 4 + i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bb[j] = Qs[kk][tx * 4 + j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            acc[i][j].x = fma(a[i].x, bb[j].x, acc[i][j].x);
+            acc[i][j].x = fma(-a[i].y, bb[j].y, acc[i][j].x);
+            acc[i][j].y = fma(a[i].x, bb[j].y, acc[i][j].y);
+            acc[i][j].y = fma(a[i].y, bb[j].x, acc[i][j].y);
+          }
+      }
+      __syncthreads();
+    }
+  }
+  double2* O = (t.obase == HH_BASE_SCR) ? scr : out;
+  O += t.ooff;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int r = ty * 4 + i, q = tx * 4 + j;
+      if (r < mrem && q < nrem) {
+        long long idx = (long long)(t.m0 + r) + (long long)(t.n0 + q) * t.ldo;
+        if (t.accumulate) {
+          double2 o = O[idx];
+          o.x += acc[i][j].x;
+          o.y += acc[i][j].y;
+          O[idx] = o;
+        } else {
+          O[idx] = acc[i][j];
+        }
+      }
+    }
+}
+
+// ----------------------------------------------------------- wave vectors
+constexpr int RB = 256;
+
+__global__ void dot_partial_kernel(const double2* a, const double2* b, long long n, double* part) {
+  __shared__ double sh[RB / 32];
+  double s = 0.0;
+  for (long long i = blockIdx.x * (long long)RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB) {
+    double2 x = a[i], y = b[i];
+    s = fma(x.x, y.x, s);
+    s = fma(x.y, y.y, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < RB / 32 ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+  }
+}
+
+__global__ void sum_kernel(const double* part, int n, double* out) {
+  __shared__ double sh[RB / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += RB) s += part[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < RB / 32 ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[0] = s;
+  }
+}
+
+__global__ void axpy_kernel(double2* y, const double2* x, double a, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = y[i], u = x[i];
+    v.x = fma(a, u.x, v.x);
+    v.y = fma(a, u.y, v.y);
+    y[i] = v;
+  }
+}
+
+__global__ void scale_kernel(double2* y, double a, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = y[i];
+    v.x *= a;
+    v.y *= a;
+    y[i] = v;
+  }
+}
+
+// Re<V_j, w> for j < k: one pass over w; partial sums per CTA, k <= 128.
+constexpr int KMAX = 128;
+__global__ void krylov_dots_kernel(const double2* V, int k, long long ld, const double2* w, long long n,
+                                   double* part) {
+  __shared__ double sh[KMAX][RB / 32 + 1];
+  double acc[8];
+  for (int j0 = 0; j0 < k; j0 += 8) {
+    int jn = min(8, k - j0);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = 0.0;
+    for (long long i = blockIdx.x * (long long)RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB) {
+      double2 x = w[i];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (j < jn) {
+          double2 v = V[(long long)(j0 + j) * ld + i];
+          acc[j] = fma(v.x, x.x, acc[j]);
+          acc[j] = fma(v.y, x.y, acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      double s = acc[j];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if ((threadIdx.x & 31) == 0 && j < jn) sh[j0 + j][threadIdx.x >> 5] = s;
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < k; j += RB) {
+    double s = 0.0;
+    for (int q = 0; q < RB / 32; ++q) s += sh[j][q];
+    part[(long long)blockIdx.x * KMAX + j] = s;
+  }
+}
+
+__global__ void krylov_reduce_kernel(const double* part, int nblk, int k, double* out) {
+  int j = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += part[(long long)b * KMAX + j];
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[j] = s;
+  }
+}
+
+// w -= sum_j c_j V_j  (sign = -1) or out = sum_j c_j V_j (sign = 0)
+__global__ void krylov_axpy_kernel(const double2* V, int k, long long ld, double2* w, long long n,
+                                   const double* coef, int overwrite) {
+  __shared__ double c[KMAX];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = coef[j];
+  __syncthreads();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int j = 0; j < k; ++j) {
+      double2 v = V[(long long)j * ld + i];
+      s.x = fma(c[j], v.x, s.x);
+      s.y = fma(c[j], v.y, s.y);
+    }
+    if (overwrite) {
+      w[i] = s;
+    } else {
+      double2 o = w[i];
+      o.x -= s.x;
+      o.y -= s.y;
+      w[i] = o;
+    }
+  }
+}
+
+int grid_for(long long n, int threads) {
+  long long g = (n + threads - 1) / threads;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long cap = (long long)sms * 8;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
+                                     double2* base_out, cudaStream_t s) {
+  if (L.tiles.empty()) return cudaSuccess;
+  // grid.x = tiles; the 65535 limit applies to grid.y only
+  dim3 grid((unsigned)L.tiles.size(), 1);
+  seg_gemm_fp64_kernel<<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, 0, 0, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_out, cudaStream_t s) {
+  // d_out must hold >= 1 + nblocks doubles: [0] result, [1..] partials
+  int g = grid_for(n, RB);
+  if (g > 1024) g = 1024;
+  dot_partial_kernel<<<g, RB, 0, s>>>(a, b, n, d_out + 1);
+  sum_kernel<<<1, RB, 0, s>>>(d_out + 1, g, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_axpy(double2* y, const double2* x, double a, long long n, cudaStream_t s) {
+  axpy_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, x, a, n);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_scale(double2* y, double a, long long n, cudaStream_t s) {
+  scale_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, a, n);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_dots(const double2* V, int k, long long ld, const double2* w, long long n, double* d_out,
+                        cudaStream_t s) {
+  // d_out: [0, KMAX) results, then nblk*KMAX partials
+  if (k > KMAX) return cudaErrorInvalidValue;
+  int g = grid_for(n, RB);
+  if (g > 512) g = 512;
+  krylov_dots_kernel<<<g, RB, 0, s>>>(V, k, ld, w, n, d_out + KMAX);
+  krylov_reduce_kernel<<<k, 256, 0, s>>>(d_out + KMAX, g, k, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_update(const double2* V, int k, long long ld, double2* w, long long n, const double* d_coef,
+                          cudaStream_t s) {
+  if (k > KMAX) return cudaErrorInvalidValue;
+  krylov_axpy_kernel<<<grid_for(n, 256), 256, 0, s>>>(V, k, ld, w, n, d_coef, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t krylov_combine(const double2* V, int k, long long ld, double2* out, long long n, const double* d_coef,
+                           cudaStream_t s) {
+  if (k > KMAX) return cudaErrorInvalidValue;
+  krylov_axpy_kernel<<<grid_for(n, 256), 256, 0, s>>>(V, k, ld, out, n, d_coef, 1);
+  return cudaGetLastError();
+}
+
+}  // namespace hh

@@ -1,0 +1,731 @@
+// C ABI of the superblock step: context, operators, bases, waves, the
+// model_wave plan, the matvec and the Lanczos driver.
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <algorithm>
+#include <new>
+
+#include "hh_internal.h"
+
+namespace hh {
+
+int fail(hh_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return HH_OK;
+  return fail(ctx, e == cudaErrorMemoryAllocation ? HH_ERR_NOMEM : HH_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static int ensure_red(hh_ctx* ctx, size_t ndouble) {
+  if (ctx->red_cap >= ndouble) return HH_OK;
+  if (ctx->d_red) cudaFree(ctx->d_red);
+  ctx->d_red = nullptr;
+  ctx->red_cap = 0;
+  cudaError_t e = cudaMalloc(&ctx->d_red, ndouble * sizeof(double));
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(reduction)");
+  ctx->red_cap = ndouble;
+  return HH_OK;
+}
+
+static int ensure_hred(hh_ctx* ctx, size_t ndouble) {
+  if (ctx->h_red_cap >= ndouble) return HH_OK;
+  if (ctx->h_red) cudaFreeHost(ctx->h_red);
+  ctx->h_red = nullptr;
+  ctx->h_red_cap = 0;
+  cudaError_t e = cudaMallocHost(&ctx->h_red, ndouble * sizeof(double));
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMallocHost(reduction)");
+  ctx->h_red_cap = ndouble;
+  return HH_OK;
+}
+
+}  // namespace hh
+
+void hh_gemm_list::upload(cudaStream_t s) {
+  release();
+  if (!segs.empty()) {
+    cudaMalloc(&d_segs, segs.size() * sizeof(hh_seg));
+    cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(hh_seg), cudaMemcpyHostToDevice, s);
+  }
+  if (!tiles.empty()) {
+    cudaMalloc(&d_tiles, tiles.size() * sizeof(hh_tile));
+    cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(hh_tile), cudaMemcpyHostToDevice, s);
+  }
+}
+
+void hh_gemm_list::release() {
+  if (d_segs) cudaFree(d_segs);
+  if (d_tiles) cudaFree(d_tiles);
+  d_segs = nullptr;
+  d_tiles = nullptr;
+}
+
+namespace hh {
+
+// Lowest eigenpair of a symmetric tridiagonal matrix (diagonal alpha, off-
+// diagonal beta[0..n-2]) by the implicit QL method with Wilkinson shifts
+// (Bowdler, Martin, Reinsch and Wilkinson, "The QR and QL algorithms for
+// symmetric matrices", Numer. Math. 11 (1968)); z receives the normalised
+// eigenvector.  Replaces the DSTEV calls of code/lanczos.f90:99,118,142.
+int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z) {
+  if (n <= 0) return HH_ERR_INVALID;
+  std::vector<double> d(alpha, alpha + n), e(n, 0.0), Z((size_t)n * n, 0.0);
+  for (int i = 0; i + 1 < n; ++i) e[i] = beta[i];
+  for (int i = 0; i < n; ++i) Z[(size_t)i * n + i] = 1.0;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0;
+    while (true) {
+      int m = l;
+      for (; m < n - 1; ++m) {
+        double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) <= 1e-300 + 2.2204460492503131e-16 * dd) break;
+      }
+      if (m == l) break;
+      if (++iter > 200) return HH_ERR_NUMERIC;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
+      double s = 1.0, c = 1.0, p = 0.0;
+      int i = m - 1;
+      bool early = false;
+      for (; i >= l; --i) {
+        double f = s * e[i], b = c * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] -= p;
+          e[m] = 0.0;
+          early = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+        for (int k = 0; k < n; ++k) {
+          double zf = Z[(size_t)(i + 1) * n + k];
+          Z[(size_t)(i + 1) * n + k] = s * Z[(size_t)i * n + k] + c * zf;
+          Z[(size_t)i * n + k] = c * Z[(size_t)i * n + k] - s * zf;
+        }
+      }
+      if (early) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  int imin = 0;
+  for (int i = 1; i < n; ++i)
+    if (d[i] < d[imin]) imin = i;
+  *e0 = d[imin];
+  if (z) {
+    double nrm = 0.0;
+    for (int k = 0; k < n; ++k) nrm += Z[(size_t)imin * n + k] * Z[(size_t)imin * n + k];
+    nrm = std::sqrt(nrm);
+    for (int k = 0; k < n; ++k) z[k] = Z[(size_t)imin * n + k] / nrm;
+  }
+  return HH_OK;
+}
+
+}  // namespace hh
+
+using namespace hh;
+
+void hh_block::build_index() {
+  idx2.clear();
+  idx3.clear();
+  for (int j = int(subs.size()) - 1; j >= 0; --j) {
+    idx2[key2(subs[j].up, subs[j].down)] = j;
+    idx3[key3(subs[j].up, subs[j].down, subs[j].dd)] = j;
+  }
+}
+
+extern "C" {
+
+int hh_version(void) { return 100; }
+
+const char* hh_status_string(int status) {
+  switch (status) {
+    case HH_OK: return "ok";
+    case HH_ERR_INVALID: return "invalid argument";
+    case HH_ERR_CUDA: return "CUDA error";
+    case HH_ERR_NOMEM: return "out of memory";
+    case HH_ERR_QN: return "quantum number mismatch";
+    case HH_ERR_TIMEOUT: return "bounded device wait timed out";
+    case HH_ERR_NUMERIC: return "numerical failure";
+    case HH_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int hh_init(int device, hh_ctx_t** out) {
+  if (!out) return HH_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return HH_ERR_CUDA;
+  if (device < 0 || device >= n) return HH_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return HH_ERR_CUDA;
+  hh_ctx* c = new (std::nothrow) hh_ctx();
+  if (!c) return HH_ERR_NOMEM;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return HH_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return HH_OK;
+}
+
+int hh_finalize(hh_ctx_t* ctx) {
+  if (!ctx) return HH_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->d_red) cudaFree(ctx->d_red);
+  if (ctx->h_red) cudaFreeHost(ctx->h_red);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HH_OK;
+}
+
+const char* hh_last_error(const hh_ctx_t* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+int hh_ctx_stream(hh_ctx_t* ctx, void** stream) {
+  if (!ctx || !stream) return HH_ERR_INVALID;
+  *stream = (void*)ctx->stream;
+  return HH_OK;
+}
+
+int hh_ctx_sync(hh_ctx_t* ctx) {
+  if (!ctx) return HH_ERR_INVALID;
+  return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+}
+
+// ------------------------------------------------------------------ blocks
+static int block_alloc(hh_ctx* ctx, int len, int up_dif, int down_dif, int nsub, const int* sub_qn,
+                       hh_block** out) {
+  if (!ctx || !out || nsub < 0 || (nsub > 0 && !sub_qn)) return HH_ERR_INVALID;
+  hh_block* b = new (std::nothrow) hh_block();
+  if (!b) return fail(ctx, HH_ERR_NOMEM, "host allocation");
+  b->ctx = ctx;
+  b->len = len;
+  b->up_dif = up_dif;
+  b->down_dif = down_dif;
+  long long off = 0;
+  b->subs.resize(nsub);
+  for (int i = 0; i < nsub; ++i) {
+    hh_sub_qn& s = b->subs[i];
+    s.up = sub_qn[5 * i];
+    s.down = sub_qn[5 * i + 1];
+    s.dd = sub_qn[5 * i + 2];
+    s.row = sub_qn[5 * i + 3];
+    s.sdim = sub_qn[5 * i + 4];
+    if (s.row < 0 || s.sdim < 0) {
+      delete b;
+      return fail(ctx, HH_ERR_INVALID, "negative sub-block dimension");
+    }
+    s.off = off;
+    off += (long long)s.row * s.sdim;
+  }
+  b->nelem = off;
+  b->build_index();
+  if (off > 0) {
+    cudaError_t e = cudaMalloc(&b->d, off * sizeof(double2));
+    if (e != cudaSuccess) {
+      delete b;
+      return cuda_check(ctx, e, "cudaMalloc(block)");
+    }
+  }
+  *out = b;
+  return HH_OK;
+}
+
+int hh_block_create(hh_ctx_t* ctx, int len, int up_dif, int down_dif, int nsub, const int* sub_qn,
+                    const double* data, hh_block_t** out) {
+  int st = block_alloc(ctx, len, up_dif, down_dif, nsub, sub_qn, out);
+  if (st != HH_OK) return st;
+  hh_block* b = *out;
+  if (b->nelem > 0) {
+    if (!data) {
+      hh_block_free(b);
+      *out = nullptr;
+      return fail(ctx, HH_ERR_INVALID, "block data pointer is NULL");
+    }
+    cudaError_t e = cudaMemcpyAsync(b->d, data, b->nelem * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+      hh_block_free(b);
+      *out = nullptr;
+      return cuda_check(ctx, e, "upload block");
+    }
+  }
+  b->scalar.assign(b->subs.size(), cplx(0, 0));
+  for (size_t i = 0; i < b->subs.size(); ++i) {
+    const auto& s = b->subs[i];
+    if (s.row == 1 && s.sdim == 1) b->scalar[i] = cplx(data[2 * s.off], data[2 * s.off + 1]);
+  }
+  return HH_OK;
+}
+
+int hh_block_zeros(hh_ctx_t* ctx, int len, int up_dif, int down_dif, int nsub, const int* sub_qn,
+                   hh_block_t** out) {
+  int st = block_alloc(ctx, len, up_dif, down_dif, nsub, sub_qn, out);
+  if (st != HH_OK) return st;
+  hh_block* b = *out;
+  if (b->nelem > 0) {
+    cudaError_t e = cudaMemsetAsync(b->d, 0, b->nelem * sizeof(double2), ctx->stream);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "memset block");
+  }
+  b->scalar.assign(b->subs.size(), cplx(0, 0));
+  return HH_OK;
+}
+
+int hh_block_info(const hh_block_t* b, int* len, int* up_dif, int* down_dif, int* nsub, long long* nelem) {
+  if (!b) return HH_ERR_INVALID;
+  if (len) *len = b->len;
+  if (up_dif) *up_dif = b->up_dif;
+  if (down_dif) *down_dif = b->down_dif;
+  if (nsub) *nsub = (int)b->subs.size();
+  if (nelem) *nelem = b->nelem;
+  return HH_OK;
+}
+
+int hh_block_qn(const hh_block_t* b, int* q) {
+  if (!b || !q) return HH_ERR_INVALID;
+  for (size_t i = 0; i < b->subs.size(); ++i) {
+    q[5 * i] = b->subs[i].up;
+    q[5 * i + 1] = b->subs[i].down;
+    q[5 * i + 2] = b->subs[i].dd;
+    q[5 * i + 3] = b->subs[i].row;
+    q[5 * i + 4] = b->subs[i].sdim;
+  }
+  return HH_OK;
+}
+
+int hh_block_download(const hh_block_t* b, double* data) {
+  if (!b || (!data && b->nelem > 0)) return HH_ERR_INVALID;
+  if (b->nelem == 0) return HH_OK;
+  cudaError_t e = cudaMemcpyAsync(data, b->d, b->nelem * sizeof(double2), cudaMemcpyDeviceToHost, b->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+  return cuda_check(b->ctx, e, "download block");
+}
+
+int hh_block_free(hh_block_t* b) {
+  if (!b) return HH_ERR_INVALID;
+  if (b->d) {
+    cudaStreamSynchronize(b->ctx->stream);
+    cudaFree(b->d);
+  }
+  delete b;
+  return HH_OK;
+}
+
+namespace {
+__global__ void caxpy_kernel(double2* y, const double2* x, double cr, double ci, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = x[i], o = y[i];
+    o.x += cr * v.x - ci * v.y;
+    o.y += cr * v.y + ci * v.x;
+    y[i] = o;
+  }
+}
+}  // namespace
+
+int hh_block_add(hh_block_t* dst, const double* coef, const hh_block_t* src) {
+  if (!dst || !src || !coef) return HH_ERR_INVALID;
+  hh_ctx* ctx = dst->ctx;
+  // forward scan of block_add_block_two (code/space_info.f90:176-214)
+  size_t x1 = 0;
+  for (size_t i = 0; i < dst->subs.size(); ++i) {
+    const hh_sub_qn& ns = dst->subs[i];
+    for (size_t x = x1; x < src->subs.size(); ++x) {
+      const hh_sub_qn& s = src->subs[x];
+      if (s.up == ns.up && s.down == ns.down && s.dd == ns.dd) {
+        x1 = x + 1;
+        if (s.row != ns.row || s.sdim != ns.sdim)
+          return fail(ctx, HH_ERR_QN, "hh_block_add: sub-block shapes differ");
+        long long n = (long long)s.row * s.sdim;
+        if (n > 0) {
+          int g = (int)std::min<long long>((n + 255) / 256, 4096);
+          caxpy_kernel<<<g, 256, 0, ctx->stream>>>(dst->d + ns.off, src->d + s.off, coef[0], coef[1], n);
+        }
+        if (ns.row == 1 && ns.sdim == 1 && !src->scalar.empty() && !dst->scalar.empty())
+          dst->scalar[i] += cplx(coef[0], coef[1]) * src->scalar[x];
+        break;
+      }
+    }
+  }
+  return cuda_check(ctx, cudaGetLastError(), "hh_block_add");
+}
+
+// ------------------------------------------------------------------ bases
+int hh_basis_create(hh_ctx_t* ctx, int len, int nsec, const int* sec, const int* subs, hh_basis_t** out) {
+  if (!ctx || !out || nsec < 0 || (nsec > 0 && (!sec || !subs))) return HH_ERR_INVALID;
+  hh_basis* b = new (std::nothrow) hh_basis();
+  if (!b) return HH_ERR_NOMEM;
+  b->ctx = ctx;
+  b->len = len;
+  b->secs.resize(nsec);
+  int p = 0;
+  for (int i = 0; i < nsec; ++i) {
+    hh_bsec& s = b->secs[i];
+    s.up = sec[3 * i];
+    s.down = sec[3 * i + 1];
+    int ns = sec[3 * i + 2];
+    s.dim = 0;
+    s.subs.resize(ns);
+    for (int j = 0; j < ns; ++j, ++p) {
+      hh_bsub& u = s.subs[j];
+      u.spos = subs[6 * p];
+      u.sdim = subs[6 * p + 1];
+      u.bu = subs[6 * p + 2];
+      u.bd = subs[6 * p + 3];
+      u.su = subs[6 * p + 4];
+      u.sd = subs[6 * p + 5];
+      if (u.spos != s.dim || u.sdim < 0) {
+        delete b;
+        return fail(ctx, HH_ERR_INVALID, "basis sub-block offsets are not contiguous");
+      }
+      s.dim += u.sdim;
+    }
+    for (int j = ns - 1; j >= 0; --j) {
+      const hh_bsub& u = s.subs[j];
+      s.full[key4(u.bu, u.bd, u.su, u.sd)] = j;
+      s.bl[key2(u.bu, u.bd)] = j;
+    }
+  }
+  for (int i = nsec - 1; i >= 0; --i) b->idx[key2(b->secs[i].up, b->secs[i].down)] = i;
+  *out = b;
+  return HH_OK;
+}
+
+int hh_basis_free(hh_basis_t* b) {
+  if (!b) return HH_ERR_INVALID;
+  delete b;
+  return HH_OK;
+}
+
+// ------------------------------------------------------------------- waves
+int hh_wave_create(hh_ctx_t* ctx, int sys_len, int env_len, int nsec, const int* sec, int nbatch, hh_wave_t** out) {
+  if (!ctx || !out || nsec < 0 || (nsec > 0 && !sec) || nbatch < 1) return HH_ERR_INVALID;
+  hh_wave* w = new (std::nothrow) hh_wave();
+  if (!w) return HH_ERR_NOMEM;
+  w->ctx = ctx;
+  w->sys_len = sys_len;
+  w->env_len = env_len;
+  w->nbatch = nbatch;
+  w->secs.resize(nsec);
+  long long off = 0;
+  for (int i = 0; i < nsec; ++i) {
+    hh_wsec& s = w->secs[i];
+    s.su = sec[6 * i];
+    s.sd = sec[6 * i + 1];
+    s.eu = sec[6 * i + 2];
+    s.ed = sec[6 * i + 3];
+    s.sdim = sec[6 * i + 4];
+    s.edim = sec[6 * i + 5];
+    if (s.sdim < 0 || s.edim < 0) {
+      delete w;
+      return fail(ctx, HH_ERR_INVALID, "negative wave sector dimension");
+    }
+    s.off = off;
+    off += (long long)s.sdim * s.edim;
+  }
+  for (int i = nsec - 1; i >= 0; --i)
+    w->idx[key4(w->secs[i].su, w->secs[i].sd, w->secs[i].eu, w->secs[i].ed)] = i;
+  w->nelem = off;
+  if (off > 0) {
+    cudaError_t e = cudaMalloc(&w->d, (size_t)off * nbatch * sizeof(double2));
+    if (e != cudaSuccess) {
+      delete w;
+      return cuda_check(ctx, e, "cudaMalloc(wave)");
+    }
+    cudaMemsetAsync(w->d, 0, (size_t)off * nbatch * sizeof(double2), ctx->stream);
+  }
+  *out = w;
+  return HH_OK;
+}
+
+int hh_wave_info(const hh_wave_t* w, long long* nelem, int* nbatch) {
+  if (!w) return HH_ERR_INVALID;
+  if (nelem) *nelem = w->nelem;
+  if (nbatch) *nbatch = w->nbatch;
+  return HH_OK;
+}
+
+int hh_wave_upload(hh_wave_t* w, const double* data) {
+  if (!w || (!data && w->nelem > 0)) return HH_ERR_INVALID;
+  size_t bytes = (size_t)w->nelem * w->nbatch * sizeof(double2);
+  if (!bytes) return HH_OK;
+  cudaError_t e = cudaMemcpyAsync(w->d, data, bytes, cudaMemcpyHostToDevice, w->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w->ctx->stream);
+  return cuda_check(w->ctx, e, "upload wave");
+}
+
+int hh_wave_download(const hh_wave_t* w, double* data) {
+  if (!w || (!data && w->nelem > 0)) return HH_ERR_INVALID;
+  size_t bytes = (size_t)w->nelem * w->nbatch * sizeof(double2);
+  if (!bytes) return HH_OK;
+  cudaError_t e = cudaMemcpyAsync(data, w->d, bytes, cudaMemcpyDeviceToHost, w->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w->ctx->stream);
+  return cuda_check(w->ctx, e, "download wave");
+}
+
+int hh_wave_copy(hh_wave_t* dst, const hh_wave_t* src) {
+  if (!dst || !src || dst->nelem * dst->nbatch != src->nelem * src->nbatch) return HH_ERR_INVALID;
+  size_t bytes = (size_t)src->nelem * src->nbatch * sizeof(double2);
+  if (!bytes) return HH_OK;
+  return cuda_check(dst->ctx, cudaMemcpyAsync(dst->d, src->d, bytes, cudaMemcpyDeviceToDevice, dst->ctx->stream),
+                    "copy wave");
+}
+
+int hh_wave_free(hh_wave_t* w) {
+  if (!w) return HH_ERR_INVALID;
+  if (w->d) {
+    cudaStreamSynchronize(w->ctx->stream);
+    cudaFree(w->d);
+  }
+  delete w;
+  return HH_OK;
+}
+
+static int dot_dev(hh_ctx* ctx, const double2* a, const double2* b, long long n, double* out) {
+  int st = ensure_red(ctx, 4096);
+  if (st) return st;
+  st = ensure_hred(ctx, 256);
+  if (st) return st;
+  cudaError_t e = wave_dot(a, b, n, ctx->d_red, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_red, ctx->d_red, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "wave dot");
+  *out = ctx->h_red[0];
+  return HH_OK;
+}
+
+int hh_wave_dot(const hh_wave_t* a, const hh_wave_t* b, double* re) {
+  if (!a || !b || !re || a->nelem != b->nelem) return HH_ERR_INVALID;
+  return dot_dev(a->ctx, a->d, b->d, a->nelem, re);
+}
+
+int hh_wave_norm(const hh_wave_t* a, double* nrm) {
+  if (!a || !nrm) return HH_ERR_INVALID;
+  double s = 0.0;
+  int st = dot_dev(a->ctx, a->d, a->d, a->nelem, &s);
+  if (st) return st;
+  *nrm = std::sqrt(s);
+  return HH_OK;
+}
+
+int hh_wave_normalize(hh_wave_t* a) {
+  if (!a) return HH_ERR_INVALID;
+  double n = 0.0;
+  int st = hh_wave_norm(a, &n);
+  if (st) return st;
+  if (!(n > 0.0) || !std::isfinite(n)) return fail(a->ctx, HH_ERR_NUMERIC, "wave norm is zero or not finite");
+  return cuda_check(a->ctx, wave_scale(a->d, 1.0 / n, a->nelem, a->ctx->stream), "wave scale");
+}
+
+// ------------------------------------------------------------------- plans
+int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* env_bs, const hh_wave_t* layout,
+                   int nterm, const hh_term_t* terms, hh_plan_t** out) {
+  if (!ctx || !sys_bs || !env_bs || !layout || !out || nterm < 0 || (nterm > 0 && !terms)) return HH_ERR_INVALID;
+  *out = nullptr;
+  hh_plan* p = new (std::nothrow) hh_plan();
+  if (!p) return HH_ERR_NOMEM;
+  p->ctx = ctx;
+  p->layout = layout;
+  p->nelem = layout->nelem;
+  int st = build_plan(ctx, sys_bs, env_bs, layout, nterm, terms, p);
+  if (st != HH_OK) {
+    delete p;
+    return st;
+  }
+  if (p->scratch_elems > 0) {
+    cudaError_t e = cudaMalloc(&p->d_scratch, (size_t)p->scratch_elems * layout->nbatch * sizeof(double2));
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_check(ctx, e, "cudaMalloc(plan scratch)");
+    }
+  }
+  p->stage1.upload(ctx->stream);
+  p->stage2.upload(ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    hh_plan_free(p);
+    return cuda_check(ctx, e, "upload plan");
+  }
+  *out = p;
+  return HH_OK;
+}
+
+int hh_plan_stats(const hh_plan_t* p, double* c) {
+  if (!p || !c) return HH_ERR_INVALID;
+  c[0] = p->ref_flops;
+  c[1] = p->exec_flops;
+  c[2] = (double)p->stage2.tiles.size() + (double)p->stage1.tiles.size();
+  c[3] = (double)p->stage2.segs.size();
+  c[4] = (double)p->stage1.segs.size();
+  c[5] = (double)p->scratch_elems * 16.0;
+  c[6] = p->op_bytes;
+  c[7] = 2.0 * 16.0 * (double)p->nelem;
+  return HH_OK;
+}
+
+int hh_plan_free(hh_plan_t* p) {
+  if (!p) return HH_ERR_INVALID;
+  cudaStreamSynchronize(p->ctx->stream);
+  p->stage1.release();
+  p->stage2.release();
+  if (p->d_scratch) cudaFree(p->d_scratch);
+  if (p->d_krylov) cudaFree(p->d_krylov);
+  delete p;
+  return HH_OK;
+}
+
+static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision) {
+  hh_ctx* ctx = p->ctx;
+  if (precision != HH_PREC_FP64 && precision != HH_PREC_BF16X3)
+    return fail(ctx, HH_ERR_INVALID, "unknown precision");
+  if (precision == HH_PREC_BF16X3)
+    return fail(ctx, HH_ERR_UNSUPPORTED, "split-precision matvec is not built into this library");
+  cudaError_t e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
+  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
+  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
+  return cuda_check(ctx, e, "matvec");
+}
+
+int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision) {
+  if (!p || !in || !out) return HH_ERR_INVALID;
+  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out)
+    return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
+  return matvec_dev(p, in->d, out->d, precision);
+}
+
+int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision) {
+  if (!p || !in || !out) return HH_ERR_INVALID;
+  hh_ctx* ctx = p->ctx;
+  size_t bytes = (size_t)p->nelem * sizeof(double2);
+  double2 *din = nullptr, *dout = nullptr;
+  cudaError_t e = cudaMalloc(&din, bytes ? bytes : 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dout, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    if (din) cudaFree(din);
+    return cuda_check(ctx, e, "cudaMalloc(matvec_host)");
+  }
+  e = cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  int st = HH_OK;
+  if (e == cudaSuccess) st = matvec_dev(p, din, dout, precision);
+  if (e == cudaSuccess && st == HH_OK) e = cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(din);
+  cudaFree(dout);
+  if (st != HH_OK) return st;
+  return cuda_check(ctx, e, "matvec_host");
+}
+
+// ----------------------------------------------------------------- Lanczos
+int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int precision, double* energy,
+               int* iterations) {
+  if (!p || !psi || !energy || psi->nelem != p->nelem || maxit < 1) return HH_ERR_INVALID;
+  hh_ctx* ctx = p->ctx;
+  if (maxit > 100) maxit = 100;  // loop_in (code/lanczos.f90:14)
+  const long long n = p->nelem;
+  const int slots = maxit + 1;
+  if (p->krylov_cap < slots) {
+    if (p->d_krylov) cudaFree(p->d_krylov);
+    p->d_krylov = nullptr;
+    p->krylov_cap = 0;
+    cudaError_t e = cudaMalloc(&p->d_krylov, (size_t)slots * n * sizeof(double2));
+    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(Krylov basis)");
+    p->krylov_cap = slots;
+  }
+  int st = ensure_red(ctx, 128 + 600 * 128);
+  if (st) return st;
+  st = ensure_hred(ctx, 256);
+  if (st) return st;
+  double2* V = p->d_krylov;
+  cudaStream_t s = ctx->stream;
+  auto slot = [&](int j) { return V + (size_t)j * n; };
+  auto dot = [&](const double2* a, const double2* b, double* r) { return dot_dev(ctx, a, b, n, r); };
+  std::vector<double> alpha, beta, vv;
+  cudaError_t e = cudaMemcpyAsync(slot(0), psi->d, n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos copy");
+  double nrm2 = 0.0;
+  if ((st = dot(slot(0), slot(0), &nrm2))) return st;
+  if (!(nrm2 > 0.0)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos start vector is zero");
+  wave_scale(slot(0), 1.0 / std::sqrt(nrm2), n, s);
+  if ((st = dot(slot(0), slot(0), &nrm2))) return st;
+  vv.push_back(nrm2);
+  int last = 1;
+  if ((st = matvec_dev(p, slot(0), slot(1), precision))) return st;
+  double a0 = 0.0;
+  if ((st = dot(slot(0), slot(1), &a0))) return st;
+  alpha.push_back(a0);
+  double ritz = a0;
+  while (last < maxit) {
+    // three-term recurrence (code/lanczos.f90:65-75)
+    wave_axpy(slot(last), slot(last - 1), -alpha[last - 1], n, s);
+    if (last >= 2) wave_axpy(slot(last), slot(last - 2), -beta[last - 2], n, s);
+    double b2 = 0.0;
+    if ((st = dot(slot(last), slot(last), &b2))) return st;
+    double b = std::sqrt(b2);
+    beta.push_back(b);
+    if (!std::isfinite(b)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos: non-finite beta");
+    if (std::fabs(b) <= lanzero) break;  // breakdown (code/lanczos.f90:78)
+    wave_scale(slot(last), 1.0 / b, n, s);
+    // Gram-Schmidt against all previous vectors, real inner product
+    // (Gram_Schmidt_process, code/space_info.f90:1176-1214)
+    e = krylov_dots(V, last, n, slot(last), n, ctx->d_red, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_red, ctx->d_red, last * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos reorthogonalisation");
+    for (int j = 0; j < last; ++j) ctx->h_red[j] /= vv[j];
+    e = cudaMemcpyAsync(ctx->d_red, ctx->h_red, last * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = krylov_update(V, last, n, slot(last), n, ctx->d_red, s);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos reorthogonalisation");
+    double w2 = 0.0;
+    if ((st = dot(slot(last), slot(last), &w2))) return st;
+    wave_scale(slot(last), 1.0 / std::sqrt(w2), n, s);
+    if ((st = dot(slot(last), slot(last), &w2))) return st;
+    vv.push_back(w2);
+    ++last;
+    if ((st = matvec_dev(p, slot(last - 1), slot(last), precision))) return st;
+    double al = 0.0;
+    if ((st = dot(slot(last - 1), slot(last), &al))) return st;
+    alpha.push_back(al);
+    double d0 = 0.0;
+    if ((st = tridiag_lowest(last, alpha.data(), beta.data(), &d0, nullptr)))
+      return fail(ctx, st, "tridiagonal eigensolver did not converge");
+    if (std::fabs(d0 - ritz) <= lanzero || last == maxit) {  // code/lanczos.f90:102
+      ritz = d0;
+      break;
+    }
+    ritz = d0;
+  }
+  std::vector<double> z(last);
+  double e0 = 0.0;
+  if ((st = tridiag_lowest(last, alpha.data(), beta.data(), &e0, z.data())))
+    return fail(ctx, st, "tridiagonal eigensolver did not converge");
+  e = cudaMemcpyAsync(ctx->d_red, z.data(), last * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = krylov_combine(V, last, n, psi->d, n, ctx->d_red, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos final combination");
+  if ((st = hh_wave_normalize(psi))) return st;
+  if (precision != HH_PREC_FP64) {
+    // FP64 Rayleigh quotient of the split-precision ground state
+    if ((st = matvec_dev(p, psi->d, slot(0), HH_PREC_FP64))) return st;
+    if ((st = dot(psi->d, slot(0), &e0))) return st;
+  }
+  *energy = e0;
+  if (iterations) *iterations = last;
+  return HH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// Internal types of the GB300 superblock-step library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+#include <unordered_map>
+#include <complex>
+
+#include "../../include/hh_dmrg.h"
+
+namespace hh {
+
+using cplx = std::complex<double>;
+
+// ---------------------------------------------------------------------------
+// Hash of small integer tuples used for the quantum-number lookups.
+static inline uint64_t key2(int a, int b) {
+  return (uint64_t(uint32_t(a)) << 32) | uint32_t(b);
+}
+static inline uint64_t key3(int a, int b, int c) {
+  return (uint64_t(uint32_t(a) & 0xFFFFF) << 40) | (uint64_t(uint32_t(b) & 0xFFFFF) << 20) |
+         uint64_t(uint32_t(c) & 0xFFFFF);
+}
+static inline uint64_t key4(int a, int b, int c, int d) {
+  return (uint64_t(uint16_t(a)) << 48) | (uint64_t(uint16_t(b)) << 32) |
+         (uint64_t(uint16_t(c)) << 16) | uint64_t(uint16_t(d));
+}
+
+}  // namespace hh
+
+struct hh_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int sm_count = 0;
+  // scratch reused by reductions (device)
+  double* d_red = nullptr;
+  size_t red_cap = 0;
+  double* h_red = nullptr;  // pinned
+  size_t h_red_cap = 0;
+};
+
+struct hh_sub_qn {
+  int up, down, dd, row, sdim;
+  long long off;  // element offset (complex) of the sub matrix in the block data
+};
+
+struct hh_block {
+  hh_ctx* ctx = nullptr;
+  int len = 0, up_dif = 0, down_dif = 0;
+  std::vector<hh_sub_qn> subs;
+  long long nelem = 0;
+  double2* d = nullptr;
+  // host copy of the 1x1 entries (site operators are used as scalars)
+  std::vector<hh::cplx> scalar;
+  std::unordered_map<uint64_t, int> idx2, idx3;
+  void build_index();
+  int find2(int up, int down) const {
+    auto it = idx2.find(hh::key2(up, down));
+    return it == idx2.end() ? -1 : it->second;
+  }
+  int find3(int up, int down, int dd) const {
+    auto it = idx3.find(hh::key3(up, down, dd));
+    return it == idx3.end() ? -1 : it->second;
+  }
+};
+
+struct hh_bsub { int spos, sdim, bu, bd, su, sd; };
+struct hh_bsec {
+  int up, down, dim;
+  std::vector<hh_bsub> subs;
+  std::unordered_map<uint64_t, int> full, bl;
+};
+
+struct hh_basis {
+  hh_ctx* ctx = nullptr;
+  int len = 0;
+  std::vector<hh_bsec> secs;
+  std::unordered_map<uint64_t, int> idx;
+  int find(int up, int down) const {
+    auto it = idx.find(hh::key2(up, down));
+    return it == idx.end() ? -1 : it->second;
+  }
+};
+
+struct hh_wsec { int su, sd, eu, ed, sdim, edim; long long off; };
+
+struct hh_wave {
+  hh_ctx* ctx = nullptr;
+  int sys_len = 0, env_len = 0, nbatch = 1;
+  std::vector<hh_wsec> secs;
+  long long nelem = 0;  // per vector
+  double2* d = nullptr; // nbatch * nelem
+  std::unordered_map<uint64_t, int> idx;
+  int find(int su, int sd, int eu, int ed) const {
+    auto it = idx.find(hh::key4(su, sd, eu, ed));
+    return it == idx.end() ? -1 : it->second;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Device task list of the grouped segment GEMM.
+//
+// A tile owns a rectangle of an output matrix (one elementary output
+// sub-block of a wave sector, an intermediate product, a density matrix ...)
+// and accumulates  sum_s coef_s * opP(P_s) * opQ(Q_s)  over its segments; a
+// copy segment adds coef_s * P_s.  Operand addresses are either absolute
+// (operators) or offsets into one of the per-launch bases.
+enum : int { HH_BASE_ABS = 0, HH_BASE_IN = 1, HH_BASE_SCR = 2, HH_BASE_OUT = 3 };
+enum : int { HH_OP_N = 0, HH_OP_C = 1, HH_OP_T = 2 };
+enum : int { HH_SEG_GEMM = 0, HH_SEG_COPY = 1 };
+
+struct hh_seg {
+  long long poff, qoff;   // element offsets (complex) or absolute addresses
+  int pbase, qbase;
+  int ldp, ldq;
+  int opP, opQ;
+  int K;
+  int kind;
+  double cre, cim;
+};
+
+struct hh_tile {
+  long long ooff;  // element offset of the rectangle origin in the output base
+  int obase;
+  int ldo;
+  int M, N;        // rectangle extent
+  int m0, n0;      // tile origin inside the rectangle
+  int seg0, nseg;
+  int accumulate;  // 1: out += acc, 0: out = acc
+};
+
+struct hh_gemm_list {
+  std::vector<hh_seg> segs;
+  std::vector<hh_tile> tiles;
+  hh_seg* d_segs = nullptr;
+  hh_tile* d_tiles = nullptr;
+  double flops = 0.0;
+  void upload(cudaStream_t s);
+  void release();
+};
+
+struct hh_plan {
+  hh_ctx* ctx = nullptr;
+  const hh_wave* layout = nullptr;
+  long long nelem = 0;
+  hh_gemm_list stage1, stage2;
+  long long scratch_elems = 0;
+  double2* d_scratch = nullptr;
+  double ref_flops = 0.0, exec_flops = 0.0;
+  double op_bytes = 0.0;
+  std::vector<const hh_block*> ops;
+  // Lanczos workspace
+  double2* d_krylov = nullptr;
+  int krylov_cap = 0;
+};
+
+namespace hh {
+int fail(hh_ctx* ctx, int code, const std::string& msg);
+int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what);
+// grouped segment GEMM (FP64); bases[4] = {abs(unused), in, scr, out}
+cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
+                                     double2* base_out, cudaStream_t s);
+// wave vector kernels
+cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_out, cudaStream_t s);
+cudaError_t wave_axpy(double2* y, const double2* x, double a, long long n, cudaStream_t s);
+cudaError_t wave_scale(double2* y, double a, long long n, cudaStream_t s);
+cudaError_t krylov_dots(const double2* V, int k, long long ld, const double2* w, long long n,
+                        double* d_out, cudaStream_t s);
+cudaError_t krylov_update(const double2* V, int k, long long ld, double2* w, long long n,
+                          const double* d_coef, cudaStream_t s);
+cudaError_t krylov_combine(const double2* V, int k, long long ld, double2* out, long long n,
+                           const double* d_coef, cudaStream_t s);
+int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wave* layout,
+               int nterm, const hh_term_t* terms, hh_plan* plan);
+double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
+int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
+}  // namespace hh

@@ -1,0 +1,160 @@
+/*
+ * hh_dmrg.h -- C ABI of the GB300 superblock step of the SU(2) block DMRG.
+ *
+ * The entry points replace the hot-path subroutines of the Fortran code in
+ * cfengno1/Hofstadter_Hubbard_TSC (paths below are inside that project).  A
+ * Fortran caller binds them with ISO_C_BINDING; every argument is a plain
+ * pointer, an int or a double.  Complex data are interleaved (re, im) doubles,
+ * sub-blocks column-major exactly as the Fortran arrays are laid out, so the
+ * caller passes its own buffers without reshuffling.
+ *
+ * Conventions
+ *   - every call returns an int status: HH_OK (0) or a negative HH_ERR_* code;
+ *     hh_last_error() returns a message for the last failure in a context;
+ *   - the library owns device memory; the caller owns host buffers;
+ *   - all work of a context runs on one CUDA stream (hh_ctx_stream), calls on
+ *     one context must not overlap from several host threads;
+ *   - quantum numbers follow the reference: num_up = electron number N,
+ *     num_down = 2S, down_dif = change of 2S, up_dif = change of N.
+ */
+#ifndef HH_DMRG_H
+#define HH_DMRG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HH_OK 0
+#define HH_ERR_INVALID (-1)   /* bad argument or handle                          */
+#define HH_ERR_CUDA (-2)      /* CUDA runtime / library failure                  */
+#define HH_ERR_NOMEM (-3)     /* device or host allocation failed                */
+#define HH_ERR_QN (-4)        /* quantum-number mismatch (the reference stops)   */
+#define HH_ERR_TIMEOUT (-5)   /* a bounded device wait ran out                   */
+#define HH_ERR_NUMERIC (-6)   /* eigensolver failure or non-finite result        */
+#define HH_ERR_UNSUPPORTED (-7)
+
+/* precision of the superblock matvec */
+#define HH_PREC_FP64 0        /* complex FP64 on the CUDA cores                   */
+#define HH_PREC_BF16X3 1      /* three-way BF16 split, FP32 accumulate (tcgen05)  */
+
+typedef struct hh_ctx hh_ctx_t;
+typedef struct hh_block hh_block_t;
+typedef struct hh_basis hh_basis_t;
+typedef struct hh_wave hh_wave_t;
+typedef struct hh_plan hh_plan_t;
+
+/* ---------------------------------------------------------------- context */
+int hh_init(int device, hh_ctx_t** ctx);
+int hh_finalize(hh_ctx_t* ctx);
+const char* hh_last_error(const hh_ctx_t* ctx);
+const char* hh_status_string(int status);
+int hh_ctx_stream(hh_ctx_t* ctx, void** stream);   /* cudaStream_t of the context */
+int hh_ctx_sync(hh_ctx_t* ctx);
+int hh_version(void);
+
+/* ----------------------------------------------- Total_Block (operators)
+ * Replaces the in-memory Total_Block of code/pubdata.f90:141-149 with a
+ * device-resident copy.  sub_qn holds 5 ints per sub: num_up, num_down,
+ * down_dif, row_dim, sdim.  data holds the sub matrices back to back, each
+ * row_dim x sdim column-major, interleaved complex.                        */
+int hh_block_create(hh_ctx_t* ctx, int len, int up_dif, int down_dif, int nsub,
+                    const int* sub_qn, const double* data, hh_block_t** out);
+int hh_block_zeros(hh_ctx_t* ctx, int len, int up_dif, int down_dif, int nsub,
+                   const int* sub_qn, hh_block_t** out);
+int hh_block_info(const hh_block_t* b, int* len, int* up_dif, int* down_dif,
+                  int* nsub, long long* nelem);
+int hh_block_qn(const hh_block_t* b, int* sub_qn);
+int hh_block_download(const hh_block_t* b, double* data);
+int hh_block_free(hh_block_t* b);
+/* dst += coef * src sub by sub, matching (num_up, num_down, down_dif) with the
+ * forward scan of block_add_block_two (code/space_info.f90:176-214); hmerge
+ * (code/mat_vec.f90:3623-3852) is a sequence of these calls. coef = {re, im}. */
+int hh_block_add(hh_block_t* dst, const double* coef, const hh_block_t* src);
+
+/* --------------------------------------------- Total_Basis (enlarged blocks)
+ * Replaces Total_Basis (code/pubdata.f90:91-108) as produced by Get_basis
+ * (code/update.f90:11-112).  sec: 3 ints per sector (new_num_up, new_num_down,
+ * number of sub-blocks); subs: 6 ints per sub-block (spos, sdim, bl_num_up,
+ * bl_num_down, st_num_up, st_num_down), sector after sector.               */
+int hh_basis_create(hh_ctx_t* ctx, int len, int nsec, const int* sec,
+                    const int* subs, hh_basis_t** out);
+int hh_basis_free(hh_basis_t* b);
+
+/* ---------------------------------------- Wavefunction (super basis layout)
+ * Replaces Wavefunction / Super_Basis (code/pubdata.f90:114-136).  sec: 6 ints
+ * per sector (sys_num_up, sys_num_down, env_num_up, env_num_down, sys_dim,
+ * env_dim).  nbatch independent vectors share the layout (batched matvec). */
+int hh_wave_create(hh_ctx_t* ctx, int sys_len, int env_len, int nsec,
+                   const int* sec, int nbatch, hh_wave_t** out);
+int hh_wave_info(const hh_wave_t* w, long long* nelem, int* nbatch);
+int hh_wave_upload(hh_wave_t* w, const double* data);     /* nbatch*nelem complex */
+int hh_wave_download(const hh_wave_t* w, double* data);
+int hh_wave_copy(hh_wave_t* dst, const hh_wave_t* src);
+int hh_wave_free(hh_wave_t* w);
+/* wave_product (Re<a|b>), wave_norm, wave_normalize (code/space_info.f90:1018-1075) */
+int hh_wave_dot(const hh_wave_t* a, const hh_wave_t* b, double* re);
+int hh_wave_norm(const hh_wave_t* a, double* nrm);
+int hh_wave_normalize(hh_wave_t* a);
+
+/* ------------------------------------------------------------- model_wave
+ * One term of model_wave (code/mat_vec.f90:3476-3620).  kind selects the term
+ * kernel it replaces; op0/op1 are the (sys-side, env-side) operators in the
+ * argument order of that kernel; trans0/trans1 = 1 means the operand is passed
+ * through block_transfer_trans (code/space_info.f90:32-63) first; flag0/flag1
+ * are 'F' (fermion) or 'B' (boson) as in the reference.                    */
+enum hh_term_kind {
+  HH_BLOCK_VEC_DIA = 1,        /* code/mat_vec.f90:165  (op0 = sys block)            */
+  HH_VEC_BLOCK_DIA = 2,        /* code/mat_vec.f90:218  (op0 = env block)            */
+  HH_SITE_VEC_SITE_DIA = 3,    /* code/mat_vec.f90:540  (op0 sys site, op1 env site) */
+  HH_SITE_VEC_SITE_NDIA = 4,   /* code/mat_vec.f90:3101                              */
+  HH_BLOCK_SITE_VEC_NDIA = 5,  /* code/mat_vec.f90:960  (sys block, sys site)        */
+  HH_VEC_BLOCK_SITE_NDIA = 6,  /* code/mat_vec.f90:1219 (env block, env site)        */
+  HH_BLOCK_VEC_SITE_NDIA = 7,  /* code/mat_vec.f90:2324 (sys block, env site)        */
+  HH_SITE_VEC_BLOCK_NDIA = 8,  /* code/mat_vec.f90:2695 (sys site, env block)        */
+  HH_BLOCK_VEC_BLOCK_NDIA = 9, /* code/mat_vec.f90:1505 (sys block, env block)       */
+  HH_BLOCK_SITE_VEC_DIA = 10,  /* code/mat_vec.f90:388                               */
+  HH_VEC_BLOCK_SITE_DIA = 11,  /* code/mat_vec.f90:463                               */
+  HH_BLOCK_VEC_SITE_DIA = 12,  /* code/mat_vec.f90:640                               */
+  HH_SITE_VEC_BLOCK_DIA = 13,  /* code/mat_vec.f90:743                               */
+  HH_BLOCK_VEC_BLOCK_DIA = 14  /* code/mat_vec.f90:846                               */
+};
+
+typedef struct {
+  int kind;
+  int flag0, flag1;            /* 'F' or 'B' (ignored for the _DIA kinds)  */
+  int trans0, trans1;
+  const hh_block_t* op0;
+  const hh_block_t* op1;       /* NULL for the one-operator kinds          */
+  double coef_re, coef_im;
+} hh_term_t;
+
+/* Builds the task list of model_wave for one superblock (the loop nests of the
+ * term kernels, their 6j coefficients, phases and fermion signs), resolved
+ * once and reused by every matvec of a Lanczos call.                       */
+int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* env_bs,
+                   const hh_wave_t* layout, int nterm, const hh_term_t* terms,
+                   hh_plan_t** out);
+/* counts: [0] reference FLOPs per matvec (8MNK over the reference's ZGEMM
+ * calls + 8 per element of the axpy terms), [1] FLOPs this plan executes,
+ * [2] output tiles, [3] segments, [4] stage-1 products, [5] scratch bytes,
+ * [6] operator bytes read per matvec, [7] wave bytes (in + out)            */
+int hh_plan_stats(const hh_plan_t* p, double* counts);
+int hh_plan_free(hh_plan_t* p);
+
+/* model_wave (code/mat_vec.f90:3476): out = H in, device-resident waves.   */
+int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision);
+/* model_wave with host buffers: copies in, multiplies, copies out.         */
+int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision);
+
+/* lanczos_memo_new (code/lanczos.f90:4-177), levels = 1.  psi is the start
+ * vector on entry and the ground state on exit; lanzero is the breakdown and
+ * convergence threshold; maxit <= 100 is loop_in.  With HH_PREC_BF16X3 the
+ * Krylov recurrence runs on the split-precision matvec and the energy is the
+ * FP64 Rayleigh quotient of the final vector.                             */
+int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit,
+               int precision, double* energy, int* iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HH_DMRG_H */

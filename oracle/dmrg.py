@@ -116,6 +116,7 @@ class DMRG:
         self.energies = []
         self.verbose = verbose
         self.last_step = None   # (sys, env, sys_bs, env_bs, geo, wave) of the last solve
+        self.record = None      # optional list: (sys, env, sys_bs, env_bs, geo, sup, start wave) per solve
 
     # ---------------------------------------------------------------------
     def _site_model(self, geo, lat_idx):
@@ -135,6 +136,9 @@ class DMRG:
         return c
 
     def solve(self, sys, env, sys_bs, env_bs, geo, sup, guess):
+        if self.record is not None:
+            self.record.append((self._copy_model(sys), self._copy_model(env), sys_bs, env_bs,
+                                self.lat.geometry(sys.len, env.len), sup, guess.copy()))
         hmerge(sys, env, geo)
 
         def apply_h(v, out):

@@ -1,0 +1,32 @@
+"""Pins the oracle: DMRG with m above the exact dimension reproduces exact
+diagonalisation singlet energies of small flux ladders and cylinders, and the
+free-fermion energy at U=0."""
+import numpy as np
+import pytest
+
+from oracle import ed
+from oracle.lattice import Lattice
+from oracle.dmrg import DMRG
+
+
+def _dmrg(lat, ne, m=256, sweeps=2):
+    d = DMRG(lat, ne, kept_min=m, kept_max=m, trun_err=1e-14, lanzero=1e-11, seed=3)
+    return d.run(sweeps=sweeps), d
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 3, 4, 0.0, 0.25), (2, 4, 6, 0.0, 0.2)])
+def test_free_fermions(W, L, ne, U, phi):
+    lat = Lattice(W, L, U=U, phi=phi)
+    e, _ = _dmrg(lat, ne)
+    assert e == pytest.approx(ed.free_fermion_energy(lat, ne), abs=1e-10)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (4, 2, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_hubbard_exact(W, L, ne, U, phi):
+    lat = Lattice(W, L, U=U, phi=phi)
+    e, d = _dmrg(lat, ne)
+    es, _ = ed.singlet_ground_energy(lat, ne)
+    assert e == pytest.approx(es, abs=1e-9)
+    # every finite-sweep step sees the same ground state
+    finals = [r[2] for r in d.energies[-4:]]
+    assert np.ptp(finals) < 1e-9
