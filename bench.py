@@ -1,0 +1,352 @@
+"""Benchmark of the superblock matvec (model_wave) on one or more GB300s.
+
+Workload: the mid-chain superblock of the Hofstadter-Hubbard cylinder W=4,
+L=32, phi=1/4 (Landau gauge), t=1, U=8, N_e=112 (1/8 hole doping), m=2000
+kept multiplets per block -- the configuration the headline metric is quoted
+on.  Block operators are seeded synthetic N(0,1) data with the sector
+structure of such a step (see hofstadter_hubbard_tsc_gb300/synth.py); the term
+list, 6j coefficients and task structure are the real ones.
+
+One step = one H psi.  ``value`` is matvecs/s with psi and the operators
+resident in HBM (CUDA events on the library's stream, L2 flushed between
+steps); ``e2e`` is the same through the C-ABI call with host buffers
+(hh_matvec_host: pinned H2D copy of psi, matvec, D2H copy of H psi every
+step).  --impl reference times the CPU restatement of the reference's
+model_wave (numpy, all host cores) on the same workload.
+Multi-GPU: replicas only (the step does not exchange data): each rank runs the
+workload, value = sum of matvecs over ranks / max time over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "matvecs/s & sweep time at fixed m, mixed+learned vs FP64 GPU, |dE/E|<=1e-8"
+UNIT = "matvecs/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "bf16x3"])
+    p.add_argument("--m", type=int, default=2000)
+    p.add_argument("--W", type=int, default=4)
+    p.add_argument("--L", type=int, default=32)
+    p.add_argument("--ne", type=int, default=112)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample", type=int, default=1, help="matvecs in the CPU baseline sample")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+        return dist, rank, ws, local
+    return None, rank, ws, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu, self.samples, self.proc = gpu, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for n, v in zip(names, s[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "_fallback": True}
+
+
+def fp64_peak_tflops():
+    """Dense FP64 rate of this GPU, measured with cuBLAS DGEMM (torch.matmul, best of 5)."""
+    try:
+        import torch
+        n = 4096
+        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.matmul(a, b)
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e))
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    except Exception:
+        return None
+
+
+def to_oracle(wl):
+    """The workload in the oracle's types (CPU baseline and parity check only)."""
+    from oracle import blocks as OB
+    from oracle.enlarge import Model
+    from oracle.lattice import Lattice
+
+    def blk(b):
+        return OB.Block(b.len, b.up_dif, b.down_dif,
+                        [OB.Sub(s.num_up, s.num_down, s.down_dif, s.row_dim, s.sdim, s.mat.copy()) for s in b.subs])
+
+    def model(m):
+        om = Model(m.len, blk(m.ham))
+        om.sub = {i: {n: blk(b) for n, b in d.items()} for i, d in m.sub.items()}
+        return om
+
+    def basis(b):
+        ob = OB.Basis(b.len)
+        for s in b.sectors:
+            sec = OB.BSector(s.new_num_up, s.new_num_down)
+            for u in s.subs:
+                sec.subs.append(OB.BSub(u.spos, u.sdim, u.bl_num_up, u.bl_num_down, u.st_num_up, u.st_num_down))
+            sec.dim = s.dim
+            ob.sectors.append(sec)
+        return ob
+
+    lat = Lattice(wl.W, wl.L, U=wl.U, phi=wl.phi)
+    sup = OB.Super(wl.sup.sys_len, wl.sup.env_len,
+                   [OB.SSector(s.sys_num_up, s.sys_num_down, s.env_num_up, s.env_num_down, s.sys_dim, s.env_dim)
+                    for s in wl.sup.subs])
+    return model(wl.sys), model(wl.env), basis(wl.sys_bs), basis(wl.env_bs), lat.geometry(wl.sys.len, wl.env.len), sup
+
+
+def cpu_matvec_timer(wl, psi_flat, nrep):
+    """The oracle's model_wave on the workload; returns (seconds per matvec, H psi)."""
+    from oracle.matvec import hmerge, model_wave
+    from oracle.blocks import allocate_wave
+    from oracle.sites import SiteOps
+    sys_, env, sbs, ebs, geo, sup = to_oracle(wl)
+    hmerge(sys_, env, geo)
+    st = SiteOps("hubbard")
+    vin = allocate_wave(sup)
+    vin.set_flat(psi_flat)
+    vout = allocate_wave(sup)
+    t0 = time.perf_counter()
+    for _ in range(nrep):
+        model_wave(sys_, env, sbs, ebs, vin, vout, geo, st)
+    dt = (time.perf_counter() - t0) / nrep
+    return dt, vout.flat()
+
+
+def run_reference(args, rank, ws, dist):
+    from hofstadter_hubbard_tsc_gb300.synth import Workload
+    if rank != 0:
+        return
+    wl = Workload(W=args.W, L=args.L, n_elec=args.ne, m=args.m)
+    rng = np.random.default_rng(1)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    steps = max(1, min(args.steps, 3))
+    for _ in range(min(args.warmup, 1)):
+        cpu_matvec_timer(wl, psi, 1)
+    dt, _ = cpu_matvec_timer(wl, psi, steps)
+    v = 1.0 / dt
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+            "warmup": min(args.warmup, 1), "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": dict(wl.describe(), **{"timing": "host wall clock per matvec"}),
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{steps} full matvec(s) of the workload (numpy restatement of model_wave, "
+                                       f"OpenBLAS threads = all host cores)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist, rank, ws, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    import ctypes as C
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    from hofstadter_hubbard_tsc_gb300 import _lib
+    from hofstadter_hubbard_tsc_gb300.device import Device, DWave
+    from hofstadter_hubbard_tsc_gb300.superblock import Superblock
+    from hofstadter_hubbard_tsc_gb300.synth import Workload
+
+    prec = _lib.HH_PREC_FP64 if args.precision == "fp64" else _lib.HH_PREC_BF16X3
+    t0 = time.perf_counter()
+    wl = Workload(W=args.W, L=args.L, n_elec=args.ne, m=args.m)
+    dev = Device(local)
+    sb = Superblock(dev, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo, precision=prec)
+    setup_s = time.perf_counter() - t0
+    stats = sb.stats()
+    rng = np.random.default_rng(1 + rank)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    psi /= np.linalg.norm(psi)
+    w_in, w_out = sb.w_in, sb.w_out
+    w_in.upload(psi)
+
+    stream = torch.cuda.ExternalStream(dev.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+    ms = (C.c_float * 3)()
+
+    def step():
+        dev.check(dev.lib.hh_matvec_timed(sb.plan, w_in.h, w_out.h, prec, ms))
+        return ms[0], ms[1], ms[2]
+
+    for _ in range(args.warmup):
+        step()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    tot = s1 = s2 = 0.0
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        a, b, c = step()
+        tot += a
+        s1 += b
+        s2 += c
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_steps = tot / 1e3  # seconds, device time of the K matvecs
+    if dist:
+        t = torch.tensor([t_steps], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_steps = float(t.item())
+    value = ws * args.steps / t_steps
+
+    # end to end through the C-ABI call with pinned host buffers
+    nbytes = wl.sup.dim * 16
+    hin, hout = C.c_void_p(), C.c_void_p()
+    dev.check(dev.lib.hh_host_alloc(nbytes, C.byref(hin)))
+    dev.check(dev.lib.hh_host_alloc(nbytes, C.byref(hout)))
+    hin_np = np.ctypeslib.as_array((C.c_double * (2 * wl.sup.dim)).from_address(hin.value))
+    hout_np = np.ctypeslib.as_array((C.c_double * (2 * wl.sup.dim)).from_address(hout.value))
+    hin_np[:] = psi.view(np.float64)
+    dp = C.POINTER(C.c_double)
+    for _ in range(max(1, args.warmup)):
+        dev.check(dev.lib.hh_matvec_host(sb.plan, C.cast(hin, dp), C.cast(hout, dp), prec))
+    if dist:
+        dist.barrier()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        dev.check(dev.lib.hh_matvec_host(sb.plan, C.cast(hin, dp), C.cast(hout, dp), prec))
+    te = time.perf_counter() - te
+    if dist:
+        t = torch.tensor([te], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    hpsi_gpu = hout_np.view(np.complex128).copy()
+    e2e = {"value": ws * args.steps / te, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+           "timing": "host wall clock around hh_matvec_host (pinned H2D, matvec, D2H, stream sync)"}
+
+    # roofline of the dominant kernel (the stage with more device time)
+    peaks = measured_peaks()
+    stage = 1 if s1 >= s2 else 2
+    t_stage = (s1 if stage == 1 else s2) / args.steps * 1e-3
+    counts = np.zeros(12)
+    dev.check(dev.lib.hh_plan_stats(sb.plan, counts.ctypes.data_as(dp)))
+    flops_stage = counts[8] if stage == 1 else counts[9]
+    achieved = flops_stage / t_stage / 1e12
+    if prec == _lib.HH_PREC_FP64:
+        peak = fp64_peak_tflops()
+        peak_note = "dense FP64 (cuBLAS DGEMM 4096^3, best of 5, measured in this run): GB300 has no FP64 tensor path"
+    else:
+        peak = peaks["bf16_tflops"] / 6.0
+        peak_note = "measured bf16 burst / 6 (three-way split: six bf16 products per real product)"
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if peak else None, "traffic": None,
+                "kernel": f"seg_gemm stage {stage}", "peak_note": peak_note,
+                "algorithmic_flops_per_launch": flops_stage,
+                "kernel_ms_per_launch": t_stage * 1e3}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128" if prec == _lib.HH_PREC_FP64 else "bf16x3(c128 io)",
+            "data": "synthetic",
+            "config": dict(wl.describe(), **{"precision": args.precision, "l2": "flushed between steps (256 MB write)",
+                                             "parallelism": f"replicas x{ws}",
+                                             "ref_gflop_per_matvec": counts[0] / 1e9,
+                                             "exec_gflop_per_matvec": counts[1] / 1e9,
+                                             "plan_setup_s": setup_s}),
+            "roofline": roofline, "e2e": e2e, "clocks": clk,
+            "gpu_launches": args.steps * (2 if prec == _lib.HH_PREC_FP64 else 4)}
+    if rank == 0 and not args.no_cpu_baseline:
+        n = max(1, args.cpu_sample)
+        dt, hpsi_cpu = cpu_matvec_timer(wl, psi, n)
+        rel = float(np.linalg.norm(hpsi_gpu - hpsi_cpu) / np.linalg.norm(hpsi_cpu))
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{n} full matvec(s) of the same workload (numpy restatement of "
+                                          f"model_wave, OpenBLAS on all host cores)"}
+        line["parity_rel_err_vs_oracle"] = rel
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sb.free()
+    dev.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

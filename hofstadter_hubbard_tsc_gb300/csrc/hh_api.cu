@@ -575,6 +575,10 @@ int hh_plan_stats(const hh_plan_t* p, double* c) {
   c[5] = (double)p->scratch_elems * 16.0;
   c[6] = p->op_bytes;
   c[7] = 2.0 * 16.0 * (double)p->nelem;
+  c[8] = p->exec_flops_s1;
+  c[9] = p->exec_flops_s2;
+  c[10] = p->ref_flops_first;
+  c[11] = p->ref_flops - p->ref_flops_first;
   return HH_OK;
 }
 
@@ -585,8 +589,14 @@ int hh_plan_free(hh_plan_t* p) {
   p->stage2.release();
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_krylov) cudaFree(p->d_krylov);
+  if (p->d_host_in) cudaFree(p->d_host_in);
+  if (p->d_host_out) cudaFree(p->d_host_out);
   delete p;
   return HH_OK;
+}
+
+static int matvec_timed_tc(hh_plan* p, const double2* in, double2* out, int precision, float* ms) {
+  return fail(p->ctx, HH_ERR_UNSUPPORTED, "split-precision matvec is not built into this library");
 }
 
 static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision) {
@@ -612,22 +622,53 @@ int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision) {
   if (!p || !in || !out) return HH_ERR_INVALID;
   hh_ctx* ctx = p->ctx;
   size_t bytes = (size_t)p->nelem * sizeof(double2);
-  double2 *din = nullptr, *dout = nullptr;
-  cudaError_t e = cudaMalloc(&din, bytes ? bytes : 16);
-  if (e == cudaSuccess) e = cudaMalloc(&dout, bytes ? bytes : 16);
-  if (e != cudaSuccess) {
-    if (din) cudaFree(din);
-    return cuda_check(ctx, e, "cudaMalloc(matvec_host)");
-  }
-  e = cudaMemcpyAsync(din, in, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e = cudaSuccess;
+  if (!p->d_host_in) e = cudaMalloc(&p->d_host_in, bytes ? bytes : 16);
+  if (e == cudaSuccess && !p->d_host_out) e = cudaMalloc(&p->d_host_out, bytes ? bytes : 16);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(matvec_host)");
+  e = cudaMemcpyAsync(p->d_host_in, in, bytes, cudaMemcpyHostToDevice, ctx->stream);
   int st = HH_OK;
-  if (e == cudaSuccess) st = matvec_dev(p, din, dout, precision);
-  if (e == cudaSuccess && st == HH_OK) e = cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) st = matvec_dev(p, p->d_host_in, p->d_host_out, precision);
+  if (e == cudaSuccess && st == HH_OK)
+    e = cudaMemcpyAsync(out, p->d_host_out, bytes, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  cudaFree(din);
-  cudaFree(dout);
   if (st != HH_OK) return st;
   return cuda_check(ctx, e, "matvec_host");
+}
+
+int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision, float* ms) {
+  if (!p || !in || !out || !ms || in == out || in->nelem != p->nelem || out->nelem != p->nelem)
+    return HH_ERR_INVALID;
+  hh_ctx* ctx = p->ctx;
+  if (precision != HH_PREC_FP64) return matvec_timed_tc(p, in->d, out->d, precision, ms);
+  cudaEvent_t ev[3];
+  for (int i = 0; i < 3; ++i) cudaEventCreate(&ev[i]);
+  cudaError_t e = cudaMemsetAsync(out->d, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
+  cudaEventRecord(ev[0], ctx->stream);
+  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, in->d, p->d_scratch, out->d, ctx->stream);
+  cudaEventRecord(ev[1], ctx->stream);
+  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, in->d, p->d_scratch, out->d, ctx->stream);
+  cudaEventRecord(ev[2], ctx->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
+  if (e == cudaSuccess) {
+    cudaEventElapsedTime(&ms[0], ev[0], ev[2]);
+    cudaEventElapsedTime(&ms[1], ev[0], ev[1]);
+    cudaEventElapsedTime(&ms[2], ev[1], ev[2]);
+  }
+  for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
+  return cuda_check(ctx, e, "matvec_timed");
+}
+
+int hh_host_alloc(long long bytes, void** ptr) {
+  if (!ptr || bytes < 0) return HH_ERR_INVALID;
+  *ptr = nullptr;
+  if (bytes == 0) return HH_OK;
+  return cudaMallocHost(ptr, (size_t)bytes) == cudaSuccess ? HH_OK : HH_ERR_NOMEM;
+}
+
+int hh_host_free(void* ptr) {
+  if (!ptr) return HH_OK;
+  return cudaFreeHost(ptr) == cudaSuccess ? HH_OK : HH_ERR_CUDA;
 }
 
 // ----------------------------------------------------------------- Lanczos

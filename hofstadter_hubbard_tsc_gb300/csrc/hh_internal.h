@@ -151,6 +151,9 @@ struct hh_plan {
   long long scratch_elems = 0;
   double2* d_scratch = nullptr;
   double ref_flops = 0.0, exec_flops = 0.0;
+  double ref_flops_first = 0.0, exec_flops_s1 = 0.0, exec_flops_s2 = 0.0;
+  double2* d_host_in = nullptr;   // device buffers of hh_matvec_host
+  double2* d_host_out = nullptr;
   double op_bytes = 0.0;
   std::vector<const hh_block*> ops;
   // Lanczos workspace

@@ -102,6 +102,7 @@ struct Emitter {
   const hh_wave* w;
   std::vector<Contrib> out;
   double ref_flops = 0.0;
+  double ref_first = 0.0;  // first GEMM of the two-GEMM terms
   std::string err;
 
   const hh_bsec* ssec(int i) const {
@@ -311,6 +312,7 @@ bool t_block_vec_block_dia(Emitter& E, const OpView& A, const OpView& B, cplx co
         Mat am = op_mat(A, a, false), bm = op_mat(B, b, true);
         E.add(i, x.spos, y.spos, x.sdim, y.sdim, i, x.spos, y.spos, x.sdim, y.sdim, &am, &bm, c);
         E.ref_flops += 8.0 * x.sdim * (double)y.sdim * x.sdim + 8.0 * x.sdim * (double)y.sdim * y.sdim;
+        E.ref_first += 8.0 * x.sdim * (double)y.sdim * x.sdim;
       }
     }
   }
@@ -432,11 +434,13 @@ bool t_block_vec_block_ndia(Emitter& E, const OpView& A, int flA, const OpView& 
               E.add(kk, ms->spos, me->spos, ms->sdim, me->sdim, i, m.spos, n.spos, m.sdim, n.sdim,
                     &am, &bm, c);
               E.ref_flops += 8.0 * ms->sdim * (double)n.sdim * m.sdim + 8.0 * ms->sdim * (double)me->sdim * n.sdim;
+              E.ref_first += 8.0 * ms->sdim * (double)n.sdim * m.sdim;
               if (up_dif != 0) {
                 Mat ah = op_mat(A, sb, true), bh = op_mat(B, ebi, true);
                 E.add(i, m.spos, n.spos, m.sdim, n.sdim, kk, ms->spos, me->spos, ms->sdim, me->sdim,
                       &ah, &bh, std::conj(c));
                 E.ref_flops += 8.0 * m.sdim * (double)me->sdim * ms->sdim + 8.0 * m.sdim * (double)n.sdim * me->sdim;
+                E.ref_first += 8.0 * m.sdim * (double)me->sdim * ms->sdim;
               }
             }
           }
@@ -669,6 +673,7 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
     if (T.op1) plan->ops.push_back(T.op1);
   }
   plan->ref_flops = E.ref_flops;
+  plan->ref_flops_first = E.ref_first;
 
   // ------------------------------------------------------------ scheduling
   constexpr int TM = 64, TN = 64;
@@ -676,7 +681,7 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
   long long scr = 0;
   std::map<std::tuple<int, int, int>, std::vector<hh_seg>> rects;  // (k, orow, ocol) -> segs
   std::vector<std::tuple<int, int, int, int, int>> rect_order;     // k, orow, ocol, M, N
-  double exec = 0.0;
+  double exec = 0.0, exec1 = 0.0;
   auto xoff = [&](int i, int r, int c) {
     const hh_wsec& s = layout->secs[i];
     return s.off + (long long)c * s.sdim + r;
@@ -716,6 +721,7 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
             plan->stage1.tiles.push_back(tl);
           }
         exec += 8.0 * t.M * (double)t.Kb * t.Ka;
+        exec1 += 8.0 * t.M * (double)t.Kb * t.Ka;
       } else {
         toff = it->second;
       }
@@ -765,6 +771,8 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
   }
   plan->scratch_elems = scr;
   plan->exec_flops = exec;
+  plan->exec_flops_s1 = exec1;
+  plan->exec_flops_s2 = exec - exec1;
   double ob = 0.0;
   {
     std::vector<const hh_block*> u = plan->ops;

@@ -1,0 +1,116 @@
+"""Seeded synthetic superblocks with the sector structure of a real DMRG step.
+
+Used by bench.py when a workload is too large to grow with a full sweep: a
+mid-chain superblock of a W x L cylinder keeps m multiplets per block, spread
+over (N, 2S) block sectors with a Gaussian profile in N around the filling and
+a decaying profile in S, like the density-matrix spectra of the reference's
+runs.  Operator entries are N(0,1) complex (re, im ~ N(0, 1/2)); block
+Hamiltonians are Hermitian.  The term list and every quantum-number rule come
+from the real geometry (hmerge / model_wave), so the task structure and FLOP
+count of the matvec are those of the physical superblock; only the numbers in
+the blocks are random.
+"""
+import numpy as np
+
+from .types import SubBlock, TotalBlock, TotalModel, get_basis, get_super_basis
+from .sites import SiteOperators
+from .lattice import SquareLattice
+
+
+def block_sectors(n_sites, n_fill, m, rng, sigma_n=None, s_scale=2.5, max_dim=None):
+    """(N, 2S, dim) of a block that keeps m multiplets."""
+    if sigma_n is None:
+        sigma_n = max(1.5, 0.45 * np.sqrt(n_sites))
+    lo = max(0, int(n_fill - 4 * sigma_n))
+    hi = min(2 * n_sites, int(n_fill + 4 * sigma_n) + 1)
+    cands, w = [], []
+    for N in range(lo, hi + 1):
+        smax = min(N, 2 * n_sites - N)
+        for S2 in range(N % 2, smax + 1, 2):
+            s = S2 / 2.0
+            wt = np.exp(-((N - n_fill) ** 2) / (2 * sigma_n ** 2)) * (2 * s + 1) * np.exp(-s * (s + 1) / (2 * s_scale ** 2))
+            cands.append((N, S2))
+            w.append(wt)
+    w = np.array(w)
+    w /= w.sum()
+    dims = np.floor(w * m).astype(int)
+    # distribute the remainder to the heaviest sectors, keep sectors with dim >= 1
+    rem = m - dims.sum()
+    order = np.argsort(-w)
+    for i in order[:rem]:
+        dims[i] += 1
+    if max_dim is not None:
+        dims = np.minimum(dims, max_dim)
+    out = [(N, S2, int(d)) for (N, S2), d in zip(cands, dims) if d >= 1]
+    rng.shuffle(out)
+    # block sectors are stored in basis order (descending 2S, then N) in the reference
+    out.sort(key=lambda q: (-q[1], -q[0]))
+    return out
+
+
+def _herm(rng, d):
+    a = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    return (a + a.conj().T) / 2.0
+
+
+def _rand(rng, r, c):
+    return (rng.normal(scale=np.sqrt(0.5), size=(r, c)) + 1j * rng.normal(scale=np.sqrt(0.5), size=(r, c)))
+
+
+def synthetic_model(length, sectors, slots, rng, names=("elec_up", "elec_down")):
+    dims = {(N, S2): d for (N, S2, d) in sectors}
+    ham = TotalBlock(length, 0, 0, [SubBlock(N, S2, 0, _herm(rng, d)) for (N, S2, d) in sectors])
+
+    def ndia(up_dif):
+        subs = []
+        for (N, S2, d) in sectors:
+            for dd in (-1, 1):
+                tgt = (N + up_dif, S2 + dd)
+                if tgt in dims and S2 + dd >= 0:
+                    subs.append(SubBlock(N, S2, dd, _rand(rng, dims[tgt], d)))
+        return TotalBlock(length, up_dif, 1, subs)
+
+    sub = {}
+    for k in range(1, slots + 1):
+        d = {}
+        if "elec_up" in names:
+            d["elec_up"] = ndia(+1)
+        if "elec_down" in names:
+            d["elec_down"] = ndia(-1)
+        sub[k] = d
+    return TotalModel(length, ham, sub)
+
+
+class Workload:
+    """A synthetic mid-chain superblock: models, bases, super basis, geometry."""
+
+    def __init__(self, W=4, L=32, n_elec=112, m=2000, U=8.0, phi=0.25, seed=20261203, sys_len=None):
+        self.W, self.L, self.n_elec, self.m, self.U, self.phi, self.seed = W, L, n_elec, m, U, phi, seed
+        rng = np.random.default_rng(seed)
+        self.lat = SquareLattice(W, L, U=U, phi=phi)
+        N = self.lat.N
+        ls = N // 2 - 1 if sys_len is None else sys_len
+        le = N - ls - 2
+        fill = n_elec / N
+        self.sys_sectors = block_sectors(ls, fill * ls, m, rng)
+        self.env_sectors = block_sectors(le, fill * le, m, rng)
+        self.sys = synthetic_model(ls, self.sys_sectors, max(1, self.lat.nleg11[ls]), rng)
+        self.env = synthetic_model(le, self.env_sectors, max(1, self.lat.nleg11[le]), rng)
+        st = SiteOperators("hubbard")
+        self.sys_bs = get_basis(self.sys.ham, st.sz)
+        self.env_bs = get_basis(self.env.ham, st.sz)
+        self.sup = get_super_basis(self.sys_bs, self.env_bs, n_elec, 0)
+        self.geo = self.lat.geometry(ls, le)
+        self.name = f"hubbard-cylinder-{W}x{L}-phi{phi:g}-U{U:g}-Ne{n_elec}-m{m}-midchain"
+
+    def describe(self):
+        return {
+            "workload": self.name,
+            "lattice": f"{self.W}x{self.L} cylinder (periodic y, open x), Landau gauge",
+            "phi": self.phi, "U": self.U, "t": 1.0, "n_elec": self.n_elec, "kept_multiplets": self.m,
+            "sys_len": self.sys.len, "env_len": self.env.len,
+            "block_sectors": [len(self.sys_sectors), len(self.env_sectors)],
+            "enlarged_dims": [self.sys_bs.dim, self.env_bs.dim],
+            "wave_sectors": self.sup.num, "wave_dim": self.sup.dim,
+            "operators": "synthetic N(0,1) complex, Hermitian block Hamiltonians, seed %d" % self.seed,
+        }

@@ -134,17 +134,27 @@ typedef struct {
 int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* env_bs,
                    const hh_wave_t* layout, int nterm, const hh_term_t* terms,
                    hh_plan_t** out);
-/* counts: [0] reference FLOPs per matvec (8MNK over the reference's ZGEMM
- * calls + 8 per element of the axpy terms), [1] FLOPs this plan executes,
- * [2] output tiles, [3] segments, [4] stage-1 products, [5] scratch bytes,
- * [6] operator bytes read per matvec, [7] wave bytes (in + out)            */
+/* counts (12 doubles): [0] reference FLOPs per matvec (8MNK over the
+ * reference's ZGEMM calls + 8 per element of the axpy terms), [1] FLOPs this
+ * plan executes, [2] output tiles, [3] segments, [4] stage-1 products,
+ * [5] scratch bytes, [6] operator bytes, [7] wave bytes (in + out),
+ * [8] executed FLOPs of stage 1, [9] of stage 2, [10] reference FLOPs of the
+ * first GEMM of the two-GEMM terms, [11] the remaining reference FLOPs.    */
 int hh_plan_stats(const hh_plan_t* p, double* counts);
 int hh_plan_free(hh_plan_t* p);
 
 /* model_wave (code/mat_vec.f90:3476): out = H in, device-resident waves.   */
 int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision);
-/* model_wave with host buffers: copies in, multiplies, copies out.         */
+/* model_wave with host buffers: copies in, multiplies, copies out (device
+ * buffers of the plan are reused between calls).                          */
 int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision);
+/* hh_matvec with CUDA events on the context stream around each stage;
+ * ms[0] = whole matvec, ms[1] = stage 1 (left products), ms[2] = stage 2.  */
+int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision, float* ms);
+
+/* pinned host memory for the caller's wave buffers (fast H2D/D2H copies)   */
+int hh_host_alloc(long long bytes, void** ptr);
+int hh_host_free(void* ptr);
 
 /* lanczos_memo_new (code/lanczos.f90:4-177), levels = 1.  psi is the start
  * vector on entry and the ground state on exit; lanzero is the breakdown and
