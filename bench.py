@@ -258,6 +258,7 @@ def main():
     clocks.start()
     tot = s1 = s2 = 0.0
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -266,6 +267,7 @@ def main():
         s1 += b
         s2 += c
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     t_steps = tot / 1e3  # seconds, device time of the K matvecs
     if dist:

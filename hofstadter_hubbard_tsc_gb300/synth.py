@@ -3,8 +3,11 @@
 Used by bench.py when a workload is too large to grow with a full sweep: a
 mid-chain superblock of a W x L cylinder keeps m multiplets per block, spread
 over (N, 2S) block sectors with a Gaussian profile in N around the filling and
-a decaying profile in S, like the density-matrix spectra of the reference's
-runs.  Operator entries are N(0,1) complex (re, im ~ N(0, 1/2)); block
+a profile (2S+1) exp(-S(S+1)/(2 s^2)) in S.  The profile was read off a real
+finite-size run (4x6 cylinder, N_e=20, U=8, phi=1/4, m=120, 12-site blocks:
+13 sectors, sigma_N = 1.2, s = 1.0, largest sector 17% of the states) and
+widened for m=2000 and 63-site blocks to sigma_N = 2.5, s = 1.5 (65 sectors,
+largest 123 multiplets).  Operator entries are N(0,1) complex (re, im ~ N(0, 1/2)); block
 Hamiltonians are Hermitian.  The term list and every quantum-number rule come
 from the real geometry (hmerge / model_wave), so the task structure and FLOP
 count of the matvec are those of the physical superblock; only the numbers in
@@ -17,10 +20,8 @@ from .sites import SiteOperators
 from .lattice import SquareLattice
 
 
-def block_sectors(n_sites, n_fill, m, rng, sigma_n=None, s_scale=2.5, max_dim=None):
+def block_sectors(n_sites, n_fill, m, rng, sigma_n=2.5, s_scale=1.5, max_dim=None):
     """(N, 2S, dim) of a block that keeps m multiplets."""
-    if sigma_n is None:
-        sigma_n = max(1.5, 0.45 * np.sqrt(n_sites))
     lo = max(0, int(n_fill - 4 * sigma_n))
     hi = min(2 * n_sites, int(n_fill + 4 * sigma_n) + 1)
     cands, w = [], []
