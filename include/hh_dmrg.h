@@ -152,6 +152,17 @@ int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision);
  * ms[0] = whole matvec, ms[1] = stage 1 (left products), ms[2] = stage 2.  */
 int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision, float* ms);
 
+/* hh_matvec (FP64) that allocates nothing during the call.  No counterpart
+ * in the reference: it exists for callers that cannot call cudaMalloc when
+ * they multiply (their own pool already holds the GPU's memory, or a fixed
+ * device budget is reserved up front).  The stage-1 scratch is a static
+ * device array of 64 MiB that every GPU loading the library holds until exit;
+ * larger plans are rejected with HH_ERR_INVALID.  All calls on a device share
+ * the array: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) with that device
+ * current; the context's device must be the current device.               */
+int hh_matvec_noalloc(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out);
+
 /* pinned host memory for the caller's wave buffers (fast H2D/D2H copies)   */
 int hh_host_alloc(long long bytes, void** ptr);
 int hh_host_free(void* ptr);
