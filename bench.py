@@ -244,7 +244,7 @@ def main():
 
     stream = torch.cuda.ExternalStream(dev.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
-    ms = (C.c_float * 3)()
+    ms = (C.c_float * 4)()
 
     def step():
         dev.check(dev.lib.hh_matvec_timed(sb.plan, w_in.h, w_out.h, prec, ms))
@@ -305,7 +305,7 @@ def main():
     peaks = measured_peaks()
     stage = 1 if s1 >= s2 else 2
     t_stage = (s1 if stage == 1 else s2) / args.steps * 1e-3
-    counts = np.zeros(12)
+    counts = np.zeros(16)
     dev.check(dev.lib.hh_plan_stats(sb.plan, counts.ctypes.data_as(dp)))
     flops_stage = counts[8] if stage == 1 else counts[9]
     achieved = flops_stage / t_stage / 1e12
@@ -317,9 +317,15 @@ def main():
         peak_note = "measured bf16 burst / 6 (three-way split: six bf16 products per real product)"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None, "traffic": None,
-                "kernel": f"seg_gemm stage {stage}", "peak_note": peak_note,
+                "kernel": (f"seg_gemm_fp64 stage {stage}" if prec == _lib.HH_PREC_FP64
+                           else f"tc_tile_kernel stage {stage}"),
+                "peak_note": peak_note,
                 "algorithmic_flops_per_launch": flops_stage,
                 "kernel_ms_per_launch": t_stage * 1e3}
+    if prec != _lib.HH_PREC_FP64:
+        issued = counts[12] if stage == 1 else counts[13]
+        roofline["bf16_flops_issued_per_launch"] = issued
+        roofline["tensor_pipe_frac_of_measured_bf16"] = issued / t_stage / 1e12 / peaks["bf16_tflops"]
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,
@@ -332,7 +338,14 @@ def main():
                                              "exec_gflop_per_matvec": counts[1] / 1e9,
                                              "plan_setup_s": setup_s}),
             "roofline": roofline, "e2e": e2e, "clocks": clk,
-            "gpu_launches": args.steps * (2 if prec == _lib.HH_PREC_FP64 else 4)}
+            "gpu_launches": args.steps * (2 if prec == _lib.HH_PREC_FP64 else 3)}
+    if prec != _lib.HH_PREC_FP64:
+        w_in.upload(psi)
+        dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, _lib.HH_PREC_FP64))
+        h64 = w_out.download()
+        dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, prec))
+        hmx = w_out.download()
+        line["rel_err_vs_fp64_gpu"] = float(np.linalg.norm(hmx - h64) / np.linalg.norm(h64))
     if rank == 0 and not args.no_cpu_baseline:
         n = max(1, args.cpu_sample)
         dt, hpsi_cpu = cpu_matvec_timer(wl, psi, n)

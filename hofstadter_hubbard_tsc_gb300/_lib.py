@@ -85,6 +85,7 @@ SIGNATURES = {
     "hh_lanczos": (I, [P, P, D, I, I, DP, IP]),
     "hh_matvec_timed": (I, [P, P, P, I, C.POINTER(C.c_float)]),
     "hh_matvec_noalloc": (I, [P, P, P]),
+    "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP]),
     "hh_host_alloc": (I, [C.c_longlong, PP]),
     "hh_host_free": (I, [P]),
 }

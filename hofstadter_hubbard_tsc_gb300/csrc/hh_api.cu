@@ -579,6 +579,10 @@ int hh_plan_stats(const hh_plan_t* p, double* c) {
   c[9] = p->exec_flops_s2;
   c[10] = p->ref_flops_first;
   c[11] = p->ref_flops - p->ref_flops_first;
+  c[12] = p->tc.mma_flops1;
+  c[13] = p->tc.mma_flops2;
+  c[14] = p->tc.bytes_op + p->tc.bytes_x + p->tc.bytes_t;
+  c[15] = p->tc.ready ? 1.0 : 0.0;
   return HH_OK;
 }
 
@@ -587,6 +591,7 @@ int hh_plan_free(hh_plan_t* p) {
   cudaStreamSynchronize(p->ctx->stream);
   p->stage1.release();
   p->stage2.release();
+  release_tc_plan(p);
   if (p->d_scratch) cudaFree(p->d_scratch);
   if (p->d_krylov) cudaFree(p->d_krylov);
   if (p->d_host_in) cudaFree(p->d_host_in);
@@ -596,15 +601,14 @@ int hh_plan_free(hh_plan_t* p) {
 }
 
 static int matvec_timed_tc(hh_plan* p, const double2* in, double2* out, int precision, float* ms) {
-  return fail(p->ctx, HH_ERR_UNSUPPORTED, "split-precision matvec is not built into this library");
+  return matvec_tc(p, in, out, ms);
 }
 
 static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision) {
   hh_ctx* ctx = p->ctx;
   if (precision != HH_PREC_FP64 && precision != HH_PREC_BF16X3)
     return fail(ctx, HH_ERR_INVALID, "unknown precision");
-  if (precision == HH_PREC_BF16X3)
-    return fail(ctx, HH_ERR_UNSUPPORTED, "split-precision matvec is not built into this library");
+  if (precision == HH_PREC_BF16X3) return matvec_tc(p, in, out, nullptr);
   cudaError_t e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
   if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
   if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
@@ -654,6 +658,7 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
     cudaEventElapsedTime(&ms[0], ev[0], ev[2]);
     cudaEventElapsedTime(&ms[1], ev[0], ev[1]);
     cudaEventElapsedTime(&ms[2], ev[1], ev[2]);
+    ms[3] = 0.f;
   }
   for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
   return cuda_check(ctx, e, "matvec_timed");

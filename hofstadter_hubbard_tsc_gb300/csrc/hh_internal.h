@@ -143,8 +143,48 @@ struct hh_gemm_list {
   void release();
 };
 
+// One contribution out_k[rect] += c * opA(A) * X_i[region] * opB(B) of the
+// model_wave term loops (see plan.cpp); the schedules of both precisions are
+// built from this list.
+struct hh_mat_ref {
+  long long off = 0;  // absolute address for operators
+  int base = 0;
+  int ld = 1;
+  int op = 0;         // HH_OP_N or HH_OP_C
+};
+
+struct hh_contrib {
+  int k_out, orow, ocol, M, N;
+  int i_in, irow, icol, Ka, Kb;
+  bool hasA, hasB;
+  hh_mat_ref A, B;
+  double cre, cim;
+};
+
+namespace hh { namespace tc { struct ImgTask; struct Seg; struct Tile; } }
+
+struct hh_tc_plan {
+  bool ready = false;
+  void* d_op_img = nullptr;    // operator images (built once)
+  void* d_x_img = nullptr;     // images of the input wave (built every matvec)
+  void* d_t_img = nullptr;     // stage-1 products
+  hh::tc::ImgTask* d_op_tasks = nullptr;
+  hh::tc::ImgTask* d_x_tasks = nullptr;
+  int n_op_tasks = 0, n_x_tasks = 0;
+  hh::tc::Tile* d_tiles1 = nullptr;
+  hh::tc::Tile* d_tiles2 = nullptr;
+  int n_tiles1 = 0, n_tiles2 = 0;
+  hh::tc::Seg* d_segs = nullptr;
+  hh_seg* d_csegs = nullptr;
+  int* d_err = nullptr;
+  double bytes_op = 0, bytes_x = 0, bytes_t = 0;
+  double mma_flops1 = 0, mma_flops2 = 0;  // tensor FLOPs issued (bf16), padding included
+};
+
 struct hh_plan {
   hh_ctx* ctx = nullptr;
+  std::vector<hh_contrib> contribs;
+  hh_tc_plan tc;
   const hh_wave* layout = nullptr;
   long long nelem = 0;
   hh_gemm_list stage1, stage2;
@@ -179,6 +219,9 @@ cudaError_t krylov_combine(const double2* V, int k, long long ld, double2* out, 
                            const double* d_coef, cudaStream_t s);
 int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wave* layout,
                int nterm, const hh_term_t* terms, hh_plan* plan);
+int build_tc_plan(hh_plan* plan);
+void release_tc_plan(hh_plan* plan);
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms);
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
 int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
 }  // namespace hh

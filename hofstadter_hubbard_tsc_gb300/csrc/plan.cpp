@@ -70,31 +70,20 @@ struct OpView {
   }
 };
 
-struct Mat {
-  long long off = 0;  // absolute address for operators, element offset otherwise
-  int base = HH_BASE_ABS;
-  int ld = 1;
-  int op = HH_OP_N;
-};
+using Mat = hh_mat_ref;
 
 inline Mat op_mat(const OpView& v, int j, bool herm) {
   Mat m;
   const auto& s = v.b->subs[j];
   m.off = (long long)(uintptr_t)(v.b->d + s.off);
-  m.base = HH_BASE_ABS;
+  m.base = HH_BASE_ABS;  // operators are absolute addresses
   m.ld = s.row > 0 ? s.row : 1;
   bool c = v.trans ^ herm;
   m.op = c ? HH_OP_C : HH_OP_N;
   return m;
 }
 
-struct Contrib {
-  int k_out, orow, ocol, M, N;
-  int i_in, irow, icol, Ka, Kb;
-  bool hasA, hasB;
-  Mat A, B;
-  cplx coef;
-};
+using Contrib = hh_contrib;
 
 struct Emitter {
   const hh_basis* sb;
@@ -145,7 +134,8 @@ struct Emitter {
     t.hasA = A != nullptr; t.hasB = B != nullptr;
     if (A) t.A = *A;
     if (B) t.B = *B;
-    t.coef = c;
+    t.cre = c.real();
+    t.cim = c.imag();
     out.push_back(t);
   }
   // rows [orow, orow+M) of sector k (all env columns) += c opA(A) X_i rows [irow, +Ka)
@@ -696,8 +686,8 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
   }
   for (const Contrib& t : E.out) {
     hh_seg s{};
-    s.cre = t.coef.real();
-    s.cim = t.coef.imag();
+    s.cre = t.cre;
+    s.cim = t.cim;
     if (t.hasA && t.hasB) {
       auto key = std::make_tuple(t.A.off, t.A.op, t.A.ld, t.i_in, t.irow, t.icol, t.Ka, t.Kb);
       auto it = t_index.find(key);
@@ -781,6 +771,7 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
     for (auto* b : u) ob += 16.0 * (double)b->nelem;
   }
   plan->op_bytes = ob;
+  plan->contribs = std::move(E.out);
   return HH_OK;
 }
 

@@ -1,0 +1,54 @@
+// Task formats of the split-precision tensor-core path (see tc_gemm.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+struct hh_seg;
+
+namespace hh {
+namespace tc {
+
+// builds one operand image: value(r,k) = coef * (conj?) src[trans ? k + r*ld : r + k*ld]
+struct ImgTask {
+  long long src;   // absolute address (HH_BASE_ABS) or element offset into the input wave
+  int sbase;
+  int ld;
+  int rows, kc;    // logical extent (complex)
+  int r8, k16;     // padded extent
+  int trans, conj;
+  double cre, cim;
+  long long dst;   // absolute address of the image (256-byte aligned)
+};
+
+// one GEMM segment of a tile: 6 planes of A rows [m0, m0+128) and of B rows
+// [n0, n0+ntile) for nkc chunks of 16 complex k
+struct Seg {
+  long long a, b;        // address of plane 0, chunk 0 at the tile's first row
+  long long a_plane, b_plane;  // bytes between planes (= R8/8 * 256 of the image)
+  int a_bytes, b_bytes;  // bytes per plane copy (rows * 32)
+  int nkc;
+  int pad;
+};
+
+struct Tile {
+  int seg0, nseg;        // GEMM segments
+  int cseg0, ncseg;      // FP64 copy segments (epilogue)
+  int mode;              // 0: FP64 output rectangle, 1: T image
+  int ntile;             // MMA N (multiple of 16, <= 128)
+  int mrem, nrem;        // valid rows / columns of the tile
+  long long out;         // mode 0: element offset of (m0, n0) in the output wave; mode 1: image address
+  int ldo;
+  int t_r8;              // mode 1: padded rows of the T image
+  int m0, n0;            // tile origin inside its rectangle
+};
+
+size_t tile_smem_bytes();
+
+}  // namespace tc
+
+cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, cudaStream_t s);
+cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, const hh_seg* d_csegs,
+                         const double2* base_in, double2* base_out, int* d_err, cudaStream_t s);
+
+}  // namespace hh

@@ -1,0 +1,401 @@
+// Split-precision tensor-core path of the block-sparse matvec (sm_103a).
+//
+// Every complex FP64 operand is carried as six BF16 planes: re0 re1 re2 im0
+// im1 im2 with x = x0 + x1 + x2 (x0 = bf16(x), x1 = bf16(x - x0), ...), i.e.
+// 24 significand bits.  A complex tile product keeps the six split products
+// with i + j <= 2 for each of the four real products (re.re, im.im, re.im,
+// im.re): 24 tcgen05.mma (M=128, K=16, FP32 accumulate in TMEM) per 16 complex
+// k.  The dropped products are below 2^-24 relative.  D_re and D_im live in
+// TMEM columns [0,128) and [128,256); the -im.im product uses the negate-A bit
+// of the instruction descriptor.
+//
+// Operand "images": a complex matrix used as an MMA operand with R rows and
+// Kc complex k is stored as BF16 in the canonical K-major no-swizzle UMMA
+// layout, padded to R8 = roundup(R,8) rows and K16 = roundup(Kc,16):
+//   byte offset of core matrix (chunk kc, plane p, row group g, k half h) =
+//     ((kc * 6 + p) * (R8 / 8) + g) * 256 + h * 128
+//   inside it, row r%8 occupies 16 bytes holding k%8 = 0..7.
+// So the 128 (or N) rows of one plane and one 16-wide k chunk are contiguous
+// and reach shared memory with one cp.async.bulk; LBO = 128 B (next 8 k),
+// SBO = 256 B (next 8 rows).
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "hh_internal.h"
+#include "tc.h"
+
+namespace hh {
+namespace tc {
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// bounded wait on an mbarrier phase; returns false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (uint32_t i = 0; i < (1u << 26); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (i > 64) __nanosleep(32);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  // start address >> 4 (bits 0-13), LBO = 128 B (bits 16-29), SBO = 256 B
+  // (bits 32-45), version 1 (bits 46-47), no swizzle (bits 61-63 = 0)
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((128u >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((256u >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+__host__ __device__ constexpr uint32_t idesc_bf16(int n, bool neg_a) {
+  // D f32 (bits 4-5 = 1), A bf16 (7-9 = 1), B bf16 (10-12 = 1), negate A
+  // (bit 13), K-major A and B (bits 15, 16 = 0), N >> 3 (17-22), M >> 4 (24-28)
+  return (1u << 4) | (1u << 7) | (1u << 10) | (neg_a ? (1u << 13) : 0u) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// ------------------------------------------------------------------ splitting
+__device__ __forceinline__ void split3d(double x, __nv_bfloat16* o) {
+  __nv_bfloat16 a = __double2bfloat16(x);
+  double r = x - (double)__bfloat162float(a);
+  __nv_bfloat16 b = __double2bfloat16(r);
+  r = r - (double)__bfloat162float(b);
+  o[0] = a;
+  o[1] = b;
+  o[2] = __double2bfloat16(r);
+}
+
+__device__ __forceinline__ void split3f(float x, __nv_bfloat16* o) {
+  __nv_bfloat16 a = __float2bfloat16_rn(x);
+  float r = x - __bfloat162float(a);
+  __nv_bfloat16 b = __float2bfloat16_rn(r);
+  r = r - __bfloat162float(b);
+  o[0] = a;
+  o[1] = b;
+  o[2] = __float2bfloat16_rn(r);
+}
+
+__device__ __forceinline__ uint4 pack8(const __nv_bfloat16* v) {
+  uint32_t w[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    w[i] = (uint32_t)__bfloat16_as_ushort(v[2 * i]) | ((uint32_t)__bfloat16_as_ushort(v[2 * i + 1]) << 16);
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__device__ __forceinline__ size_t img_off(int r8, int r, int k) {
+  // byte offset of the 16-byte row chunk (row r, k rounded down to 8) in a plane-0 image
+  return ((size_t)((k >> 4) * 6) * (r8 >> 3) + (r >> 3)) * 256 + ((k >> 3) & 1) * 128 + (r & 7) * 16;
+}
+
+// ------------------------------------------------------------------ image build
+// One CTA per task: value(r,k) = coef * (conj?) src[trans ? k + r*ld : r + k*ld]
+// for r < rows, k < kc, zero in the padding; written as six BF16 planes.
+__global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __restrict__ tasks,
+                                                           const double2* __restrict__ base_in) {
+  const ImgTask t = tasks[blockIdx.x];
+  const double2* src = t.sbase == HH_BASE_IN ? base_in + t.src : reinterpret_cast<const double2*>(t.src);
+  uint8_t* dst = reinterpret_cast<uint8_t*>(t.dst);
+  const int r8 = t.r8, k16 = t.k16;
+  const size_t plane = (size_t)(r8 >> 3) * 256;
+  const int ngroups = r8 * (k16 >> 3);
+  for (int idx = threadIdx.x; idx < ngroups; idx += blockDim.x) {
+    const int r = idx % r8, k0 = (idx / r8) * 8;
+    __nv_bfloat16 re[3][8], im[3][8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = k0 + j;
+      double2 v = make_double2(0.0, 0.0);
+      if (r < t.rows && k < t.kc) {
+        v = t.trans ? src[(long long)k + (long long)r * t.ld] : src[(long long)r + (long long)k * t.ld];
+        if (t.conj) v.y = -v.y;
+        v = make_double2(t.cre * v.x - t.cim * v.y, t.cre * v.y + t.cim * v.x);
+      }
+      __nv_bfloat16 s[3];
+      split3d(v.x, s);
+      re[0][j] = s[0]; re[1][j] = s[1]; re[2][j] = s[2];
+      split3d(v.y, s);
+      im[0][j] = s[0]; im[1][j] = s[1]; im[2][j] = s[2];
+    }
+    const size_t o = img_off(r8, r, k0);
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      *reinterpret_cast<uint4*>(dst + o + (size_t)p * plane) = pack8(re[p]);
+      *reinterpret_cast<uint4*>(dst + o + (size_t)(p + 3) * plane) = pack8(im[p]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ tile GEMM
+constexpr int kPlaneA = 128 * 32;            // 128 rows x 16 bf16
+constexpr int kStageA = 6 * kPlaneA;         // 24 KB
+constexpr int kThreads = 192;                // producer, MMA, 4 epilogue warps
+
+__device__ __forceinline__ void flag_error(int* err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+template <int STAGES>
+__global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __restrict__ tiles,
+                                                             const Seg* __restrict__ segs,
+                                                             const hh_seg* __restrict__ csegs,
+                                                             const double2* __restrict__ base_in,
+                                                             double2* __restrict__ base_out, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const Tile t = tiles[blockIdx.x];
+  const int stage_bytes = kStageA + 6 * 128 * 32;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accf = empty + STAGES;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(accf + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accf, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tslot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      bool ok = true;
+      for (int si = 0; si < t.nseg && ok; ++si) {
+        const Seg sg = segs[t.seg0 + si];
+        for (int kc = 0; kc < sg.nkc; ++kc, ++it) {
+          const int s = it % STAGES;
+          if (it >= STAGES && !mbar_wait(&empty[s], ((it / STAGES) + 1) & 1)) {
+            flag_error(err, 1);
+            ok = false;
+            break;
+          }
+          uint8_t* sa = smem + s * stage_bytes;
+          uint8_t* sb = sa + kStageA;
+          mbar_expect_tx(&full[s], 6u * (sg.a_bytes + sg.b_bytes));
+          const uint8_t* ga = reinterpret_cast<const uint8_t*>(sg.a) + (size_t)kc * 6 * sg.a_plane;
+          const uint8_t* gb = reinterpret_cast<const uint8_t*>(sg.b) + (size_t)kc * 6 * sg.b_plane;
+#pragma unroll
+          for (int p = 0; p < 6; ++p) {
+            bulk_g2s(sa + p * kPlaneA, ga + (size_t)p * sg.a_plane, sg.a_bytes, &full[s]);
+            bulk_g2s(sb + p * (t.ntile * 32), gb + (size_t)p * sg.b_plane, sg.b_bytes, &full[s]);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t id_pos = idesc_bf16(t.ntile, false), id_neg = idesc_bf16(t.ntile, true);
+      const uint32_t d_re = tmem, d_im = tmem + 128;
+      int it = 0;
+      uint32_t acc = 0;
+      bool ok = true;
+      for (int si = 0; si < t.nseg && ok; ++si) {
+        const Seg sg = segs[t.seg0 + si];
+        for (int kc = 0; kc < sg.nkc; ++kc, ++it) {
+          const int s = it % STAGES;
+          if (!mbar_wait(&full[s], (it / STAGES) & 1)) {
+            flag_error(err, 2);
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t sa = smem_u32(smem + s * stage_bytes);
+          const uint32_t sb = sa + kStageA;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+#pragma unroll
+            for (int j = 0; j < 3 - i; ++j) {
+              const uint64_t are = smem_desc(sa + i * kPlaneA), aim = smem_desc(sa + (3 + i) * kPlaneA);
+              const uint64_t bre = smem_desc(sb + j * t.ntile * 32), bim = smem_desc(sb + (3 + j) * t.ntile * 32);
+              mma_bf16(d_re, are, bre, id_pos, acc);
+              mma_bf16(d_re, aim, bim, id_neg, 1u);
+              mma_bf16(d_im, are, bim, id_pos, acc);
+              mma_bf16(d_im, aim, bre, id_pos, 1u);
+              acc = 1u;
+            }
+          }
+          mma_commit(&empty[s]);
+        }
+      }
+      if (it > 0) mma_commit(accf);
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one output row per thread
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    int total = 0;
+    for (int si = 0; si < t.nseg; ++si) total += segs[t.seg0 + si].nkc;
+    bool have = total > 0;
+    if (have) {
+      if (!mbar_wait(accf, 0)) {
+        flag_error(err, 3);
+        have = false;
+      }
+      fence_after();
+    }
+    have = __all_sync(0xffffffffu, have);  // tcgen05.ld below is warp-collective
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    for (int c0 = 0; c0 < t.ntile; c0 += 16) {
+      float re[16], im[16];
+      if (have) {
+        tmem_ld16(lane_base + c0, re);
+        tmem_ld16(lane_base + 128 + c0, im);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) re[j] = im[j] = 0.f;
+      }
+      if (t.mode == 0) {
+        if (row < t.mrem) {
+          double2* O = base_out + t.out;
+#pragma unroll 4
+          for (int j = 0; j < 16; ++j) {
+            const int col = c0 + j;
+            if (col < t.nrem) {
+              double2 v = make_double2((double)re[j], (double)im[j]);
+              for (int ci = 0; ci < t.ncseg; ++ci) {
+                const hh_seg cs = csegs[t.cseg0 + ci];
+                const double2 x = base_in[cs.poff + (long long)(t.m0 + row) + (long long)(t.n0 + col) * cs.ldp];
+                v.x += cs.cre * x.x - cs.cim * x.y;
+                v.y += cs.cre * x.y + cs.cim * x.x;
+              }
+              O[(long long)row + (long long)col * t.ldo] = v;
+            }
+          }
+        }
+      } else {
+        // T image: rows of T, k = T columns; zero outside the valid rectangle
+        const int r = t.m0 + row;
+        if (r < t.t_r8) {
+          uint8_t* img = reinterpret_cast<uint8_t*>(t.out);
+          const size_t plane = (size_t)(t.t_r8 >> 3) * 256;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            __nv_bfloat16 pr[3][8], pi[3][8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int cc = c0 + h * 8 + j;
+              const bool valid = row < t.mrem && cc < t.nrem;
+              __nv_bfloat16 s[3];
+              split3f(valid ? re[h * 8 + j] : 0.f, s);
+              pr[0][j] = s[0]; pr[1][j] = s[1]; pr[2][j] = s[2];
+              split3f(valid ? im[h * 8 + j] : 0.f, s);
+              pi[0][j] = s[0]; pi[1][j] = s[1]; pi[2][j] = s[2];
+            }
+            const size_t o = img_off(t.t_r8, r, t.n0 + c0 + h * 8);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) {
+              *reinterpret_cast<uint4*>(img + o + (size_t)p * plane) = pack8(pr[p]);
+              *reinterpret_cast<uint4*>(img + o + (size_t)(p + 3) * plane) = pack8(pi[p]);
+            }
+          }
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+  }
+}
+
+constexpr int kStages = 3;
+
+size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8 * (2 * kStages + 2) + 64; }
+
+}  // namespace tc
+
+cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, cudaStream_t s) {
+  if (ntask <= 0) return cudaSuccess;
+  tc::build_images_kernel<<<ntask, 256, 0, s>>>(d_tasks, base_in);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, const hh_seg* d_csegs,
+                         const double2* base_in, double2* base_out, int* d_err, cudaStream_t s) {
+  if (ntile <= 0) return cudaSuccess;
+  const size_t smem = tc::tile_smem_bytes();
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc::tc_tile_kernel<tc::kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  tc::tc_tile_kernel<tc::kStages><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, d_csegs, base_in, base_out,
+                                                                    d_err);
+  return cudaGetLastError();
+}
+
+}  // namespace hh

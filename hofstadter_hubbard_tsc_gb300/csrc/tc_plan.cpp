@@ -1,0 +1,437 @@
+// Schedule of the split-precision tensor-core matvec, built from the plan's
+// contribution list on the first BF16X3 matvec of a plan.
+//
+//   operator images  built once: one per (operator sub-block, role, op, coef);
+//                    the coefficient of a segment is folded into the image of
+//                    the operator it multiplies, so every tile accumulates all
+//                    of its GEMM segments in TMEM without rescaling;
+//   wave images      built every matvec from the FP64 input, one per
+//                    (elementary region, role);
+//   stage 1          T = opA(A) X for the deduplicated two-operator products,
+//                    written as T images (mode 1);
+//   stage 2          every output sub-block, 128 x N tiles, GEMM segments
+//                    (T B, A X, X B) accumulated in TMEM, copy terms added in
+//                    FP64 in the epilogue (mode 0).
+#include <map>
+#include <tuple>
+#include <algorithm>
+#include <cstring>
+
+#include "hh_internal.h"
+#include "tc.h"
+
+namespace hh {
+
+namespace {
+
+inline int r8(int r) { return (r + 7) & ~7; }
+inline int k16(int k) { return (k + 15) & ~15; }
+inline long long img_bytes(int rows, int kc) {
+  long long b = (long long)r8(rows) * k16(kc) * 12;  // six bf16 planes
+  return (b + 255) & ~255LL;
+}
+
+struct ImgRef {
+  long long off = 0;  // offset into its arena
+  int rows = 0, kc = 0;
+};
+
+struct Arena {
+  long long size = 0;
+  long long take(long long b) {
+    long long o = size;
+    size += b;
+    return o;
+  }
+};
+
+}  // namespace
+
+void release_tc_plan(hh_plan* p) {
+  hh_tc_plan& t = p->tc;
+  void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
+                  t.d_tiles2, t.d_segs, t.d_csegs, t.d_err};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  t = hh_tc_plan();
+}
+
+int build_tc_plan(hh_plan* p) {
+  hh_ctx* ctx = p->ctx;
+  const hh_wave* L = p->layout;
+  // ---------------------------------------------------------------- images
+  std::map<std::tuple<long long, int, int, int, double, double, int, int>, ImgRef> op_imgs;
+  std::map<std::tuple<int, int, int, int, int, int>, ImgRef> x_imgs;
+  std::vector<tc::ImgTask> op_tasks, x_tasks;
+  Arena a_op, a_x, a_t;
+  // role 0 = A operand (rows = M, k = K), role 1 = B operand (rows = N, k = K)
+  auto op_img = [&](const hh_mat_ref& m, int role, int rows, int kc, double cre, double cim) {
+    auto key = std::make_tuple(m.off, m.op, m.ld, role, cre, cim, rows, kc);
+    auto it = op_imgs.find(key);
+    if (it != op_imgs.end()) return it->second;
+    ImgRef r;
+    r.rows = rows;
+    r.kc = kc;
+    r.off = a_op.take(img_bytes(rows, kc));
+    tc::ImgTask t{};
+    t.src = m.off;
+    t.sbase = HH_BASE_ABS;
+    t.ld = m.ld;
+    t.rows = rows;
+    t.kc = kc;
+    t.r8 = r8(rows);
+    t.k16 = k16(kc);
+    // A, op N: O[r + k ld]; A, op C: conj O[k + r ld]; B, op N: O[k + n ld]; B, op C: conj O[n + k ld]
+    t.trans = (role == 0) ? (m.op == HH_OP_C) : (m.op == HH_OP_N);
+    t.conj = (m.op == HH_OP_C);
+    t.cre = cre;
+    t.cim = cim;
+    t.dst = r.off;  // fixed up with the arena base below
+    op_tasks.push_back(t);
+    op_imgs.emplace(key, r);
+    return r;
+  };
+  auto x_img = [&](int i, int irow, int icol, int nrow, int ncol, int role) {
+    auto key = std::make_tuple(i, irow, icol, nrow, ncol, role);
+    auto it = x_imgs.find(key);
+    if (it != x_imgs.end()) return it->second;
+    const hh_wsec& w = L->secs[i];
+    ImgRef r;
+    // role 1 (B): rows = region columns, k = region rows; role 0 (A): rows = region rows
+    r.rows = role == 1 ? ncol : nrow;
+    r.kc = role == 1 ? nrow : ncol;
+    r.off = a_x.take(img_bytes(r.rows, r.kc));
+    tc::ImgTask t{};
+    t.src = w.off + (long long)icol * w.sdim + irow;
+    t.sbase = HH_BASE_IN;
+    t.ld = w.sdim;
+    t.rows = r.rows;
+    t.kc = r.kc;
+    t.r8 = r8(r.rows);
+    t.k16 = k16(r.kc);
+    t.trans = role == 1 ? 1 : 0;
+    t.conj = 0;
+    t.cre = 1.0;
+    t.cim = 0.0;
+    t.dst = r.off;
+    x_tasks.push_back(t);
+    x_imgs.emplace(key, r);
+    return r;
+  };
+
+  // --------------------------------------------------------------- stage 1
+  std::map<std::tuple<long long, int, int, int, int, int, int, int>, ImgRef> t_imgs;
+  std::vector<tc::Seg> segs;
+  std::vector<hh_seg> csegs;
+  std::vector<tc::Tile> tiles1, tiles2;
+  // addresses are arena offsets here; bases are added after allocation
+  // (bits 60-61 of an address mark its arena: 0 operators, 1 wave, 2 T)
+  auto tag = [](long long off, int arena) { return off | ((long long)arena << 60); };
+  double mma1 = 0.0, mma2 = 0.0;
+  auto make_seg = [&](long long a, const ImgRef& ai, int m0, long long b, const ImgRef& bi, int n0, int ntile) {
+    tc::Seg s{};
+    const int ar8 = r8(ai.rows), br8 = r8(bi.rows);
+    s.a = a + (long long)(m0 / 8) * 256;
+    s.b = b + (long long)(n0 / 8) * 256;
+    s.a_plane = (long long)(ar8 / 8) * 256;
+    s.b_plane = (long long)(br8 / 8) * 256;
+    s.a_bytes = std::min(128, ar8 - m0) * 32;
+    s.b_bytes = std::min(ntile, br8 - n0) * 32;
+    s.nkc = k16(ai.kc) / 16;
+    return s;
+  };
+
+  std::vector<ImgRef> contrib_t(p->contribs.size());
+  for (size_t ci = 0; ci < p->contribs.size(); ++ci) {
+    const hh_contrib& c = p->contribs[ci];
+    if (!(c.hasA && c.hasB)) continue;
+    auto key = std::make_tuple(c.A.off, c.A.op, c.A.ld, c.i_in, c.irow, c.icol, c.Ka, c.Kb);
+    auto it = t_imgs.find(key);
+    if (it != t_imgs.end()) {
+      contrib_t[ci] = it->second;
+      continue;
+    }
+    ImgRef T;
+    T.rows = c.M;
+    T.kc = c.Kb;
+    T.off = a_t.take(img_bytes(c.M, c.Kb));
+    t_imgs.emplace(key, T);
+    contrib_t[ci] = T;
+    ImgRef ai = op_img(c.A, 0, c.M, c.Ka, 1.0, 0.0);
+    ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.Kb, 1);
+    for (int m0 = 0; m0 < c.M; m0 += 128)
+      for (int n0 = 0; n0 < c.Kb; n0 += 128) {
+        const int ntile = k16(std::min(128, c.Kb - n0));
+        tc::Tile tl{};
+        tl.seg0 = (int)segs.size();
+        tl.nseg = 1;
+        segs.push_back(make_seg(tag(ai.off, 0), ai, m0, tag(xi.off, 1), xi, n0, ntile));
+        tl.mode = 1;
+        tl.ntile = ntile;
+        tl.mrem = std::min(128, c.M - m0);
+        tl.nrem = std::min(128, c.Kb - n0);
+        tl.out = tag(T.off, 2);
+        tl.t_r8 = r8(c.M);
+        tl.m0 = m0;
+        tl.n0 = n0;
+        tiles1.push_back(tl);
+        mma1 += 8.0 * 128 * ntile * (double)k16(c.Ka) * 6.0;
+      }
+  }
+
+  // --------------------------------------------------------------- stage 2
+  std::map<std::tuple<int, int, int>, std::vector<size_t>> rects;
+  std::vector<std::tuple<int, int, int>> order;
+  for (size_t ci = 0; ci < p->contribs.size(); ++ci) {
+    const hh_contrib& c = p->contribs[ci];
+    auto k = std::make_tuple(c.k_out, c.orow, c.ocol);
+    auto it = rects.find(k);
+    if (it == rects.end()) {
+      order.push_back(k);
+      rects[k].push_back(ci);
+    } else {
+      it->second.push_back(ci);
+    }
+  }
+  for (const auto& rk : order) {
+    const auto& list = rects[rk];
+    const hh_contrib& c0 = p->contribs[list[0]];
+    const int M = c0.M, N = c0.N;
+    const hh_wsec& w = L->secs[c0.k_out];
+    for (int m0 = 0; m0 < M; m0 += 128)
+      for (int n0 = 0; n0 < N; n0 += 128) {
+        const int ntile = k16(std::min(128, N - n0));
+        tc::Tile tl{};
+        tl.seg0 = (int)segs.size();
+        tl.cseg0 = (int)csegs.size();
+        for (size_t ci : list) {
+          const hh_contrib& c = p->contribs[ci];
+          if (c.hasA && c.hasB) {
+            const ImgRef& T = contrib_t[ci];
+            ImgRef bi = op_img(c.B, 1, c.N, c.Kb, c.cre, c.cim);
+            segs.push_back(make_seg(tag(T.off, 2), T, m0, tag(bi.off, 0), bi, n0, ntile));
+            mma2 += 8.0 * 128 * ntile * (double)k16(c.Kb) * 6.0;
+          } else if (c.hasA) {
+            ImgRef ai = op_img(c.A, 0, c.M, c.Ka, c.cre, c.cim);
+            ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.N, 1);
+            segs.push_back(make_seg(tag(ai.off, 0), ai, m0, tag(xi.off, 1), xi, n0, ntile));
+            mma2 += 8.0 * 128 * ntile * (double)k16(c.Ka) * 6.0;
+          } else if (c.hasB) {
+            ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.M, c.Kb, 0);
+            ImgRef bi = op_img(c.B, 1, c.N, c.Kb, c.cre, c.cim);
+            segs.push_back(make_seg(tag(xi.off, 1), xi, m0, tag(bi.off, 0), bi, n0, ntile));
+            mma2 += 8.0 * 128 * ntile * (double)k16(c.Kb) * 6.0;
+          } else {
+            hh_seg cs{};
+            const hh_wsec& wi = L->secs[c.i_in];
+            cs.poff = wi.off + (long long)c.icol * wi.sdim + c.irow;
+            cs.pbase = HH_BASE_IN;
+            cs.ldp = wi.sdim;
+            cs.kind = HH_SEG_COPY;
+            cs.cre = c.cre;
+            cs.cim = c.cim;
+            csegs.push_back(cs);
+          }
+        }
+        tl.nseg = (int)segs.size() - tl.seg0;
+        tl.ncseg = (int)csegs.size() - tl.cseg0;
+        tl.mode = 0;
+        tl.ntile = ntile;
+        tl.mrem = std::min(128, M - m0);
+        tl.nrem = std::min(128, N - n0);
+        tl.out = w.off + (long long)(c0.ocol + n0) * w.sdim + c0.orow + m0;
+        tl.ldo = w.sdim;
+        tl.m0 = m0;
+        tl.n0 = n0;
+        tiles2.push_back(tl);
+      }
+  }
+
+  // --------------------------------------------------------------- device
+  hh_tc_plan& t = p->tc;
+  auto alloc = [&](void** ptr, size_t bytes) -> int {
+    if (bytes == 0) bytes = 256;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    return e == cudaSuccess ? HH_OK : cuda_check(ctx, e, "cudaMalloc(tensor-core plan)");
+  };
+  int st;
+  if ((st = alloc(&t.d_op_img, a_op.size)) || (st = alloc(&t.d_x_img, a_x.size)) ||
+      (st = alloc(&t.d_t_img, a_t.size))) {
+    release_tc_plan(p);
+    return st;
+  }
+  const long long base[3] = {(long long)(uintptr_t)t.d_op_img, (long long)(uintptr_t)t.d_x_img,
+                             (long long)(uintptr_t)t.d_t_img};
+  auto untag = [&](long long v) {
+    int arena = (int)((unsigned long long)v >> 60);
+    return base[arena] + (v & ((1LL << 60) - 1));
+  };
+  for (auto& s : segs) {
+    s.a = untag(s.a);
+    s.b = untag(s.b);
+  }
+  for (auto& tl : tiles1) tl.out = untag(tl.out);
+  for (auto& tk : op_tasks) tk.dst += base[0];
+  for (auto& tk : x_tasks) tk.dst += base[1];
+  auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
+    if ((st = alloc(dptr, bytes))) return st;
+    if (bytes) {
+      cudaError_t e = cudaMemcpyAsync(*dptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+      if (e != cudaSuccess) return cuda_check(ctx, e, "upload tensor-core plan");
+    }
+    return HH_OK;
+  };
+  if ((st = upload((void**)&t.d_op_tasks, op_tasks.data(), op_tasks.size() * sizeof(tc::ImgTask))) ||
+      (st = upload((void**)&t.d_x_tasks, x_tasks.data(), x_tasks.size() * sizeof(tc::ImgTask))) ||
+      (st = upload((void**)&t.d_tiles1, tiles1.data(), tiles1.size() * sizeof(tc::Tile))) ||
+      (st = upload((void**)&t.d_tiles2, tiles2.data(), tiles2.size() * sizeof(tc::Tile))) ||
+      (st = upload((void**)&t.d_segs, segs.data(), segs.size() * sizeof(tc::Seg))) ||
+      (st = upload((void**)&t.d_csegs, csegs.data(), csegs.size() * sizeof(hh_seg))) ||
+      (st = alloc((void**)&t.d_err, sizeof(int)))) {
+    release_tc_plan(p);
+    return st;
+  }
+  cudaMemsetAsync(t.d_err, 0, sizeof(int), ctx->stream);
+  t.n_op_tasks = (int)op_tasks.size();
+  t.n_x_tasks = (int)x_tasks.size();
+  t.n_tiles1 = (int)tiles1.size();
+  t.n_tiles2 = (int)tiles2.size();
+  t.bytes_op = (double)a_op.size;
+  t.bytes_x = (double)a_x.size;
+  t.bytes_t = (double)a_t.size;
+  t.mma_flops1 = mma1;
+  t.mma_flops2 = mma2;
+  // operator images are built once here
+  cudaError_t e = tc_build_images(t.d_op_tasks, t.n_op_tasks, nullptr, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    release_tc_plan(p);
+    return cuda_check(ctx, e, "build operator images");
+  }
+  t.ready = true;
+  return HH_OK;
+}
+
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms) {
+  hh_ctx* ctx = p->ctx;
+  if (!p->tc.ready) {
+    int st = build_tc_plan(p);
+    if (st != HH_OK) return st;
+  }
+  hh_tc_plan& t = p->tc;
+  cudaEvent_t ev[4];
+  if (ms)
+    for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
+  if (ms) cudaEventRecord(ev[0], ctx->stream);
+  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, ctx->stream);
+  if (ms) cudaEventRecord(ev[1], ctx->stream);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, t.d_csegs, in, out, t.d_err, ctx->stream);
+  if (ms) cudaEventRecord(ev[2], ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, t.d_csegs, in, out, t.d_err, ctx->stream);
+  if (ms) cudaEventRecord(ev[3], ctx->stream);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, t.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (ms && e == cudaSuccess) {
+    cudaEventElapsedTime(&ms[0], ev[0], ev[3]);
+    cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
+    cudaEventElapsedTime(&ms[2], ev[2], ev[3]);
+    float conv = 0.f;
+    cudaEventElapsedTime(&conv, ev[0], ev[1]);
+    ms[3] = conv;
+  }
+  if (ms)
+    for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "tensor-core matvec");
+  if (herr != 0) {
+    cudaMemsetAsync(t.d_err, 0, sizeof(int), ctx->stream);
+    return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
+                                         std::to_string(herr) + ")");
+  }
+  return HH_OK;
+}
+
+}  // namespace hh
+
+// ---------------------------------------------------------------------------
+// Self-test of the tensor-core tile path on one dense complex product
+// C = A B (column-major, interleaved complex), used by the unit tests.
+extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C) {
+  using namespace hh;
+  if (!ctx || M < 1 || N < 1 || K < 1 || !A || !B || !C) return HH_ERR_INVALID;
+  const long long ia = img_bytes(M, K), ib = img_bytes(N, K);
+  void *dA = nullptr, *dB = nullptr, *dC = nullptr, *dimg = nullptr, *dtask = nullptr, *dtile = nullptr,
+       *dseg = nullptr, *derr = nullptr;
+  auto cleanup = [&]() {
+    void* q[] = {dA, dB, dC, dimg, dtask, dtile, dseg, derr};
+    for (void* x : q)
+      if (x) cudaFree(x);
+  };
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaMalloc(&dA, (size_t)M * K * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, (size_t)K * N * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dC, (size_t)M * N * 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dimg, (size_t)(ia + ib));
+  if (e == cudaSuccess) e = cudaMalloc(&derr, sizeof(int));
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_check(ctx, e, "selftest alloc");
+  }
+  cudaMemcpyAsync(dA, A, (size_t)M * K * 16, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dB, B, (size_t)K * N * 16, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(derr, 0, sizeof(int), s);
+  tc::ImgTask tk[2] = {};
+  tk[0].src = (long long)(uintptr_t)dA; tk[0].sbase = HH_BASE_ABS; tk[0].ld = M; tk[0].rows = M; tk[0].kc = K;
+  tk[0].r8 = r8(M); tk[0].k16 = k16(K); tk[0].trans = 0; tk[0].cre = 1.0; tk[0].dst = (long long)(uintptr_t)dimg;
+  tk[1].src = (long long)(uintptr_t)dB; tk[1].sbase = HH_BASE_ABS; tk[1].ld = K; tk[1].rows = N; tk[1].kc = K;
+  tk[1].r8 = r8(N); tk[1].k16 = k16(K); tk[1].trans = 1; tk[1].cre = 1.0;
+  tk[1].dst = (long long)(uintptr_t)dimg + ia;
+  std::vector<tc::Seg> segs;
+  std::vector<tc::Tile> tiles;
+  ImgRef ai, bi;
+  ai.rows = M; ai.kc = K; bi.rows = N; bi.kc = K;
+  for (int m0 = 0; m0 < M; m0 += 128)
+    for (int n0 = 0; n0 < N; n0 += 128) {
+      const int ntile = k16(std::min(128, N - n0));
+      tc::Seg sg{};
+      const int ar8 = r8(M), br8 = r8(N);
+      sg.a = tk[0].dst + (long long)(m0 / 8) * 256;
+      sg.b = tk[1].dst + (long long)(n0 / 8) * 256;
+      sg.a_plane = (long long)(ar8 / 8) * 256;
+      sg.b_plane = (long long)(br8 / 8) * 256;
+      sg.a_bytes = std::min(128, ar8 - m0) * 32;
+      sg.b_bytes = std::min(ntile, br8 - n0) * 32;
+      sg.nkc = k16(K) / 16;
+      tc::Tile tl{};
+      tl.seg0 = (int)segs.size();
+      tl.nseg = 1;
+      segs.push_back(sg);
+      tl.mode = 0;
+      tl.ntile = ntile;
+      tl.mrem = std::min(128, M - m0);
+      tl.nrem = std::min(128, N - n0);
+      tl.out = (long long)n0 * M + m0;
+      tl.ldo = M;
+      tl.m0 = m0;
+      tl.n0 = n0;
+      tiles.push_back(tl);
+    }
+  e = cudaMalloc(&dtask, sizeof(tk));
+  if (e == cudaSuccess) e = cudaMalloc(&dtile, tiles.size() * sizeof(tc::Tile));
+  if (e == cudaSuccess) e = cudaMalloc(&dseg, segs.size() * sizeof(tc::Seg));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dtask, tk, sizeof(tk), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dtile, tiles.data(), tiles.size() * sizeof(tc::Tile), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dseg, segs.data(), segs.size() * sizeof(tc::Seg), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = tc_build_images((tc::ImgTask*)dtask, 2, nullptr, s);
+  if (e == cudaSuccess)
+    e = tc_run_tiles((tc::Tile*)dtile, (int)tiles.size(), (tc::Seg*)dseg, nullptr, nullptr, (double2*)dC, (int*)derr, s);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(C, dC, (size_t)M * N * 16, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cleanup();
+  if (e != cudaSuccess) return cuda_check(ctx, e, "selftest");
+  if (herr) return fail(ctx, HH_ERR_TIMEOUT, "selftest: bounded wait ran out, code " + std::to_string(herr));
+  return HH_OK;
+}

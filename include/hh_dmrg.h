@@ -134,12 +134,15 @@ typedef struct {
 int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* env_bs,
                    const hh_wave_t* layout, int nterm, const hh_term_t* terms,
                    hh_plan_t** out);
-/* counts (12 doubles): [0] reference FLOPs per matvec (8MNK over the
+/* counts (16 doubles): [0] reference FLOPs per matvec (8MNK over the
  * reference's ZGEMM calls + 8 per element of the axpy terms), [1] FLOPs this
  * plan executes, [2] output tiles, [3] segments, [4] stage-1 products,
  * [5] scratch bytes, [6] operator bytes, [7] wave bytes (in + out),
  * [8] executed FLOPs of stage 1, [9] of stage 2, [10] reference FLOPs of the
- * first GEMM of the two-GEMM terms, [11] the remaining reference FLOPs.    */
+ * first GEMM of the two-GEMM terms, [11] the remaining reference FLOPs,
+ * [12], [13] BF16 tensor FLOPs issued by the split-precision stages 1 and 2
+ * (padding included), [14] bytes of its operand images, [15] 1 once the
+ * split-precision schedule has been built (first BF16X3 matvec).          */
 int hh_plan_stats(const hh_plan_t* p, double* counts);
 int hh_plan_free(hh_plan_t* p);
 
@@ -149,7 +152,8 @@ int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision);
  * buffers of the plan are reused between calls).                          */
 int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision);
 /* hh_matvec with CUDA events on the context stream around each stage;
- * ms[0] = whole matvec, ms[1] = stage 1 (left products), ms[2] = stage 2.  */
+ * ms[0] = whole matvec, ms[1] = stage 1 (left products), ms[2] = stage 2,
+ * ms[3] = BF16 split of the input wave (split-precision path only).     */
 int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision, float* ms);
 
 /* hh_matvec (FP64) that allocates nothing during the call.  No counterpart
@@ -174,6 +178,10 @@ int hh_host_free(void* ptr);
  * FP64 Rayleigh quotient of the final vector.                             */
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit,
                int precision, double* energy, int* iterations);
+
+/* Diagnostic: C = A B for dense complex column-major A (M x K), B (K x N)
+ * through the split-precision tensor-core tile kernel (host buffers).     */
+int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C);
 
 #ifdef __cplusplus
 }

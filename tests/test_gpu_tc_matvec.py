@@ -1,0 +1,58 @@
+"""Split-precision (three-way BF16, tcgen05) model_wave against the FP64 path on
+oracle DMRG superblocks, and its Lanczos energy against the FP64 Lanczos."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from hofstadter_hubbard_tsc_gb300 import _lib
+from hofstadter_hubbard_tsc_gb300.superblock import Superblock
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 5e-6  # FP32-level: 24-bit split operands, FP32 accumulation
+
+
+def test_tc_matvec_matches_fp64(device):
+    lat, d = H.record_superblocks(2, 6, 10, 32)
+    plat = H.product_lattice(lat)
+    for idx, rec in enumerate(d.record[::2]):
+        sys, env, sys_bs, env_bs, geo, sup, _ = rec
+        sb = Superblock(device, H.model(sys), H.model(env), H.basis(sys_bs), H.basis(env_bs),
+                        H.superbasis(sup), plat.geometry(sys.len, env.len))
+        x = H.wave(H.random_wave(sup, idx))
+        a = sb.model_wave(x, precision=_lib.HH_PREC_FP64).flat()
+        b = sb.model_wave(x, precision=_lib.HH_PREC_BF16X3).flat()
+        err = np.linalg.norm(a - b) / np.linalg.norm(a)
+        assert err < RTOL, (idx, err)
+        sb.free()
+
+
+def test_tc_matvec_synthetic_m200(device):
+    from hofstadter_hubbard_tsc_gb300.synth import Workload
+    wl = Workload(W=4, L=8, n_elec=28, m=200)
+    sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
+    rng = np.random.default_rng(3)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    sb.w_in.upload(psi)
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
+    ref = sb.w_out.download()
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_BF16X3))
+    got = sb.w_out.download()
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < RTOL
+    sb.free()
+
+
+def test_tc_lanczos_energy(device):
+    lat, d = H.record_superblocks(2, 6, 10, 32)
+    plat = H.product_lattice(lat)
+    rec = d.record[-3]
+    sys, env, sys_bs, env_bs, geo, sup, _ = rec
+    sb = Superblock(device, H.model(sys), H.model(env), H.basis(sys_bs), H.basis(env_bs),
+                    H.superbasis(sup), plat.geometry(sys.len, env.len))
+    start = H.wave(H.random_wave(sup, 9))
+    e64, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_FP64)
+    emx, _, _ = sb.lanczos_memo_new(start, 1e-8, precision=_lib.HH_PREC_BF16X3)
+    assert abs(emx - e64) / abs(e64) < 1e-8, (emx, e64)
+    sb.free()
