@@ -39,7 +39,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64", "bf16x3"])
+    p.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3"])
     p.add_argument("--m", type=int, default=2000)
     p.add_argument("--W", type=int, default=4)
     p.add_argument("--L", type=int, default=32)
