@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--ne", type=int, default=112)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=1, help="matvecs in the CPU baseline sample")
+    p.add_argument("--energy-check", action="store_true",
+                   help="also run Lanczos (100 vectors) in FP64 and in split precision from one start "
+                        "vector and report |dE/E| (outside the timed region)")
     return p.parse_args()
 
 
@@ -346,6 +349,20 @@ def main():
         dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, prec))
         hmx = w_out.download()
         line["rel_err_vs_fp64_gpu"] = float(np.linalg.norm(hmx - h64) / np.linalg.norm(h64))
+    if args.energy_check:
+        rs = np.random.default_rng(7)
+        start = rs.normal(size=wl.sup.dim) + 1j * rs.normal(size=wl.sup.dim)
+        res = {}
+        for name, pp in (("fp64", _lib.HH_PREC_FP64), ("split", prec)):
+            w_in.upload(start)
+            e, it = C.c_double(), C.c_int()
+            t0 = time.perf_counter()
+            dev.check(dev.lib.hh_lanczos(sb.plan, w_in.h, 1e-12, 100, pp, C.byref(e), C.byref(it)))
+            res[name] = (e.value, it.value, time.perf_counter() - t0)
+        line["energy_check"] = {"E_fp64": res["fp64"][0], "E_split_fp64_rayleigh": res["split"][0],
+                                "rel_dE": abs(res["split"][0] - res["fp64"][0]) / abs(res["fp64"][0]),
+                                "iterations": [res["fp64"][1], res["split"][1]],
+                                "lanczos_s": [res["fp64"][2], res["split"][2]]}
     if rank == 0 and not args.no_cpu_baseline:
         n = max(1, args.cpu_sample)
         dt, hpsi_cpu = cpu_matvec_timer(wl, psi, n)

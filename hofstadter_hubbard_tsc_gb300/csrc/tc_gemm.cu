@@ -5,9 +5,14 @@
 // 24 significand bits.  A complex tile product keeps the six split products
 // with i + j <= 2 for each of the four real products (re.re, im.im, re.im,
 // im.re): 24 tcgen05.mma (M=128, K=16, FP32 accumulate in TMEM) per 16 complex
-// k.  The dropped products are below 2^-24 relative.  D_re and D_im live in
-// TMEM columns [0,128) and [128,256); the -im.im product uses the negate-A bit
-// of the instruction descriptor.
+// k.  The dropped products are below 2^-24 relative.  The tensor core rounds
+// every accumulation toward zero, so the leading products x0 y0 and the five
+// correction products go to separate accumulators (main: TMEM columns
+// [0,256), correction: [256,512), re then im): the correction terms, 2^-8 of
+// the main ones, then cost no accumulator precision, and the bias of the main
+// accumulator grows with 2 instead of 12 accumulations per 16 complex k.  The
+// epilogue adds the two in FP64.  The -im.im product uses the negate-A bit of
+// the instruction descriptor.
 //
 // Operand "images": a complex matrix used as an MMA operand with R rows and
 // Kc complex k is stored as BF16 in the canonical K-major no-swizzle UMMA
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tslot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -255,9 +260,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t id_pos = idesc_bf16(t.ntile, false), id_neg = idesc_bf16(t.ntile, true);
-      const uint32_t d_re = tmem, d_im = tmem + 128;
+      const uint32_t d_re = tmem, d_im = tmem + 128, c_re = tmem + 256, c_im = tmem + 384;
       int it = 0;
-      uint32_t acc = 0;
+      uint32_t acc = 0, acc_c = 0;
       bool ok = true;
       for (int si = 0; si < t.nseg && ok; ++si) {
         const Seg sg = segs[t.seg0 + si];
@@ -277,11 +282,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
             for (int j = 0; j < 3 - i; ++j) {
               const uint64_t are = smem_desc(sa + i * kPlaneA), aim = smem_desc(sa + (3 + i) * kPlaneA);
               const uint64_t bre = smem_desc(sb + j * t.ntile * 32), bim = smem_desc(sb + (3 + j) * t.ntile * 32);
-              mma_bf16(d_re, are, bre, id_pos, acc);
-              mma_bf16(d_re, aim, bim, id_neg, 1u);
-              mma_bf16(d_im, are, bim, id_pos, acc);
-              mma_bf16(d_im, aim, bre, id_pos, 1u);
-              acc = 1u;
+              if (i + j == 0) {
+                mma_bf16(d_re, are, bre, id_pos, acc);
+                mma_bf16(d_re, aim, bim, id_neg, 1u);
+                mma_bf16(d_im, are, bim, id_pos, acc);
+                mma_bf16(d_im, aim, bre, id_pos, 1u);
+                acc = 1u;
+              } else {
+                mma_bf16(c_re, are, bre, id_pos, acc_c);
+                mma_bf16(c_re, aim, bim, id_neg, 1u);
+                mma_bf16(c_im, are, bim, id_pos, acc_c);
+                mma_bf16(c_im, aim, bre, id_pos, 1u);
+                acc_c = 1u;
+              }
             }
           }
           mma_commit(&empty[s]);
@@ -306,13 +319,15 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
     have = __all_sync(0xffffffffu, have);  // tcgen05.ld below is warp-collective
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
     for (int c0 = 0; c0 < t.ntile; c0 += 16) {
-      float re[16], im[16];
+      float re[16], im[16], cr[16], cm[16];
       if (have) {
         tmem_ld16(lane_base + c0, re);
         tmem_ld16(lane_base + 128 + c0, im);
+        tmem_ld16(lane_base + 256 + c0, cr);
+        tmem_ld16(lane_base + 384 + c0, cm);
       } else {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) re[j] = im[j] = 0.f;
+        for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
       }
       if (t.mode == 0) {
         if (row < t.mrem) {
@@ -321,7 +336,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
           for (int j = 0; j < 16; ++j) {
             const int col = c0 + j;
             if (col < t.nrem) {
-              double2 v = make_double2((double)re[j], (double)im[j]);
+              double2 v = make_double2((double)re[j] + (double)cr[j], (double)im[j] + (double)cm[j]);
               for (int ci = 0; ci < t.ncseg; ++ci) {
                 const hh_seg cs = csegs[t.cseg0 + ci];
                 const double2 x = base_in[cs.poff + (long long)(t.m0 + row) + (long long)(t.n0 + col) * cs.ldp];
@@ -346,9 +361,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
               const int cc = c0 + h * 8 + j;
               const bool valid = row < t.mrem && cc < t.nrem;
               __nv_bfloat16 s[3];
-              split3f(valid ? re[h * 8 + j] : 0.f, s);
+              split3f(valid ? re[h * 8 + j] + cr[h * 8 + j] : 0.f, s);
               pr[0][j] = s[0]; pr[1][j] = s[1]; pr[2][j] = s[2];
-              split3f(valid ? im[h * 8 + j] : 0.f, s);
+              split3f(valid ? im[h * 8 + j] + cm[h * 8 + j] : 0.f, s);
               pi[0][j] = s[0]; pi[1][j] = s[1]; pi[2][j] = s[2];
             }
             const size_t o = img_off(t.t_r8, r, t.n0 + c0 + h * 8);
@@ -366,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
   __syncthreads();
   fence_after();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
   }
 }
 
