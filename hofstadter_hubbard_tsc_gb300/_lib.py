@@ -86,6 +86,9 @@ SIGNATURES = {
     "hh_matvec_timed": (I, [P, P, P, I, C.POINTER(C.c_float)]),
     "hh_matvec_noalloc": (I, [P, P, P]),
     "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP]),
+    "hh_density_truncate": (I, [P, P, I, I, I, D, PP, IP, DP, DP, DP]),
+    "hh_renormalize": (I, [P, P, P, I, PP]),
+    "hh_wave_transform": (I, [P, I, P, P, P, P, P, P]),
     "hh_host_alloc": (I, [C.c_longlong, PP]),
     "hh_host_free": (I, [P]),
 }

@@ -78,6 +78,16 @@ class DBlock:
         return cls(dev, h, blk.len, blk.up_dif, blk.down_dif, qn[:blk.num].copy())
 
     @classmethod
+    def from_handle(cls, dev, h):
+        """Wraps a block the library created (takes ownership)."""
+        ln, up, dn, ns = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        dev.check(dev.lib.hh_block_info(h, C.byref(ln), C.byref(up), C.byref(dn), C.byref(ns), None))
+        qn = np.zeros((max(1, ns.value), 5), dtype=np.int32)
+        if ns.value:
+            dev.check(dev.lib.hh_block_qn(h, _ip(qn)))
+        return cls(dev, h, ln.value, up.value, dn.value, qn[:ns.value].copy())
+
+    @classmethod
     def zeros_like(cls, other):
         dev = other.dev
         h = C.c_void_p()

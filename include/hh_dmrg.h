@@ -179,6 +179,31 @@ int hh_host_free(void* ptr);
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit,
                int precision, double* energy, int* iterations);
 
+/* ------------------------------------------- density matrix and truncation
+ * Get_density_matrix_sys/env + Get_truncation_operator (code/get_den.f90:4-99,
+ * 184-428): rho = psi psi^H (side 0, sys) or psi^H psi (side 1, env) per
+ * sector, per-sector Hermitian eigensolve (ascending, eigenvector phases fixed
+ * so that the largest-modulus component is real positive), global descending
+ * sort (the reference's quicksort), normalisation to trace 1, selection from
+ * kept_min until the discarded weight is <= trun_err or kept_max states are
+ * kept.  *trun receives the truncation operator (enlarged x kept per sector,
+ * device resident); spectrum (may be NULL) receives the sorted normalised
+ * eigenvalues (total dimension of the side).                             */
+int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side, int kept_min, int kept_max,
+                        double trun_err, hh_block_t** trun, int* num_state, double* discarded,
+                        double* entropy, double* spectrum);
+/* update_trun_dia (dia = 1) / update_trun_ndia (dia = 0), code/update.f90:
+ * 1387-1605: *out = T^H O T sector pair by sector pair.                    */
+int hh_renormalize(hh_ctx_t* ctx, const hh_block_t* op, const hh_block_t* trun, int dia, hh_block_t** out);
+/* wave_trans_LR (dir 0) / wave_trans_RL (dir 1), code/warm_up.f90:1855-2170:
+ * the initial Lanczos vector of the next superblock from the last ground
+ * state; sys_bs/env_bs are the bases the reference passes (the new sys basis
+ * and the old env basis for LR, the old sys basis and the new env basis for
+ * RL); new_wave is overwritten and normalised.                            */
+int hh_wave_transform(hh_ctx_t* ctx, int dir, const hh_basis_t* sys_bs, const hh_basis_t* env_bs,
+                      const hh_block_t* sys_trun, const hh_block_t* env_trun, const hh_wave_t* old_wave,
+                      hh_wave_t* new_wave);
+
 /* Diagnostic: C = A B for dense complex column-major A (M x K), B (K x N)
  * through the split-precision tensor-core tile kernel (host buffers).     */
 int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C);
