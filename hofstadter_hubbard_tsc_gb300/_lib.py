@@ -87,6 +87,11 @@ SIGNATURES = {
     "hh_matvec_noalloc": (I, [P, P, P]),
     "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP]),
     "hh_density_truncate": (I, [P, P, I, I, I, D, PP, IP, DP, DP, DP]),
+    "hh_enlarge_operator": (I, [P, I, P, P, I, I, PP]),
+    "hh_ham_add_bond": (I, [P, P, P, P, I, P, DP, I, I]),
+    "hh_ham_add_product": (I, [P, P, P, P, DP]),
+    "hh_block_copy": (I, [P, P, PP]),
+    "hh_wave_random": (I, [P, C.c_ulonglong]),
     "hh_renormalize": (I, [P, P, P, I, PP]),
     "hh_wave_transform": (I, [P, I, P, P, P, P, P, P]),
     "hh_host_alloc": (I, [C.c_longlong, PP]),

@@ -287,6 +287,28 @@ int grid_for(long long n, int threads) {
 
 }  // namespace
 
+namespace {
+// counter-based generator (splitmix64) so that a seed gives the same wave on every GPU
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__global__ void random_kernel(double2* w, long long n, unsigned long long seed) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long a = mix64(seed ^ (2ull * i)), b = mix64(seed ^ (2ull * i + 1));
+    w[i] = make_double2((double)(a >> 11) * 0x1.0p-53, (double)(b >> 11) * 0x1.0p-53);
+  }
+}
+}  // namespace
+
+cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  random_kernel<<<grid_for(n, 256), 256, 0, s>>>(w, n, seed);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
                                      double2* base_out, cudaStream_t s) {
   if (L.tiles.empty()) return cudaSuccess;

@@ -523,6 +523,13 @@ int hh_wave_norm(const hh_wave_t* a, double* nrm) {
   return HH_OK;
 }
 
+int hh_wave_random(hh_wave_t* w, unsigned long long seed) {
+  if (!w) return HH_ERR_INVALID;
+  cudaError_t e = wave_fill_random(w->d, w->nelem * w->nbatch, seed, w->ctx->stream);
+  if (e != cudaSuccess) return cuda_check(w->ctx, e, "wave random");
+  return hh_wave_normalize(w);
+}
+
 int hh_wave_normalize(hh_wave_t* a) {
   if (!a) return HH_ERR_INVALID;
   double n = 0.0;

@@ -211,6 +211,7 @@ cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, do
 cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_out, cudaStream_t s);
 cudaError_t wave_axpy(double2* y, const double2* x, double a, long long n, cudaStream_t s);
 cudaError_t wave_scale(double2* y, double a, long long n, cudaStream_t s);
+cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, cudaStream_t s);
 cudaError_t krylov_dots(const double2* V, int k, long long ld, const double2* w, long long n,
                         double* d_out, cudaStream_t s);
 cudaError_t krylov_update(const double2* V, int k, long long ld, double2* w, long long n,

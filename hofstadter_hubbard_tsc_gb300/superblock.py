@@ -282,6 +282,15 @@ class Superblock:
         eigvec.set_flat(self.w_in.download())
         return e.value, it.value, eigvec
 
+    def lanczos_device(self, psi, lanzero, maxit=100, precision=None):
+        """lanczos_memo_new on a device-resident wave (DWave), in place: returns (E0, iterations)."""
+        p = self.precision if precision is None else precision
+        e = C.c_double()
+        it = C.c_int()
+        self.dev.check(self.dev.lib.hh_lanczos(self.plan, psi.h, float(lanzero), int(maxit), int(p),
+                                               C.byref(e), C.byref(it)))
+        return e.value, it.value
+
     def free(self):
         if getattr(self, "plan", None) is not None and self.dev.h is not None:
             self.dev.lib.hh_plan_free(self.plan)

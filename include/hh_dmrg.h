@@ -178,6 +178,9 @@ int hh_host_free(void* ptr);
  * FP64 Rayleigh quotient of the final vector.                             */
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit,
                int precision, double* energy, int* iterations);
+/* Fills a wave with uniform [0,1) real and imaginary parts from a seeded
+ * generator and normalises it (wave_initialize, code/space_info.f90:1079).  */
+int hh_wave_random(hh_wave_t* w, unsigned long long seed);
 
 /* ------------------------------------------- density matrix and truncation
  * Get_density_matrix_sys/env + Get_truncation_operator (code/get_den.f90:4-99,
@@ -203,6 +206,24 @@ int hh_renormalize(hh_ctx_t* ctx, const hh_block_t* op, const hh_block_t* trun, 
 int hh_wave_transform(hh_ctx_t* ctx, int dir, const hh_basis_t* sys_bs, const hh_basis_t* env_bs,
                       const hh_block_t* sys_trun, const hh_block_t* env_trun, const hh_wave_t* old_wave,
                       hh_wave_t* new_wave);
+
+/* ------------------------------------------------------- block enlargement
+ * Embeds an operator in the enlarged basis B (block + site), returning a new
+ * block: mode 0 update_block_dia, 1 update_site_dia, 2 update_block_ndia_sys/
+ * env, 3 update_site_ndia_sys/env (code/update.f90:419-1381); flag 'F'/'B',
+ * side 0 sys / 1 env (fermion sign conventions of the two sides).          */
+int hh_enlarge_operator(hh_ctx_t* ctx, int mode, const hh_block_t* op, const hh_basis_t* B, int flag, int side,
+                        hh_block_t** out);
+/* Get_hamiltonian_ndia (code/get_ham.f90:954-1152): ham += coef [O_block .
+ * O_site]^0 + h.c.; site_trans = 1 passes the site operator through
+ * block_transfer_trans; flags 'S' (sys) or 'E' (env).                     */
+int hh_ham_add_bond(hh_ctx_t* ctx, hh_block_t* ham, const hh_block_t* block, const hh_block_t* site,
+                    int site_trans, const hh_basis_t* B, const double* coef, int flag_sign, int flags);
+/* Get_hamiltonian_dia (code/get_ham.f90:852-941): ham += coef/sqrt(2S+1) O1 O2 */
+int hh_ham_add_product(hh_ctx_t* ctx, hh_block_t* ham, const hh_block_t* o1, const hh_block_t* o2,
+                       const double* coef);
+/* block_transfer (code/space_info.f90:100-129): device copy of a block     */
+int hh_block_copy(hh_ctx_t* ctx, const hh_block_t* src, hh_block_t** out);
 
 /* Diagnostic: C = A B for dense complex column-major A (M x K), B (K x N)
  * through the split-precision tensor-core tile kernel (host buffers).     */

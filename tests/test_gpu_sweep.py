@@ -1,0 +1,32 @@
+"""Whole DMRG on the GPU (enlargement, Lanczos, truncation, renormalisation,
+wave transforms all in libhh_dmrg.so) against exact diagonalisation and the
+oracle DMRG."""
+import numpy as np
+import pytest
+
+from oracle import ed
+from oracle.lattice import Lattice
+from hofstadter_hubbard_tsc_gb300 import _lib
+from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
+from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (4, 2, 6, 8.0, 0.25)])
+def test_gpu_dmrg_exact(device, W, L, ne, U, phi):
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11)
+    e = d.run(sweeps=1)
+    es, _ = ed.singlet_ground_energy(Lattice(W, L, U=U, phi=phi), ne)
+    assert e == pytest.approx(es, abs=1e-8)
+
+
+def test_gpu_dmrg_split_precision(device):
+    lat = SquareLattice(2, 6, U=8.0, phi=0.25)
+    d64 = GPUDMRG(device, lat, 10, kept_min=48, kept_max=48, trun_err=1e-14, lanzero=1e-10)
+    e64 = d64.run(sweeps=1)
+    dmx = GPUDMRG(device, lat, 10, kept_min=48, kept_max=48, trun_err=1e-14, lanzero=1e-8,
+                  precision=_lib.HH_PREC_BF16X3)
+    emx = dmx.run(sweeps=1)
+    assert abs(emx - e64) / abs(e64) < 1e-8, (emx, e64)
