@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--ne", type=int, default=112)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=1, help="matvecs in the CPU baseline sample")
+    p.add_argument("--no-sweep", action="store_true", help="skip the sweep-time measurement")
+    p.add_argument("--sweeps", type=int, default=1, help="finite sweeps timed per precision")
     p.add_argument("--energy-check", action="store_true",
                    help="also run Lanczos (100 vectors) in FP64 and in split precision from one start "
                         "vector and report |dE/E| (outside the timed region)")
@@ -186,6 +188,30 @@ def cpu_matvec_timer(wl, psi_flat, nrep):
         model_wave(sys_, env, sbs, ebs, vin, vout, geo, st)
     dt = (time.perf_counter() - t0) / nrep
     return dt, vout.flat()
+
+
+def sweep_bench(dev, args):
+    """Sweep time on the plain-method configuration: Hubbard 2x16 ladder, phi=1/4
+    (Landau gauge), t=1, U=8, N_e=28 (1/8 hole doping), singlet, m=256 kept
+    multiplets; warm-up plus the first two half sweeps, then ``args.sweeps``
+    timed finite sweeps, in FP64 (Lanczos tol 1e-10) and in split precision
+    (tol 1e-8: the split matvec's noise floor; energies are FP64 Rayleigh
+    quotients)."""
+    from hofstadter_hubbard_tsc_gb300 import _lib
+    from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
+    from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
+    lat = SquareLattice(2, 16, U=8.0, phi=0.25)
+    out = {"config": "hubbard-ladder-2x16-phi0.25-U8-Ne28-m256", "sweeps_timed": args.sweeps}
+    for name, prec, tol in (("fp64", _lib.HH_PREC_FP64, 1e-10), ("split", _lib.HH_PREC_BF16X3, 1e-8)):
+        d = GPUDMRG(dev, lat, 28, kept_min=256, kept_max=256, trun_err=1e-12, lanzero=tol, precision=prec, seed=11)
+        t0 = time.perf_counter()
+        e = d.run(sweeps=args.sweeps)
+        its = [r[3] for r in d.energies[-2 * (lat.N - 3):]]
+        out[name] = {"E0": e, "sweep_s": d.sweep_times, "total_s": time.perf_counter() - t0,
+                     "lanczos_iterations_last_sweep": int(np.sum(its)), "lanzero": tol}
+    out["rel_dE"] = abs(out["split"]["E0"] - out["fp64"]["E0"]) / abs(out["fp64"]["E0"])
+    out["sweep_speedup_split_vs_fp64"] = out["fp64"]["sweep_s"][-1] / out["split"]["sweep_s"][-1]
+    return out
 
 
 def run_reference(args, rank, ws, dist):
@@ -349,6 +375,8 @@ def main():
         dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, prec))
         hmx = w_out.download()
         line["rel_err_vs_fp64_gpu"] = float(np.linalg.norm(hmx - h64) / np.linalg.norm(h64))
+    if rank == 0 and not args.no_sweep:
+        line["sweep"] = sweep_bench(dev, args)
     if args.energy_check:
         rs = np.random.default_rng(7)
         start = rs.normal(size=wl.sup.dim) + 1j * rs.normal(size=wl.sup.dim)
