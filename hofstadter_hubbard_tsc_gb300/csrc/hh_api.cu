@@ -190,6 +190,7 @@ int hh_finalize(hh_ctx_t* ctx) {
   cudaStreamSynchronize(ctx->stream);
   if (ctx->d_red) cudaFree(ctx->d_red);
   if (ctx->h_red) cudaFreeHost(ctx->h_red);
+  release_step_resources(ctx);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return HH_OK;
@@ -684,9 +685,37 @@ int hh_host_free(void* ptr) {
 }
 
 // ----------------------------------------------------------------- Lanczos
+static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int first_precision, int precision,
+                        double* energy, int* iterations);
+
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int precision, double* energy,
                int* iterations) {
   if (!p || !psi || !energy || psi->nelem != p->nelem || maxit < 1) return HH_ERR_INVALID;
+  if (precision == HH_PREC_FP64)
+    return lanczos_core(p, psi, lanzero, maxit, precision, precision, energy, iterations);
+  if (precision != HH_PREC_BF16X3) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
+  // Split precision, two passes.  (1) Lanczos on the tensor-core matvec down
+  // to its noise floor: Ritz value change <= max(lanzero, 1e-8).  (2) Lanczos
+  // restarted from that vector psi_m whose first product H psi_m is FP64 and
+  // whose later ones are split precision.  The FP64 residual H psi_m - a0 psi_m
+  // starts the correction space and the Gram-Schmidt step keeps every later
+  // vector orthogonal to psi_m and to it, so the tridiagonal's first row is
+  // FP64-exact; the split-precision entries enter the Ritz value weighted by
+  // the squares of the correction coefficients (about the vector error of
+  // psi_m, 1e-4), which takes the energy to FP64 accuracy at the cost of one
+  // FP64 matvec.
+  double e_mixed = 0.0;
+  int it1 = 0, it2 = 0;
+  int st = lanczos_core(p, psi, std::max(lanzero, 1e-8), maxit, precision, precision, &e_mixed, &it1);
+  if (st) return st;
+  st = lanczos_core(p, psi, lanzero, maxit, HH_PREC_FP64, precision, energy, &it2);
+  if (st) return st;
+  if (iterations) *iterations = it1 + it2;
+  return HH_OK;
+}
+
+static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int first_precision, int precision,
+                        double* energy, int* iterations) {
   hh_ctx* ctx = p->ctx;
   if (maxit > 100) maxit = 100;  // loop_in (code/lanczos.f90:14)
   const long long n = p->nelem;
@@ -717,7 +746,7 @@ int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int prec
   if ((st = dot(slot(0), slot(0), &nrm2))) return st;
   vv.push_back(nrm2);
   int last = 1;
-  if ((st = matvec_dev(p, slot(0), slot(1), precision))) return st;
+  if ((st = matvec_dev(p, slot(0), slot(1), first_precision))) return st;
   double a0 = 0.0;
   if ((st = dot(slot(0), slot(1), &a0))) return st;
   alpha.push_back(a0);
@@ -771,11 +800,6 @@ int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int prec
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos final combination");
   if ((st = hh_wave_normalize(psi))) return st;
-  if (precision != HH_PREC_FP64) {
-    // FP64 Rayleigh quotient of the split-precision ground state
-    if ((st = matvec_dev(p, psi->d, slot(0), HH_PREC_FP64))) return st;
-    if ((st = dot(psi->d, slot(0), &e0))) return st;
-  }
   *energy = e0;
   if (iterations) *iterations = last;
   return HH_OK;

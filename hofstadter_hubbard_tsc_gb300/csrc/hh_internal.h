@@ -41,6 +41,9 @@ struct hh_ctx {
   size_t red_cap = 0;
   double* h_red = nullptr;  // pinned
   size_t h_red_cap = 0;
+  // density-matrix eigensolver state (streams, solver handles, workspace),
+  // created on first use (eig.cu)
+  void* eig = nullptr;
 };
 
 struct hh_sub_qn {
@@ -225,4 +228,11 @@ void release_tc_plan(hh_plan* plan);
 int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms);
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
 int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
+// Eigenvalues (ascending, into *d_w: sector k's at the sum of the earlier
+// dims) and eigenvectors (in place) of the Hermitian sectors A + offs[k] of
+// size dims[k]; *d_w is context-owned scratch valid until the next call.
+int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>& offs,
+                          const std::vector<int>& dims, double** d_w);
+// frees the eigensolver state held by the context
+void release_step_resources(hh_ctx* ctx);
 }  // namespace hh

@@ -4,11 +4,9 @@
 // transformations (wave_trans_LR/RL, code/warm_up.f90:1855-2170).
 //
 // Products run on the FP64 grouped segment GEMM; the per-sector Hermitian
-// eigensolve uses cuSOLVER (zheevd, ascending eigenvalues like the ZHEEV call
-// of code/get_den.f90:242).  The global sort and the selection of kept states
-// are host work on the eigenvalues only.
-#include <cusolverDn.h>
-
+// eigensolves (ascending eigenvalues like the ZHEEV call of
+// code/get_den.f90:242) are eig.cu's batched solver.  The global sort and the
+// selection of kept states are host work on the eigenvalues only.
 #include <algorithm>
 #include <cmath>
 #include <map>
@@ -73,47 +71,6 @@ hh_seg gemm_seg(long long poff, int pbase, int ldp, int opP, long long qoff, int
 
 long long addr(const hh_block* b, int j) { return (long long)(uintptr_t)(b->d + b->subs[j].off); }
 
-// Rotates every eigenvector so that its largest-modulus component (first one
-// on ties) is real and positive: one fixed phase convention for the oracle
-// and this library, where LAPACK implementations differ.
-__global__ void canonical_phase_kernel(double2* V, int n) {
-  const int col = blockIdx.x;
-  double2* v = V + (long long)col * n;
-  __shared__ double best[256];
-  __shared__ int bidx[256];
-  double m = -1.0;
-  int mi = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double a = v[i].x * v[i].x + v[i].y * v[i].y;
-    if (a > m) {
-      m = a;
-      mi = i;
-    }
-  }
-  best[threadIdx.x] = m;
-  bidx[threadIdx.x] = mi;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      double o = best[threadIdx.x + s];
-      int oi = bidx[threadIdx.x + s];
-      if (o > best[threadIdx.x] || (o == best[threadIdx.x] && oi < bidx[threadIdx.x])) {
-        best[threadIdx.x] = o;
-        bidx[threadIdx.x] = oi;
-      }
-    }
-    __syncthreads();
-  }
-  const double2 p = v[bidx[0]];
-  const double a = sqrt(p.x * p.x + p.y * p.y);
-  if (a == 0.0) return;
-  const double2 ph = make_double2(p.x / a, -p.y / a);  // conj(p)/|p|
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double2 x = v[i];
-    v[i] = make_double2(x.x * ph.x - x.y * ph.y, x.x * ph.y + x.y * ph.x);
-  }
-}
-
 // QuickSort_Double of the reference (code/update.f90:322-368): descending,
 // middle pivot, Hoare partition, index array carried along.  Restated exactly
 // so that ties among eigenvalues of different sectors are resolved in the
@@ -149,6 +106,7 @@ int make_block(hh_ctx* ctx, int len, int up_dif, int down_dif, const std::vector
 
 using namespace hh;
 
+
 extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side, int kept_min, int kept_max,
                                    double trun_err, hh_block_t** trun_out, int* num_state_out, double* discarded,
                                    double* entropy, double* spectrum) {
@@ -179,81 +137,26 @@ extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side
     hh_block_free(den);
     return st;
   }
-  // ---- per-sector eigensolve (ZHEEV 'V','U', ascending)
-  cusolverDnHandle_t h = nullptr;
-  if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
-    hh_block_free(den);
-    return fail(ctx, HH_ERR_CUDA, "cusolverDnCreate failed");
-  }
-  cusolverDnSetStream(h, ctx->stream);
-  int maxd = 0;
-  long long nev = 0;
-  for (const auto& s : den->subs) {
-    maxd = std::max(maxd, s.sdim);
-    nev += s.sdim;
-  }
+  // ---- per-sector eigensolve (ZHEEV 'V','U', ascending; code/get_den.f90:242)
   double* d_w = nullptr;
-  int* d_info = nullptr;
-  cuDoubleComplex* d_work = nullptr;
-  int lwork = 0;
-  cudaError_t e = cudaMalloc(&d_w, std::max<long long>(1, nev) * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&d_info, sizeof(int) * std::max<size_t>(1, den->subs.size()));
-  if (e == cudaSuccess && maxd > 0) {
-    cusolverDnZheevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, maxd,
-                                reinterpret_cast<cuDoubleComplex*>(den->d), maxd, d_w, &lwork);
-    e = cudaMalloc(&d_work, std::max(1, lwork) * sizeof(cuDoubleComplex));
+  long long nev = 0;
+  std::vector<long long> offs;
+  std::vector<int> dims;
+  for (const auto& sq : den->subs) {
+    offs.push_back(sq.off);
+    dims.push_back(sq.sdim);
+    nev += sq.sdim;
   }
-  auto cleanup = [&]() {
-    if (d_w) cudaFree(d_w);
-    if (d_info) cudaFree(d_info);
-    if (d_work) cudaFree(d_work);
-    cusolverDnDestroy(h);
-  };
-  if (e != cudaSuccess) {
-    cleanup();
+  if ((st = eig_hermitian_sectors(ctx, den->d, offs, dims, &d_w))) {
     hh_block_free(den);
-    return cuda_check(ctx, e, "density workspace");
-  }
-  long long woff = 0;
-  for (size_t k = 0; k < den->subs.size(); ++k) {
-    const int n = den->subs[k].sdim;
-    if (n > 0) {
-      int lw = 0;
-      cusolverDnZheevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
-                                  reinterpret_cast<cuDoubleComplex*>(den->d + den->subs[k].off), n, d_w + woff, &lw);
-      if (lw > lwork) {
-        cudaFree(d_work);
-        lwork = lw;
-        cudaMalloc(&d_work, lwork * sizeof(cuDoubleComplex));
-      }
-      cusolverStatus_t cs = cusolverDnZheevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
-                                             reinterpret_cast<cuDoubleComplex*>(den->d + den->subs[k].off), n,
-                                             d_w + woff, d_work, lwork, d_info + k);
-      if (cs != CUSOLVER_STATUS_SUCCESS) {
-        cleanup();
-        hh_block_free(den);
-        return fail(ctx, HH_ERR_NUMERIC, "cusolverDnZheevd failed");
-      }
-      canonical_phase_kernel<<<n, 256, 0, ctx->stream>>>(den->d + den->subs[k].off, n);
-    }
-    woff += n;
+    return st;
   }
   std::vector<double> w(std::max<long long>(1, nev));
-  std::vector<int> info(den->subs.size() + 1, 0);
-  e = cudaMemcpyAsync(w.data(), d_w, nev * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess && !den->subs.empty())
-    e = cudaMemcpyAsync(info.data(), d_info, den->subs.size() * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  cleanup();
+  cudaError_t e = cudaMemcpy(w.data(), d_w, nev * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) {
     hh_block_free(den);
-    return cuda_check(ctx, e, "density eigensolve");
+    return cuda_check(ctx, e, "density eigenvalues");
   }
-  for (size_t k = 0; k < den->subs.size(); ++k)
-    if (info[k] != 0) {
-      hh_block_free(den);
-      return fail(ctx, HH_ERR_NUMERIC, "zheevd did not converge in sector " + std::to_string(k));
-    }
   // ---- global sort, renormalisation, selection (code/get_den.f90:268-311)
   std::vector<double> arr(w.begin(), w.begin() + nev);
   std::vector<int> idx(nev);

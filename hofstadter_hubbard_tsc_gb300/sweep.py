@@ -9,6 +9,8 @@ reference writes them to disk per length.
 """
 import ctypes as C
 import time
+from collections import defaultdict
+from contextlib import contextmanager
 
 import numpy as np
 
@@ -60,6 +62,15 @@ class GPUDMRG:
         self.guess_hook = guess_hook
         self.verbose = verbose
         self._nrand = 0
+        self.phase_s = defaultdict(float)   # host wall seconds per phase of a step
+
+    @contextmanager
+    def _phase(self, name):
+        t0 = time.perf_counter()
+        try:
+            yield
+        finally:
+            self.phase_s[name] += time.perf_counter() - t0
 
     # ------------------------------------------------------------------ setup
     def _site_model(self, geo, lat_idx):
@@ -76,8 +87,13 @@ class GPUDMRG:
         return TotalBlock(1, 0, 0, [SubBlock(s.num_up, s.num_down, 0, u * s.mat) for s in self.st.double.subs])
 
     def _basis(self, model):
-        b = get_basis(_sector_block(model.ham), self.sz_host)
-        return b, DBasis(self.dev, b)
+        with self._phase("basis"):
+            b = get_basis(_sector_block(model.ham), self.sz_host)
+            return b, DBasis(self.dev, b)
+
+    def _super(self, sys_bs, env_bs, tot_up, tot_down):
+        with self._phase("basis"):
+            return get_super_basis(sys_bs, env_bs, tot_up, tot_down)
 
     def _new_wave(self, sup):
         return DWave(self.dev, sup.array(), sup.sys_len, sup.env_len)
@@ -91,6 +107,10 @@ class GPUDMRG:
     # --------------------------------------------------------- enlargement
     def _enlarge(self, pre, basis, dbasis, trun, geo, side, mshift):
         """Get_Hamiltonian_Sys (side 'sys') / Get_Hamiltonian_Env ('env') on the device."""
+        with self._phase("enlarge"):
+            return self._enlarge_impl(pre, basis, dbasis, trun, geo, side, mshift)
+
+    def _enlarge_impl(self, pre, basis, dbasis, trun, geo, side, mshift):
         dev, lat, st = self.dev, self.lat, self.d_st
         sd = 0 if side == "sys" else 1
 
@@ -181,13 +201,18 @@ class GPUDMRG:
     # ---------------------------------------------------------------- solve
     def _solve(self, sys, env, sys_bs, env_bs, geo, sup, psi):
         t0 = time.perf_counter()
-        sb = Superblock(self.dev, sys, env, sys_bs, env_bs, sup, geo, self.st, precision=self.precision)
+        with self._phase("plan"):
+            sb = Superblock(self.dev, sys, env, sys_bs, env_bs, sup, geo, self.st, precision=self.precision)
         if self.guess_hook is not None:
-            self.guess_hook(self, sb, psi, "before")
-        e0, it = sb.lanczos_device(psi, self.lanzero, self.maxit)
+            with self._phase("guess"):
+                self.guess_hook(self, sb, psi, "before")
+        with self._phase("lanczos"):
+            e0, it = sb.lanczos_device(psi, self.lanzero, self.maxit)
         if self.guess_hook is not None:
-            self.guess_hook(self, sb, psi, "after")
-        sb.free()
+            with self._phase("guess"):
+                self.guess_hook(self, sb, psi, "after")
+        with self._phase("plan"):
+            sb.free()
         dt = time.perf_counter() - t0
         self.energies.append((sys.len, env.len, e0, it, dt))
         if self.verbose:
@@ -199,7 +224,9 @@ class GPUDMRG:
             # identity truncation (code/warm_up.f90:1432-1439)
             subs = [SubBlock(s.new_num_up, s.new_num_down, 0, np.eye(s.dim)) for s in basis.sectors]
             return DBlock.upload(self.dev, TotalBlock(basis.len, 0, 0, subs))
-        trun, ns, err, ent, _ = density_truncate(self.dev, wave, side, self.kept_min, self.kept_max, self.trun_err)
+        with self._phase("truncate"):
+            trun, ns, err, ent, _ = density_truncate(self.dev, wave, side, self.kept_min, self.kept_max,
+                                                     self.trun_err)
         self.last_trunc = (ns, err, ent)
         return trun
 
@@ -219,7 +246,7 @@ class GPUDMRG:
             tot_up = int(1.0 * (sys_bs.len + env_bs.len) / N * self.n_elec + 0.001)
             tot_up -= tot_up % 2
             tot_up = min(tot_up, self.n_elec)
-            sup = get_super_basis(sys_bs, env_bs, tot_up, 0)
+            sup = self._super(sys_bs, env_bs, tot_up, 0)
             wv = self._random_wave(sup)
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
             strun = self._trun(wv, SYS, sys_bs, dsys_bs)
@@ -242,7 +269,7 @@ class GPUDMRG:
         geo = self.lat.geometry(sys.len, env.len)
         sys_bs, dsys_bs = self._basis(sys)
         env_bs, denv_bs = self._basis(env)
-        sup = get_super_basis(sys_bs, env_bs, self.n_elec, 0)
+        sup = self._super(sys_bs, env_bs, self.n_elec, 0)
         if self.wave is not None and self.wave[1].sys_len == sys_bs.len and self.wave[1].env_len == env_bs.len:
             wv = self.wave[0]
         elif self.wave is not None:
@@ -263,10 +290,11 @@ class GPUDMRG:
             env_bs, denv_bs = self.env_bases[N - label - 1]
             env = self.env_models[N - label - 2].copy()
             geo = self.lat.geometry(sys.len, env.len)
-            sup = get_super_basis(sys_bs, env_bs, self.n_elec, 0)
+            sup = self._super(sys_bs, env_bs, self.n_elec, 0)
             wv = self._new_wave(sup)
-            wave_trans(self.dev, "LR", dsys_bs, self.env_bases[N - label][1], strun,
-                       self.env_truns[N - label - 1], self.wave[0], wv)
+            with self._phase("transform"):
+                wave_trans(self.dev, "LR", dsys_bs, self.env_bases[N - label][1], strun,
+                           self.env_truns[N - label - 1], self.wave[0], wv)
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
             strun = self._trun(wv, SYS, sys_bs, dsys_bs, force_truncate=True)
             self._enlarge(sys, sys_bs, dsys_bs, strun, geo, "sys", 0)
@@ -284,7 +312,7 @@ class GPUDMRG:
         geo = self.lat.geometry(sys.len, env.len)
         sys_bs, dsys_bs = self._basis(sys)
         env_bs, denv_bs = self._basis(env)
-        sup = get_super_basis(sys_bs, env_bs, self.n_elec, 0)
+        sup = self._super(sys_bs, env_bs, self.n_elec, 0)
         if self.wave is not None and self.wave[1].sys_len == sys_bs.len and self.wave[1].env_len == env_bs.len:
             wv = self.wave[0]
         elif self.wave is not None:
@@ -303,12 +331,13 @@ class GPUDMRG:
         while label - 1 >= end_id:
             sys_bs, dsys_bs = self.sys_bases[label]
             env_bs, denv_bs = self._basis(env)
-            sup = get_super_basis(sys_bs, env_bs, self.n_elec, 0)
+            sup = self._super(sys_bs, env_bs, self.n_elec, 0)
             sys = self.sys_models[label - 1].copy()
             geo = self.lat.geometry(sys.len, env.len)
             wv = self._new_wave(sup)
-            wave_trans(self.dev, "RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label], etrun,
-                       self.wave[0], wv)
+            with self._phase("transform"):
+                wave_trans(self.dev, "RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label], etrun,
+                           self.wave[0], wv)
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
             etrun = self._trun(wv, ENV, env_bs, denv_bs, force_truncate=True)
             self._enlarge(env, env_bs, denv_bs, etrun, geo, "env", sys.len + 1)
@@ -331,6 +360,7 @@ class GPUDMRG:
         self.right_to_left(N - 2, 1)
         times = []
         for _ in range(sweeps):
+            self.phase_s.clear()
             t0 = time.perf_counter()
             self.sweep()
             times.append(time.perf_counter() - t0)

@@ -174,8 +174,11 @@ int hh_host_free(void* ptr);
 /* lanczos_memo_new (code/lanczos.f90:4-177), levels = 1.  psi is the start
  * vector on entry and the ground state on exit; lanzero is the breakdown and
  * convergence threshold; maxit <= 100 is loop_in.  With HH_PREC_BF16X3 the
- * Krylov recurrence runs on the split-precision matvec and the energy is the
- * FP64 Rayleigh quotient of the final vector.                             */
+ * Krylov recurrence first runs on the split-precision matvec until the Ritz
+ * value moves by <= max(lanzero, 1e-8); a second Lanczos restarted from that
+ * vector takes its first product in FP64 and the rest in split precision and
+ * converges to lanzero (one FP64 matvec per call); *iterations counts the
+ * Krylov vectors of both passes.                                          */
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit,
                int precision, double* energy, int* iterations);
 /* Fills a wave with uniform [0,1) real and imaginary parts from a seeded

@@ -51,6 +51,50 @@ def test_density_truncate(device, side):
             np.testing.assert_allclose(pg[k], po[k], atol=1e-10)
 
 
+@pytest.mark.parametrize("side", [0, 1])
+def test_density_truncate_sector_sizes(device, side):
+    """Sector sizes on both sides of the eigensolver's switch from its Jacobi
+    kernel to zheevd (48 states) and well past it, with a spectrum decaying over
+    many decades like a DMRG density matrix."""
+    from oracle.blocks import SSector, Super, WSub, Wave
+    dims = [(1, 2), (7, 9), (30, 12), (47, 60), (48, 40), (49, 50), (112, 120), (150, 160), (300, 280)]
+    rng = np.random.default_rng(21)
+    subs = []
+    for k, (a, b) in enumerate(dims):
+        ss = SSector(2 * k, k % 3, 40 - 2 * k, k % 3, a, b)
+        decay = np.exp(-np.arange(max(a, b)) / 6.0)
+        v = rng.normal(size=(a, b)) + 1j * rng.normal(size=(a, b))
+        v *= (decay[:a, None] if side == 0 else decay[None, :b]) * np.exp(-k / 2.0)
+        subs.append(WSub(ss, v))
+    psi = Wave(3, 3, subs)
+    nrm = np.sqrt(sum(np.vdot(w.vec, w.vec).real for w in subs))
+    for w in subs:
+        w.vec /= nrm
+    den = get_density_matrix_sys(psi) if side == 0 else get_density_matrix_env(psi)
+    kmin, kmax = 150, 260
+    o_trun, o_ns, o_err, o_ent, o_spec = get_truncation_operator(den, kmin, kmax, 1e-10)
+    trun, ns, err, ent, spec = step.density_truncate(device, _dwave(device, psi), side, kmin, kmax, 1e-10)
+    assert ns == o_ns
+    assert err == pytest.approx(o_err, abs=1e-12)
+    assert ent == pytest.approx(o_ent, abs=1e-12)
+    np.testing.assert_allclose(spec, o_spec, atol=5e-14)
+    g = trun.download()
+    assert [(s.num_up, s.num_down, s.row_dim, s.sdim) for s in g.subs] == \
+           [(s.num_up, s.num_down, s.row_dim, s.sdim) for s in o_trun.subs]
+    rho = {(s.num_up, s.num_down): s.mat for s in den.subs}
+    for sg in g.subs:
+        # every kept column is an eigenvector of its sector, the columns are
+        # orthonormal and each carries the canonical phase
+        v = sg.mat
+        r = rho[(sg.num_up, sg.num_down)]
+        lam = np.einsum("ij,ik,kj->j", v.conj(), r, v).real
+        np.testing.assert_allclose(r @ v - v * lam, 0.0, atol=5e-14)
+        np.testing.assert_allclose(v.conj().T @ v, np.eye(sg.sdim), atol=1e-12)
+        top = v[np.argmax(np.abs(v), axis=0), np.arange(sg.sdim)]
+        np.testing.assert_allclose(top.imag, 0.0, atol=1e-15)
+        assert np.all(top.real > 0)
+
+
 def test_renormalize(device):
     lat, d = H.record_superblocks(2, 6, 10, 24)
     st = odmrg.SiteOps("hubbard")
