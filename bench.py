@@ -194,22 +194,34 @@ def sweep_bench(dev, args):
     """Sweep time on the plain-method configuration: Hubbard 2x16 ladder, phi=1/4
     (Landau gauge), t=1, U=8, N_e=28 (1/8 hole doping), singlet, m=256 kept
     multiplets; warm-up plus the first two half sweeps, then ``args.sweeps``
-    timed finite sweeps, in FP64 and in split precision, both with Lanczos
-    tol 1e-10 (the split solver iterates on the tensor-core matvec to 1e-8,
-    its noise floor, then finishes with a short FP64 Lanczos)."""
+    timed finite sweeps, in FP64 and in split precision with the learned guess
+    corrector, both with Lanczos tol 1e-10 (the split solver iterates on the
+    tensor-core matvec to 1e-8, its noise floor, then restarts with one FP64
+    product).  The corrector trains between sweeps, outside the sweep timer;
+    its training time is reported."""
     from hofstadter_hubbard_tsc_gb300 import _lib
     from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
     from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
     lat = SquareLattice(2, 16, U=8.0, phi=0.25)
     out = {"config": "hubbard-ladder-2x16-phi0.25-U8-Ne28-m256", "sweeps_timed": args.sweeps}
+    from hofstadter_hubbard_tsc_gb300.guess import LearnedGuess
     for name, prec, tol in (("fp64", _lib.HH_PREC_FP64, 1e-10), ("split", _lib.HH_PREC_BF16X3, 1e-10)):
-        d = GPUDMRG(dev, lat, 28, kept_min=256, kept_max=256, trun_err=1e-12, lanzero=tol, precision=prec, seed=11)
+        hook = LearnedGuess(dev, lat.N, 28) if name == "split" else None
+        d = GPUDMRG(dev, lat, 28, kept_min=256, kept_max=256, trun_err=1e-12, lanzero=tol, precision=prec, seed=11,
+                    guess_hook=hook)
         t0 = time.perf_counter()
         e = d.run(sweeps=args.sweeps)
         its = [r[3] for r in d.energies[-2 * (lat.N - 3):]]
         out[name] = {"E0": e, "sweep_s": d.sweep_times, "total_s": time.perf_counter() - t0,
                      "lanczos_iterations_last_sweep": int(np.sum(its)), "lanzero": tol,
                      "phase_s_last_sweep": {k: round(v, 4) for k, v in d.phase_s.items()}}
+        if hook is not None:
+            out[name]["learned_guess"] = {
+                "samples": int(len(hook.data()[1])), "train_s": round(hook.train_s, 4),
+                "held_out_hellinger_corrected": hook.val[0] if hook.val else None,
+                "held_out_hellinger_plain": hook.val[1] if hook.val else None,
+                "applied": bool(hook.enabled), "corrected_steps": int(sum(1 for r in hook.log if r[2]))}
+            hook.free()
     out["rel_dE"] = abs(out["split"]["E0"] - out["fp64"]["E0"]) / abs(out["fp64"]["E0"])
     out["sweep_speedup_split_vs_fp64"] = out["fp64"]["sweep_s"][-1] / out["split"]["sweep_s"][-1]
     return out

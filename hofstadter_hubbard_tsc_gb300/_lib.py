@@ -49,6 +49,7 @@ D = C.c_double
 IP = C.POINTER(C.c_int)
 DP = C.POINTER(C.c_double)
 LLP = C.POINTER(C.c_longlong)
+FP = C.POINTER(C.c_float)
 
 # name -> (restype, argtypes); every symbol declared in include/hh_dmrg.h
 SIGNATURES = {
@@ -94,6 +95,16 @@ SIGNATURES = {
     "hh_wave_random": (I, [P, C.c_ulonglong]),
     "hh_renormalize": (I, [P, P, P, I, PP]),
     "hh_wave_transform": (I, [P, I, P, P, P, P, P, P]),
+    "hh_mlp_create": (I, [P, I, C.c_ulonglong, PP]),
+    "hh_mlp_free": (I, [P]),
+    "hh_mlp_nparams": (I, [P, IP]),
+    "hh_mlp_get_params": (I, [P, FP]),
+    "hh_mlp_set_params": (I, [P, FP]),
+    "hh_mlp_forward": (I, [P, FP, I, FP]),
+    "hh_mlp_loss_grad": (I, [P, FP, FP, FP, I, FP, FP]),
+    "hh_mlp_train": (I, [P, FP, FP, FP, I, I, C.c_float, FP]),
+    "hh_wave_sector_norms": (I, [P, DP]),
+    "hh_wave_scale_sectors": (I, [P, DP]),
     "hh_host_alloc": (I, [C.c_longlong, PP]),
     "hh_host_free": (I, [P]),
 }

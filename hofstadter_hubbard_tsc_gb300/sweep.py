@@ -62,6 +62,7 @@ class GPUDMRG:
         self.guess_hook = guess_hook
         self.verbose = verbose
         self._nrand = 0
+        self.guess_kind = "random"     # how the next Lanczos start vector was made
         self.phase_s = defaultdict(float)   # host wall seconds per phase of a step
 
     @contextmanager
@@ -248,6 +249,7 @@ class GPUDMRG:
             tot_up = min(tot_up, self.n_elec)
             sup = self._super(sys_bs, env_bs, tot_up, 0)
             wv = self._random_wave(sup)
+            self.guess_kind = "random"
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
             strun = self._trun(wv, SYS, sys_bs, dsys_bs)
             etrun = self._trun(wv, ENV, env_bs, denv_bs)
@@ -272,12 +274,15 @@ class GPUDMRG:
         sup = self._super(sys_bs, env_bs, self.n_elec, 0)
         if self.wave is not None and self.wave[1].sys_len == sys_bs.len and self.wave[1].env_len == env_bs.len:
             wv = self.wave[0]
+            self.guess_kind = "previous"
         elif self.wave is not None:
             wv = self._new_wave(sup)
             wave_trans(self.dev, "LR", dsys_bs, self.env_bases[N - label][1], self.sys_truns[label],
                        self.env_truns[N - label - 1], self.wave[0], wv)
+            self.guess_kind = "transformed"
         else:
             wv = self._random_wave(sup)
+            self.guess_kind = "random"
         self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
         strun = self._trun(wv, SYS, sys_bs, dsys_bs, force_truncate=True)
         self._enlarge(sys, sys_bs, dsys_bs, strun, geo, "sys", 0)
@@ -295,6 +300,7 @@ class GPUDMRG:
             with self._phase("transform"):
                 wave_trans(self.dev, "LR", dsys_bs, self.env_bases[N - label][1], strun,
                            self.env_truns[N - label - 1], self.wave[0], wv)
+            self.guess_kind = "transformed"
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
             strun = self._trun(wv, SYS, sys_bs, dsys_bs, force_truncate=True)
             self._enlarge(sys, sys_bs, dsys_bs, strun, geo, "sys", 0)
@@ -315,12 +321,15 @@ class GPUDMRG:
         sup = self._super(sys_bs, env_bs, self.n_elec, 0)
         if self.wave is not None and self.wave[1].sys_len == sys_bs.len and self.wave[1].env_len == env_bs.len:
             wv = self.wave[0]
+            self.guess_kind = "previous"
         elif self.wave is not None:
             wv = self._new_wave(sup)
             wave_trans(self.dev, "RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label],
                        self.env_truns[N - label - 1], self.wave[0], wv)
+            self.guess_kind = "transformed"
         else:
             wv = self._random_wave(sup)
+            self.guess_kind = "random"
         self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
         etrun = self._trun(wv, ENV, env_bs, denv_bs, force_truncate=True)
         self._enlarge(env, env_bs, denv_bs, etrun, geo, "env", sys.len + 1)
@@ -338,6 +347,7 @@ class GPUDMRG:
             with self._phase("transform"):
                 wave_trans(self.dev, "RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label], etrun,
                            self.wave[0], wv)
+            self.guess_kind = "transformed"
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
             etrun = self._trun(wv, ENV, env_bs, denv_bs, force_truncate=True)
             self._enlarge(env, env_bs, denv_bs, etrun, geo, "env", sys.len + 1)
@@ -352,17 +362,25 @@ class GPUDMRG:
         self.left_to_right(1, N - 2)
         self.right_to_left(N - 2, 1)
 
+    def _end_sweep(self):
+        """Lets a guess hook with an ``end_sweep`` method (the learned corrector
+        trains there) see the finished sweep; runs outside the sweep timer."""
+        if self.guess_hook is not None and hasattr(self.guess_hook, "end_sweep"):
+            self.guess_hook.end_sweep(self)
+
     def run(self, sweeps=2):
         """Get_Ground_State with trun_idx = 1 (code/quantum.f90:179-288)."""
         N = self.lat.N
         self.warm_up()
         self.left_to_right(N // 2 - 1, N - 2)
         self.right_to_left(N - 2, 1)
+        self._end_sweep()
         times = []
         for _ in range(sweeps):
             self.phase_s.clear()
             t0 = time.perf_counter()
             self.sweep()
             times.append(time.perf_counter() - t0)
+            self._end_sweep()
         self.sweep_times = times
         return self.energies[-1][2]

@@ -42,6 +42,7 @@ typedef struct hh_block hh_block_t;
 typedef struct hh_basis hh_basis_t;
 typedef struct hh_wave hh_wave_t;
 typedef struct hh_plan hh_plan_t;
+typedef struct hh_mlp hh_mlp_t;
 
 /* ---------------------------------------------------------------- context */
 int hh_init(int device, hh_ctx_t** ctx);
@@ -227,6 +228,36 @@ int hh_ham_add_product(hh_ctx_t* ctx, hh_block_t* ham, const hh_block_t* o1, con
                        const double* coef);
 /* block_transfer (code/space_info.f90:100-129): device copy of a block     */
 int hh_block_copy(hh_ctx_t* ctx, const hh_block_t* src, hh_block_t** out);
+
+/* --------------------------------------- learned initial-guess corrector
+ * No counterpart in the reference: a per-sector MLP that corrects the
+ * wave_trans_LR/RL guess (code/warm_up.f90:1855-2170) before
+ * lanczos_memo_new (code/lanczos.f90:4).  Network: nfeat inputs -> 64 -> 64
+ * -> 1, tanh hidden layers, FP32, trained full batch with Adam on the
+ * weighted mean squared error sum_s w_s (y_s - t_s)^2 / sum_s w_s.
+ * Parameters (hh_mlp_nparams floats): W1[64][nfeat] row-major, b1[64],
+ * W2[64][64] (out, in) row-major, b2[64], W3[64], b3.  x is n x nfeat
+ * row-major; all buffers are host memory; w may be NULL (unit weights).  */
+int hh_mlp_create(hh_ctx_t* ctx, int nfeat, unsigned long long seed, hh_mlp_t** mlp);
+int hh_mlp_free(hh_mlp_t* mlp);
+int hh_mlp_nparams(const hh_mlp_t* mlp, int* n);
+int hh_mlp_get_params(const hh_mlp_t* mlp, float* params);
+/* also resets the Adam state                                              */
+int hh_mlp_set_params(hh_mlp_t* mlp, const float* params);
+int hh_mlp_forward(hh_mlp_t* mlp, const float* x, int n, float* y);
+/* loss and its gradient with respect to the parameters (grad may be NULL) */
+int hh_mlp_loss_grad(hh_mlp_t* mlp, const float* x, const float* t, const float* w, int n, float* loss,
+                     float* grad);
+/* epochs full-batch Adam steps (beta 0.9/0.999, eps 1e-8, learning rate lr),
+ * one epoch captured as a CUDA graph; *final_loss (may be NULL) is the loss
+ * at the trained parameters.                                              */
+int hh_mlp_train(hh_mlp_t* mlp, const float* x, const float* t, const float* w, int n, int epochs, float lr,
+                 float* final_loss);
+/* Squared norm of every sector of a wave (host array, one per sector, in the
+ * wave's sector order).                                                   */
+int hh_wave_sector_norms(const hh_wave_t* w, double* norms2);
+/* Multiplies sector k of a wave by scale[k] (host array).                 */
+int hh_wave_scale_sectors(hh_wave_t* w, const double* scale);
 
 /* Diagnostic: C = A B for dense complex column-major A (M x K), B (K x N)
  * through the split-precision tensor-core tile kernel (host buffers).     */

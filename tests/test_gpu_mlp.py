@@ -1,0 +1,119 @@
+"""The learned corrector's network on the GPU (the library's own forward,
+backward and Adam kernels) against the CPU oracle, the per-sector wave
+kernels, and an A/B run of the GPU DMRG with and without the corrector."""
+import numpy as np
+import pytest
+
+from oracle import mlp as omlp
+from hofstadter_hubbard_tsc_gb300 import _lib
+from hofstadter_hubbard_tsc_gb300.device import DWave
+from hofstadter_hubbard_tsc_gb300.guess import SectorMLP, LearnedGuess, NFEAT, sector_norms, scale_sectors
+from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
+from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(n, seed=5):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-1, 1, size=(n, NFEAT)).astype(np.float32)
+    T = (0.3 * np.sin(3 * X[:, 0]) + 0.2 * X[:, 1] * X[:, 3] - 0.1).astype(np.float32)
+    W = rng.uniform(0.1, 1.0, size=n).astype(np.float32)
+    return X, T, W
+
+
+@pytest.mark.parametrize("n", [1, 37, 700, 5000])
+def test_forward_and_gradient_match_oracle(device, n):
+    net = SectorMLP(device, seed=11)
+    rng = np.random.default_rng(n)
+    p = (rng.normal(scale=0.2, size=net.nparams)).astype(np.float32)
+    net.set_params(p)
+    np.testing.assert_array_equal(net.get_params(), p)
+    X, T, W = _data(n)
+    y = net.forward(X)
+    yo, _ = omlp.forward(p.astype(np.float64), X.astype(np.float64))
+    np.testing.assert_allclose(y, yo, rtol=2e-5, atol=2e-5)
+    loss, g = net.loss_grad(X, T, W)
+    lo, go = omlp.loss_grad(p.astype(np.float64), X.astype(np.float64), T.astype(np.float64),
+                            W.astype(np.float64))
+    assert loss == pytest.approx(lo, rel=1e-4, abs=1e-7)
+    np.testing.assert_allclose(g, go, rtol=0, atol=2e-5 * max(1.0, np.abs(go).max()))
+    net.free()
+
+
+def test_adam_steps_match_oracle(device):
+    net = SectorMLP(device, seed=12)
+    p0 = net.get_params().astype(np.float64)
+    X, T, W = _data(300, seed=9)
+    lr, steps = 1e-3, 5
+    net.train(X, T, W, epochs=steps, lr=lr)
+    p = p0.copy()
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for t in range(1, steps + 1):
+        _, g = omlp.loss_grad(p, X.astype(np.float64), T.astype(np.float64), W.astype(np.float64))
+        p, m, v = omlp.adam_step(p, g, m, v, t, lr)
+    np.testing.assert_allclose(net.get_params(), p, rtol=0, atol=5e-5)
+    net.free()
+
+
+def test_training_fits(device):
+    net = SectorMLP(device, seed=13)
+    X, T, W = _data(2000, seed=10)
+    l0, _ = net.loss_grad(X, T, W)
+    l1 = net.train(X, T, W, epochs=600, lr=3e-3)
+    assert l1 < 0.05 * l0, (l0, l1)
+    # the same run again gives the same parameters (ordered reductions)
+    a = net.get_params()
+    net2 = SectorMLP(device, seed=13)
+    net2.train(X, T, W, epochs=600, lr=3e-3)
+    np.testing.assert_array_equal(net2.get_params(), a)
+    net.free()
+    net2.free()
+
+
+def test_sector_norms_and_scale(device):
+    layout = np.array([[2, 1, 4, 1, 3, 5], [4, 0, 2, 0, 7, 2], [0, 1, 6, 1, 1, 1], [6, 1, 0, 1, 40, 33]],
+                      dtype=np.int32)
+    w = DWave(device, layout, 3, 3)
+    rng = np.random.default_rng(2)
+    z = rng.normal(size=w.nelem) + 1j * rng.normal(size=w.nelem)
+    w.upload(z)
+    ends = np.cumsum([r[4] * r[5] for r in layout])
+    parts = np.split(z, ends[:-1])
+    np.testing.assert_allclose(sector_norms(device, w), [np.vdot(q, q).real for q in parts], rtol=1e-13)
+    s = np.array([0.5, 2.0, 1.0, 1e-3])
+    scale_sectors(device, w, s)
+    np.testing.assert_allclose(w.download(), np.concatenate([a * q for a, q in zip(s, parts)]), rtol=1e-15)
+
+
+def _run(device, apply, sweeps=3):
+    lat = SquareLattice(2, 8, U=8.0, phi=0.25)
+    hook = LearnedGuess(device, lat.N, 14, apply=apply, seed=3)
+    d = GPUDMRG(device, lat, 14, kept_min=64, kept_max=64, trun_err=1e-12, lanzero=1e-10,
+                precision=_lib.HH_PREC_BF16X3, seed=11, guess_hook=hook)
+    e = d.run(sweeps=sweeps)
+    nstep = 2 * (lat.N - 3)
+    its = [r[3] for r in d.energies[-nstep:]]
+    return e, its, hook, d
+
+
+def test_learned_guess_ab(device):
+    """Plain transformed guess (A) against the learned correction (B), the same
+    trajectory until the network is first applied.  Reports the iterations of
+    the last sweep of both; the converged energy judges the correction (equal
+    to 1e-8 relative: the runs part ways once corrections start), and the
+    corrected run may not need more than 2 % more Lanczos iterations.  The gain is bounded by about 1 % on this ladder: restarting
+    from the exact converged sector weights saves no more."""
+    ea, its_a, ha, _ = _run(device, apply=False)
+    eb, its_b, hb, _ = _run(device, apply=True)
+    used = sum(1 for r in hb.log if r[2])
+    print(f"\nA/B: plain {sum(its_a)} iterations E={ea:.12f}; learned {sum(its_b)} iterations "
+          f"E={eb:.12f}; corrected guesses {used}/{len(hb.log)}; train loss {hb.last_loss:.3e}; "
+          f"held-out Hellinger distance {hb.val[0]:.3e} corrected vs {hb.val[1]:.3e} plain")
+    assert ha.trained and hb.trained
+    # same trajectory, data and network up to the first training
+    assert ha.val_history[0] == hb.val_history[0]
+    assert (len(hb.log) > 0) == any(v[0] < 0.8 * v[1] for v in hb.val_history[:-1])
+    assert abs(ea - eb) <= 1e-8 * abs(ea)
+    assert sum(its_b) <= 1.02 * sum(its_a)
