@@ -176,7 +176,7 @@ struct hh_tc_plan {
   int n_op_tasks = 0, n_x_tasks = 0;
   hh::tc::Tile* d_tiles1 = nullptr;
   hh::tc::Tile* d_tiles2 = nullptr;
-  int n_tiles1 = 0, n_tiles2 = 0;
+  int n_tiles1 = 0, n_tiles2 = 0, n_cseg = 0;
   hh::tc::Seg* d_segs = nullptr;
   hh_seg* d_csegs = nullptr;
   int* d_err = nullptr;

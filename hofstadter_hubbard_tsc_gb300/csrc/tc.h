@@ -33,7 +33,7 @@ struct Seg {
 
 struct Tile {
   int seg0, nseg;        // GEMM segments
-  int cseg0, ncseg;      // FP64 copy segments (epilogue)
+  int cseg0, ncseg;      // FP64 copy segments (copy_terms_kernel)
   int mode;              // 0: FP64 output rectangle, 1: T image
   int ntile;             // MMA N (multiple of 16, <= 128)
   int mrem, nrem;        // valid rows / columns of the tile
@@ -47,7 +47,12 @@ size_t tile_smem_bytes();
 
 }  // namespace tc
 
-cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, cudaStream_t s);
+// fp32: scale and split in FP32 (wave images) instead of FP64 (operator images)
+cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
+                            cudaStream_t s);
+// adds the FP64 copy terms of the stage-2 tiles to their output rectangles
+cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
+                          double2* base_out, cudaStream_t s);
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, const hh_seg* d_csegs,
                          const double2* base_in, double2* base_out, int* d_err, cudaStream_t s);
 

@@ -154,6 +154,10 @@ __device__ __forceinline__ size_t img_off(int r8, int r, int k) {
 // ------------------------------------------------------------------ image build
 // One CTA per task: value(r,k) = coef * (conj?) src[trans ? k + r*ld : r + k*ld]
 // for r < rows, k < kc, zero in the padding; written as six BF16 planes.
+// The value is rounded to FP32 first and scaled and split in FP32: three BF16
+// parts hold FP32's 24 significand bits, and GB300 retires FP32 at 64 times
+// its FP64 rate.  Operator images (built once per plan) keep the FP64 split.
+template <bool kFp32>
 __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __restrict__ tasks,
                                                            const double2* __restrict__ base_in) {
   const ImgTask t = tasks[blockIdx.x];
@@ -162,23 +166,37 @@ __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __rest
   const int r8 = t.r8, k16 = t.k16;
   const size_t plane = (size_t)(r8 >> 3) * 256;
   const int ngroups = r8 * (k16 >> 3);
+  const float fre = (float)t.cre, fim = (float)t.cim;
   for (int idx = threadIdx.x; idx < ngroups; idx += blockDim.x) {
     const int r = idx % r8, k0 = (idx / r8) * 8;
     __nv_bfloat16 re[3][8], im[3][8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int k = k0 + j;
-      double2 v = make_double2(0.0, 0.0);
-      if (r < t.rows && k < t.kc) {
-        v = t.trans ? src[(long long)k + (long long)r * t.ld] : src[(long long)r + (long long)k * t.ld];
-        if (t.conj) v.y = -v.y;
-        v = make_double2(t.cre * v.x - t.cim * v.y, t.cre * v.y + t.cim * v.x);
-      }
       __nv_bfloat16 s[3];
-      split3d(v.x, s);
-      re[0][j] = s[0]; re[1][j] = s[1]; re[2][j] = s[2];
-      split3d(v.y, s);
-      im[0][j] = s[0]; im[1][j] = s[1]; im[2][j] = s[2];
+      if (kFp32) {
+        float2 v = make_float2(0.f, 0.f);
+        if (r < t.rows && k < t.kc) {
+          const double2 d = t.trans ? src[(long long)k + (long long)r * t.ld] : src[(long long)r + (long long)k * t.ld];
+          v = make_float2((float)d.x, t.conj ? -(float)d.y : (float)d.y);
+          v = make_float2(fre * v.x - fim * v.y, fre * v.y + fim * v.x);
+        }
+        split3f(v.x, s);
+        re[0][j] = s[0]; re[1][j] = s[1]; re[2][j] = s[2];
+        split3f(v.y, s);
+        im[0][j] = s[0]; im[1][j] = s[1]; im[2][j] = s[2];
+      } else {
+        double2 v = make_double2(0.0, 0.0);
+        if (r < t.rows && k < t.kc) {
+          v = t.trans ? src[(long long)k + (long long)r * t.ld] : src[(long long)r + (long long)k * t.ld];
+          if (t.conj) v.y = -v.y;
+          v = make_double2(t.cre * v.x - t.cim * v.y, t.cre * v.y + t.cim * v.x);
+        }
+        split3d(v.x, s);
+        re[0][j] = s[0]; re[1][j] = s[1]; re[2][j] = s[2];
+        split3d(v.y, s);
+        im[0][j] = s[0]; im[1][j] = s[1]; im[2][j] = s[2];
+      }
     }
     const size_t o = img_off(r8, r, k0);
 #pragma unroll
@@ -330,21 +348,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
         for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
       }
       if (t.mode == 0) {
+        // main + correction in FP32 (one rounding at 2^-24), one conversion;
+        // the FP64 copy terms follow in copy_terms_kernel
         if (row < t.mrem) {
           double2* O = base_out + t.out;
-#pragma unroll 4
+#pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int col = c0 + j;
-            if (col < t.nrem) {
-              double2 v = make_double2((double)re[j] + (double)cr[j], (double)im[j] + (double)cm[j]);
-              for (int ci = 0; ci < t.ncseg; ++ci) {
-                const hh_seg cs = csegs[t.cseg0 + ci];
-                const double2 x = base_in[cs.poff + (long long)(t.m0 + row) + (long long)(t.n0 + col) * cs.ldp];
-                v.x += cs.cre * x.x - cs.cim * x.y;
-                v.y += cs.cre * x.y + cs.cim * x.x;
-              }
-              O[(long long)row + (long long)col * t.ldo] = v;
-            }
+            if (col < t.nrem) O[(long long)row + (long long)col * t.ldo] = make_double2(re[j] + cr[j], im[j] + cm[j]);
           }
         }
       } else {
@@ -385,15 +396,50 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
   }
 }
 
+// out[rect] += sum_c coef_c * in[region_c] for the FP64 copy terms of each
+// stage-2 tile (site-diagonal terms), element by element after the tiles:
+// coalesced along the column-major rows, bandwidth bound.
+__global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict__ tiles,
+                                                         const hh_seg* __restrict__ csegs,
+                                                         const double2* __restrict__ base_in,
+                                                         double2* __restrict__ base_out) {
+  const Tile t = tiles[blockIdx.x];
+  if (t.mode != 0 || t.ncseg == 0) return;
+  double2* O = base_out + t.out;
+  const int n = t.mrem * t.nrem;
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const int row = idx % t.mrem, col = idx / t.mrem;
+    double2 v = O[(long long)row + (long long)col * t.ldo];
+    for (int ci = 0; ci < t.ncseg; ++ci) {
+      const hh_seg cs = csegs[t.cseg0 + ci];
+      const double2 x = base_in[cs.poff + (long long)(t.m0 + row) + (long long)(t.n0 + col) * cs.ldp];
+      v.x += cs.cre * x.x - cs.cim * x.y;
+      v.y += cs.cre * x.y + cs.cim * x.x;
+    }
+    O[(long long)row + (long long)col * t.ldo] = v;
+  }
+}
+
 constexpr int kStages = 3;
 
 size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8 * (2 * kStages + 2) + 64; }
 
 }  // namespace tc
 
-cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, cudaStream_t s) {
+cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
+                            cudaStream_t s) {
   if (ntask <= 0) return cudaSuccess;
-  tc::build_images_kernel<<<ntask, 256, 0, s>>>(d_tasks, base_in);
+  if (fp32)
+    tc::build_images_kernel<true><<<ntask, 256, 0, s>>>(d_tasks, base_in);
+  else
+    tc::build_images_kernel<false><<<ntask, 256, 0, s>>>(d_tasks, base_in);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
+                          double2* base_out, cudaStream_t s) {
+  if (ntile <= 0) return cudaSuccess;
+  tc::copy_terms_kernel<<<ntile, 256, 0, s>>>(d_tiles, d_csegs, base_in, base_out);
   return cudaGetLastError();
 }
 

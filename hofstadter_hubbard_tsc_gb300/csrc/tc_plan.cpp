@@ -230,7 +230,16 @@ int build_tc_plan(hh_plan* p) {
             cs.kind = HH_SEG_COPY;
             cs.cre = c.cre;
             cs.cim = c.cim;
-            csegs.push_back(cs);
+            // terms copying the same input region (the site-diagonal terms of
+            // one sector) add up into one coefficient
+            bool merged = false;
+            for (size_t q = tl.cseg0; q < csegs.size() && !merged; ++q)
+              if (csegs[q].poff == cs.poff && csegs[q].ldp == cs.ldp) {
+                csegs[q].cre += cs.cre;
+                csegs[q].cim += cs.cim;
+                merged = true;
+              }
+            if (!merged) csegs.push_back(cs);
           }
         }
         tl.nseg = (int)segs.size() - tl.seg0;
@@ -296,13 +305,14 @@ int build_tc_plan(hh_plan* p) {
   t.n_x_tasks = (int)x_tasks.size();
   t.n_tiles1 = (int)tiles1.size();
   t.n_tiles2 = (int)tiles2.size();
+  t.n_cseg = (int)csegs.size();
   t.bytes_op = (double)a_op.size;
   t.bytes_x = (double)a_x.size;
   t.bytes_t = (double)a_t.size;
   t.mma_flops1 = mma1;
   t.mma_flops2 = mma2;
   // operator images are built once here
-  cudaError_t e = tc_build_images(t.d_op_tasks, t.n_op_tasks, nullptr, ctx->stream);
+  cudaError_t e = tc_build_images(t.d_op_tasks, t.n_op_tasks, nullptr, false, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     release_tc_plan(p);
@@ -323,12 +333,13 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms) {
   if (ms)
     for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
   if (ms) cudaEventRecord(ev[0], ctx->stream);
-  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, ctx->stream);
+  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, ctx->stream);
   if (ms) cudaEventRecord(ev[1], ctx->stream);
   if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, t.d_csegs, in, out, t.d_err, ctx->stream);
   if (ms) cudaEventRecord(ev[2], ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
   if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, t.d_csegs, in, out, t.d_err, ctx->stream);
+  if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, ctx->stream);
   if (ms) cudaEventRecord(ev[3], ctx->stream);
   int herr = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, t.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
@@ -423,7 +434,7 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
   if (e == cudaSuccess) e = cudaMemcpyAsync(dtask, tk, sizeof(tk), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dtile, tiles.data(), tiles.size() * sizeof(tc::Tile), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dseg, segs.data(), segs.size() * sizeof(tc::Seg), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = tc_build_images((tc::ImgTask*)dtask, 2, nullptr, s);
+  if (e == cudaSuccess) e = tc_build_images((tc::ImgTask*)dtask, 2, nullptr, false, s);
   if (e == cudaSuccess)
     e = tc_run_tiles((tc::Tile*)dtile, (int)tiles.size(), (tc::Seg*)dseg, nullptr, nullptr, (double2*)dC, (int*)derr, s);
   int herr = 0;
