@@ -290,7 +290,7 @@ def main():
 
     def step():
         dev.check(dev.lib.hh_matvec_timed(sb.plan, w_in.h, w_out.h, prec, ms))
-        return ms[0], ms[1], ms[2]
+        return ms[0], ms[1], ms[2], ms[3]
 
     for _ in range(args.warmup):
         step()
@@ -298,16 +298,17 @@ def main():
         dist.barrier()
     clocks = Clocks(local)
     clocks.start()
-    tot = s1 = s2 = 0.0
+    tot = s1 = s2 = s0 = 0.0
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("timed")
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
-        a, b, c = step()
+        a, b, c, d = step()
         tot += a
         s1 += b
         s2 += c
+        s0 += d
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
@@ -380,7 +381,9 @@ def main():
                                              "exec_gflop_per_matvec": counts[1] / 1e9,
                                              "plan_setup_s": setup_s}),
             "roofline": roofline, "e2e": e2e, "clocks": clk,
-            "gpu_launches": args.steps * (2 if prec == _lib.HH_PREC_FP64 else 3)}
+            "stage_ms": {"wave_images": s0 / args.steps, "stage1": s1 / args.steps,
+                         "stage2_and_copy_terms": s2 / args.steps},
+            "gpu_launches": args.steps * (2 if prec == _lib.HH_PREC_FP64 else 4)}
     if prec != _lib.HH_PREC_FP64:
         w_in.upload(psi)
         dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, _lib.HH_PREC_FP64))
@@ -400,7 +403,7 @@ def main():
             t0 = time.perf_counter()
             dev.check(dev.lib.hh_lanczos(sb.plan, w_in.h, 1e-12, 100, pp, C.byref(e), C.byref(it)))
             res[name] = (e.value, it.value, time.perf_counter() - t0)
-        line["energy_check"] = {"E_fp64": res["fp64"][0], "E_split_fp64_rayleigh": res["split"][0],
+        line["energy_check"] = {"E_fp64": res["fp64"][0], "E_split": res["split"][0],
                                 "rel_dE": abs(res["split"][0] - res["fp64"][0]) / abs(res["fp64"][0]),
                                 "iterations": [res["fp64"][1], res["split"][1]],
                                 "lanczos_s": [res["fp64"][2], res["split"][2]]}

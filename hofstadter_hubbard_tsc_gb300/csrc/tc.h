@@ -41,6 +41,8 @@ struct Tile {
   int ldo;
   int t_r8;              // mode 1: padded rows of the T image
   int m0, n0;            // tile origin inside its rectangle
+  int nchunk;            // sum of the segments' nkc (MMA chunks of the tile)
+  int pad;
 };
 
 size_t tile_smem_bytes();
@@ -53,7 +55,9 @@ cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2
 // adds the FP64 copy terms of the stage-2 tiles to their output rectangles
 cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
                           double2* base_out, cudaStream_t s);
-cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, const hh_seg* d_csegs,
-                         const double2* base_in, double2* base_out, int* d_err, cudaStream_t s);
+// tile GEMM over ntile tiles: persistent (one CTA per SM, CTA b takes tiles
+// b, b + G, ...: the list must be ordered for balance) or one CTA per tile
+cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
+                         bool persistent, cudaStream_t s);
 
 }  // namespace hh

@@ -216,12 +216,16 @@ __device__ __forceinline__ void flag_error(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
 }
 
+// One CTA per tile (grid = number of tiles; the hardware hands tiles to SMs
+// as they free up).  Same roles, layout and epilogue as the persistent kernel
+// below, without its tile loop: used for stage 2, whose few hundred long,
+// uneven tiles run faster this way than under the persistent kernel (0.50
+// against 0.54-0.62 ms on the m = 2000 workload, measured).  Every wait is
+// bounded and reports through *err.
 template <int STAGES>
-__global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __restrict__ tiles,
-                                                             const Seg* __restrict__ segs,
-                                                             const hh_seg* __restrict__ csegs,
-                                                             const double2* __restrict__ base_in,
-                                                             double2* __restrict__ base_out, int* err) {
+__global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* __restrict__ tiles,
+                                                                  const Seg* __restrict__ segs,
+                                                                  double2* __restrict__ base_out, int* err) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const Tile t = tiles[blockIdx.x];
   const int stage_bytes = kStageA + 6 * 128 * 32;
@@ -396,6 +400,253 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
   }
 }
 
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent: CTA b of G handles tiles b, b + G, b + 2G, ... (the plan orders
+// them so that the CTAs' shares balance); TMEM (512 columns) and the barriers
+// are set up once per CTA.  Used for stage 1, thousands of short tiles whose
+// set-up cost it amortises.  The producer runs up to STAGES chunks ahead
+// across tile boundaries, so the next tile's operands stream in while the
+// epilogue drains the accumulators.  Barriers: full/empty per stage
+// (producer <-> MMA), accf (MMA -> epilogue) and tfree (epilogue -> MMA, four
+// warp arrivals), one phase each per tile that has MMAs; tiles without MMAs
+// (copy terms only) never touch TMEM and skip both, so neither side runs more
+// than one phase ahead of the other.  Every wait is bounded; a wait that runs
+// out sets *err and an abort flag in shared memory that every role checks
+// between chunks, so the CTA winds down without another full-length wait per
+// remaining tile.  On the way out the producer waits (bounded) for the copies
+// it issued and the MMA warp for its MMAs (mdone) before TMEM is freed.
+template <int STAGES>
+__global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __restrict__ tiles, int ntile,
+                                                             const Seg* __restrict__ segs,
+                                                             double2* __restrict__ base_out, int* err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int stage_bytes = kStageA + 6 * 128 * 32;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accf = empty + STAGES;
+  uint64_t* tfree = accf + 1;
+  uint64_t* mdone = tfree + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mdone + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accf, 1);
+    mbar_init(tfree, 4);
+    mbar_init(mdone, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  auto give_up = [&](int code) {
+    flag_error(err, code);
+    *abort_flag = 1;
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      for (int ti = blockIdx.x; ti < ntile && !*abort_flag; ti += gridDim.x) {
+        const Tile t = tiles[ti];
+        Seg nxt;
+        if (t.nseg > 0) nxt = segs[t.seg0];
+        for (int si = 0; si < t.nseg && !*abort_flag; ++si) {
+          const Seg sg = nxt;
+          if (si + 1 < t.nseg) nxt = segs[t.seg0 + si + 1];  // in flight while this one's copies go out
+          for (int kc = 0; kc < sg.nkc; ++kc, ++it) {
+            const int s = it % STAGES;
+            if (*abort_flag) break;
+            if (it >= STAGES && !mbar_wait(&empty[s], ((it / STAGES) + 1) & 1)) {
+              give_up(1);
+              break;
+            }
+            uint8_t* sa = smem + s * stage_bytes;
+            uint8_t* sb = sa + kStageA;
+            mbar_expect_tx(&full[s], 6u * (sg.a_bytes + sg.b_bytes));
+            const uint8_t* ga = reinterpret_cast<const uint8_t*>(sg.a) + (size_t)kc * 6 * sg.a_plane;
+            const uint8_t* gb = reinterpret_cast<const uint8_t*>(sg.b) + (size_t)kc * 6 * sg.b_plane;
+#pragma unroll
+            for (int p = 0; p < 6; ++p) {
+              bulk_g2s(sa + p * kPlaneA, ga + (size_t)p * sg.a_plane, sg.a_bytes, &full[s]);
+              bulk_g2s(sb + p * (t.ntile * 32), gb + (size_t)p * sg.b_plane, sg.b_bytes, &full[s]);
+            }
+          }
+        }
+      }
+      // copies still in flight land before the CTA leaves (already done
+      // unless a wait gave up)
+      for (int j = it > STAGES ? it - STAGES : 0; j < it; ++j)
+        if (!mbar_wait(&full[j % STAGES], (j / STAGES) & 1)) flag_error(err, 5);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t d_re = tmem, d_im = tmem + 128, c_re = tmem + 256, c_im = tmem + 384;
+      int it = 0, n = 0;  // n: tiles with MMAs so far
+      bool issued = false;
+      for (int ti = blockIdx.x; ti < ntile && !*abort_flag; ti += gridDim.x) {
+        const Tile t = tiles[ti];
+        if (t.nchunk == 0) continue;
+        const uint32_t id_pos = idesc_bf16(t.ntile, false), id_neg = idesc_bf16(t.ntile, true);
+        // the epilogue has read the previous tile's accumulators
+        if (n > 0 && !mbar_wait(tfree, (n - 1) & 1)) {
+          give_up(4);
+          break;
+        }
+        ++n;
+        fence_after();
+        uint32_t acc = 0, acc_c = 0;
+        int chunks = 0;
+        int nkc_next = t.nseg > 0 ? segs[t.seg0].nkc : 0;
+        for (int si = 0; si < t.nseg && !*abort_flag; ++si) {
+          const int nkc = nkc_next;
+          if (si + 1 < t.nseg) nkc_next = segs[t.seg0 + si + 1].nkc;
+          for (int kc = 0; kc < nkc; ++kc, ++it, ++chunks) {
+            const int s = it % STAGES;
+            if (*abort_flag) break;
+            if (!mbar_wait(&full[s], (it / STAGES) & 1)) {
+              give_up(2);
+              break;
+            }
+            fence_after();
+            const uint32_t sa = smem_u32(smem + s * stage_bytes);
+            const uint32_t sb = sa + kStageA;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+#pragma unroll
+              for (int j = 0; j < 3 - i; ++j) {
+                const uint64_t are = smem_desc(sa + i * kPlaneA), aim = smem_desc(sa + (3 + i) * kPlaneA);
+                const uint64_t bre = smem_desc(sb + j * t.ntile * 32), bim = smem_desc(sb + (3 + j) * t.ntile * 32);
+                if (i + j == 0) {
+                  mma_bf16(d_re, are, bre, id_pos, acc);
+                  mma_bf16(d_re, aim, bim, id_neg, 1u);
+                  mma_bf16(d_im, are, bim, id_pos, acc);
+                  mma_bf16(d_im, aim, bre, id_pos, 1u);
+                  acc = 1u;
+                } else {
+                  mma_bf16(c_re, are, bre, id_pos, acc_c);
+                  mma_bf16(c_re, aim, bim, id_neg, 1u);
+                  mma_bf16(c_im, are, bim, id_pos, acc_c);
+                  mma_bf16(c_im, aim, bre, id_pos, 1u);
+                  acc_c = 1u;
+                }
+              }
+            }
+            mma_commit(&empty[s]);
+            issued = true;
+          }
+        }
+        if (chunks > 0) mma_commit(accf);
+      }
+      // every MMA issued here has completed before TMEM is freed
+      if (issued) {
+        mma_commit(mdone);
+        if (!mbar_wait(mdone, 0)) flag_error(err, 6);
+      }
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one output row per thread
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+    int nacc = 0;
+    for (int ti = blockIdx.x; ti < ntile; ti += gridDim.x) {
+      if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
+      const Tile t = tiles[ti];
+      const bool mmas = t.nchunk > 0;
+      bool have = mmas;
+      if (have) {
+        if (!mbar_wait(accf, nacc & 1)) {
+          give_up(3);
+          have = false;
+        }
+        ++nacc;
+        fence_after();
+      }
+      have = __all_sync(0xffffffffu, have);  // tcgen05.ld below is warp-collective
+      for (int c0 = 0; c0 < t.ntile; c0 += 16) {
+        float re[16], im[16], cr[16], cm[16];
+        if (have) {
+          tmem_ld16(lane_base + c0, re);
+          tmem_ld16(lane_base + 128 + c0, im);
+          tmem_ld16(lane_base + 256 + c0, cr);
+          tmem_ld16(lane_base + 384 + c0, cm);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
+        }
+        if (t.mode == 0) {
+          // main + correction in FP32 (one rounding at 2^-24), one conversion;
+          // the FP64 copy terms follow in copy_terms_kernel
+          if (row < t.mrem) {
+            double2* O = base_out + t.out;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int col = c0 + j;
+              if (col < t.nrem)
+                O[(long long)row + (long long)col * t.ldo] = make_double2(re[j] + cr[j], im[j] + cm[j]);
+            }
+          }
+        } else {
+          // T image: rows of T, k = T columns; zero outside the valid rectangle
+          const int r = t.m0 + row;
+          if (r < t.t_r8) {
+            uint8_t* img = reinterpret_cast<uint8_t*>(t.out);
+            const size_t plane = (size_t)(t.t_r8 >> 3) * 256;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              __nv_bfloat16 pr[3][8], pi[3][8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int cc = c0 + h * 8 + j;
+                const bool valid = row < t.mrem && cc < t.nrem;
+                __nv_bfloat16 s3[3];
+                split3f(valid ? re[h * 8 + j] + cr[h * 8 + j] : 0.f, s3);
+                pr[0][j] = s3[0]; pr[1][j] = s3[1]; pr[2][j] = s3[2];
+                split3f(valid ? im[h * 8 + j] + cm[h * 8 + j] : 0.f, s3);
+                pi[0][j] = s3[0]; pi[1][j] = s3[1]; pi[2][j] = s3[2];
+              }
+              const size_t o = img_off(t.t_r8, r, t.n0 + c0 + h * 8);
+#pragma unroll
+              for (int p = 0; p < 3; ++p) {
+                *reinterpret_cast<uint4*>(img + o + (size_t)p * plane) = pack8(pr[p]);
+                *reinterpret_cast<uint4*>(img + o + (size_t)(p + 3) * plane) = pack8(pi[p]);
+              }
+            }
+          }
+        }
+      }
+      // accumulators read: release them to the MMA warp
+      if (mmas) {
+        fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(tfree);
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
 // out[rect] += sum_c coef_c * in[region_c] for the FP64 copy terms of each
 // stage-2 tile (site-diagonal terms), element by element after the tiles:
 // coalesced along the column-major rows, bandwidth bound.
@@ -420,9 +671,9 @@ __global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict_
   }
 }
 
-constexpr int kStages = 3;
+constexpr int kStages = 4;
 
-size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8 * (2 * kStages + 2) + 64; }
+size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8 * (2 * kStages + 3) + 64; }
 
 }  // namespace tc
 
@@ -443,19 +694,28 @@ cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_cs
   return cudaGetLastError();
 }
 
-cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, const hh_seg* d_csegs,
-                         const double2* base_in, double2* base_out, int* d_err, cudaStream_t s) {
+cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
+                         bool persistent, cudaStream_t s) {
   if (ntile <= 0) return cudaSuccess;
   const size_t smem = tc::tile_smem_bytes();
-  static bool attr_set = false;
-  if (!attr_set) {
+  static int sms = 0;
+  if (!sms) {
     cudaError_t e = cudaFuncSetAttribute(tc::tc_tile_kernel<tc::kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(tc::tc_tile_once_kernel<tc::kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    attr_set = true;
   }
-  tc::tc_tile_kernel<tc::kStages><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, d_csegs, base_in, base_out,
-                                                                    d_err);
+  if (persistent && ntile > sms) {
+    // one CTA per SM: shared memory and the 512 TMEM columns allow no second
+    tc::tc_tile_kernel<tc::kStages><<<sms, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err);
+  } else {
+    tc::tc_tile_once_kernel<tc::kStages><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err);
+  }
   return cudaGetLastError();
 }
 

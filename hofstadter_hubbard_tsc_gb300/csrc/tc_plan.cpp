@@ -256,6 +256,38 @@ int build_tc_plan(hh_plan* p) {
       }
   }
 
+  for (auto* tl : {&tiles1, &tiles2})
+    for (auto& x : *tl) {
+      x.nchunk = 0;
+      for (int si = 0; si < x.nseg; ++si) x.nchunk += segs[x.seg0 + si].nkc;
+    }
+
+  // ------------------------------------------------------- tile order
+  // Stage 1 (thousands of short tiles) runs on the persistent kernel, where
+  // CTA c of G takes tiles c, c + G, c + 2G, ...  Its tiles go longest first
+  // (MMA chunks x N, plus a fixed epilogue share), in a snake over the CTAs,
+  // so that every CTA receives a near-equal share.  Stage 2 (hundreds of long,
+  // uneven tiles) runs one CTA per tile in plan order, which keeps the tiles
+  // of one output sector together for L2 reuse and lets the hardware balance.
+  {
+    int sms = 148, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t n = tiles1.size();
+    if (n > (size_t)sms) {
+      std::vector<std::pair<double, size_t>> cost(n);
+      for (size_t i = 0; i < n; ++i) cost[i] = {8.0 + tiles1[i].nchunk * (tiles1[i].ntile / 128.0), i};
+      std::stable_sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+      std::vector<tc::Tile> out(n);
+      for (size_t k = 0; k < n; ++k) {
+        const size_t round = k / sms, c = k % sms, base = round * sms;
+        const size_t cnt = std::min((size_t)sms, n - base);  // the last round may be partial
+        out[base + ((round & 1) ? cnt - 1 - c : c)] = tiles1[cost[k].second];
+      }
+      tiles1.swap(out);
+    }
+  }
+
   // --------------------------------------------------------------- device
   hh_tc_plan& t = p->tc;
   auto alloc = [&](void** ptr, size_t bytes) -> int {
@@ -335,10 +367,10 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms) {
   if (ms) cudaEventRecord(ev[0], ctx->stream);
   cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, ctx->stream);
   if (ms) cudaEventRecord(ev[1], ctx->stream);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, t.d_csegs, in, out, t.d_err, ctx->stream);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, out, t.d_err, true, ctx->stream);
   if (ms) cudaEventRecord(ev[2], ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, t.d_csegs, in, out, t.d_err, ctx->stream);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, out, t.d_err, false, ctx->stream);
   if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, ctx->stream);
   if (ms) cudaEventRecord(ev[3], ctx->stream);
   int herr = 0;
@@ -417,6 +449,7 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
       tc::Tile tl{};
       tl.seg0 = (int)segs.size();
       tl.nseg = 1;
+      tl.nchunk = sg.nkc;
       segs.push_back(sg);
       tl.mode = 0;
       tl.ntile = ntile;
@@ -436,7 +469,7 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
   if (e == cudaSuccess) e = cudaMemcpyAsync(dseg, segs.data(), segs.size() * sizeof(tc::Seg), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = tc_build_images((tc::ImgTask*)dtask, 2, nullptr, false, s);
   if (e == cudaSuccess)
-    e = tc_run_tiles((tc::Tile*)dtile, (int)tiles.size(), (tc::Seg*)dseg, nullptr, nullptr, (double2*)dC, (int*)derr, s);
+    e = tc_run_tiles((tc::Tile*)dtile, (int)tiles.size(), (tc::Seg*)dseg, (double2*)dC, (int*)derr, true, s);
   int herr = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(C, dC, (size_t)M * N * 16, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s);
