@@ -8,14 +8,18 @@
 // in an L2-resident scratch matrix.  Jacobi costs about 150 n^3 FP64 flops
 // against zheevd's 22 n^3, and a GB300 SM retires about two FP64 FMAs per
 // clock, so it only pays where zheevd's per-call latency (0.4 ms at n = 8,
-// 1.2 ms at n = 32, 3.7 ms at n = 64, measured) dominates: n <= 48.  Larger
-// sectors go to cuSOLVER zheevd, spread over a pool of streams so that their
-// host-side latency overlaps, concurrently with the Jacobi launch.  A
-// canonical phase is applied to every eigenvector afterwards (one launch).
+// 1.2 ms at n = 32, 3.7 ms at n = 64, measured) dominates: n <= 32.  Larger
+// sectors go to cuSOLVER zheevd.  Most of a small zheevd's time is host-side
+// work between its kernels, so the large sectors are shared out over kPool
+// host threads, each with its own solver handle and stream; they run
+// concurrently with the Jacobi launch.  A canonical phase is applied to every
+// eigenvector afterwards (one launch).
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <thread>
 #include <vector>
 
 #include "hh_internal.h"
@@ -23,10 +27,10 @@
 namespace hh {
 namespace {
 
-constexpr int kJacobiMaxN = 48;  // 48^2 complex doubles = 36 KiB of shared memory
+constexpr int kJacobiMaxN = 32;  // 32^2 complex doubles = 16 KiB of shared memory
 constexpr int kJacobiThreads = 256;
 constexpr int kJacobiMaxSweeps = 30;
-constexpr int kPool = 8;  // zheevd streams
+constexpr int kPool = 8;  // zheevd host threads, each with a stream and a solver handle
 
 struct EigItem {
   long long off;   // n x n sector (column-major, ld n) in the density block
@@ -253,7 +257,7 @@ void release_step_resources(hh_ctx* ctx) {
     if (s->join[i]) cudaEventDestroy(s->join[i]);
   }
   if (s->fork) cudaEventDestroy(s->fork);
-  if (s->d_buf) cudaFree(s->d_buf);
+  dev_free(ctx, s->d_buf);
   delete s;
   ctx->eig = nullptr;
 }
@@ -295,11 +299,11 @@ int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>&
   const size_t b_work = align256(std::max<size_t>(16, (size_t)lwork * sizeof(cuDoubleComplex)));
   const size_t need = b_items + b_w + b_v + b_status + kPool * b_work;
   if (S->cap < need) {
-    if (S->d_buf) cudaFree(S->d_buf);
+    dev_free(ctx, S->d_buf);
     S->d_buf = nullptr;
     S->cap = 0;
-    cudaError_t e = cudaMalloc(&S->d_buf, need);
-    if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(eigensolver workspace)");
+    cudaError_t e = dev_alloc(ctx, &S->d_buf, need);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "allocate eigensolver workspace");
     S->cap = need;
   }
   char* base = (char*)S->d_buf;
@@ -313,20 +317,14 @@ int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>&
   if (ns > 0) e = cudaMemcpyAsync(d_items, items.data(), ns * sizeof(EigItem), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, b_status, s);
   if (e != cudaSuccess) return cuda_check(ctx, e, "eigensolver set-up");
-  // large sectors: zheevd on the pool streams, after everything queued so far
+  // large sectors: zheevd on the pool streams (after everything queued so
+  // far), largest first, handed out to the host threads through a counter
+  std::vector<std::thread> workers;
+  std::atomic<int> next{0}, solver_failed{0};
   if (!big.empty()) {
     e = cudaEventRecord(S->fork, s);
     for (int i = 0; i < kPool && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(S->stream[i], S->fork, 0);
     if (e != cudaSuccess) return cuda_check(ctx, e, "eigensolver fork");
-    for (size_t b = 0; b < big.size(); ++b) {
-      const int k = big[b], slot = (int)(b % kPool);
-      const int n = items[k].n;
-      if (cusolverDnZheevd(S->solver[slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
-                           reinterpret_cast<cuDoubleComplex*>(A + items[k].off), n, d_w + items[k].woff,
-                           reinterpret_cast<cuDoubleComplex*>(d_work + slot * b_work), lwork,
-                           d_status + k) != CUSOLVER_STATUS_SUCCESS)
-        return fail(ctx, HH_ERR_NUMERIC, "cusolverDnZheevd failed");
-    }
   }
   // small sectors: one Jacobi launch on the context stream, concurrent with the pool
   if (maxj > 0) {
@@ -341,6 +339,27 @@ int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>&
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_check(ctx, e, "Jacobi eigensolver launch");
   }
+  if (!big.empty()) {
+    std::stable_sort(big.begin(), big.end(), [&](int a, int b) { return items[a].n > items[b].n; });
+    const int nthreads = std::min<int>(kPool, (int)big.size());
+    const int device = ctx->device;
+    auto work = [&, device](int slot) {
+      cudaSetDevice(device);
+      for (int b = next.fetch_add(1); b < (int)big.size(); b = next.fetch_add(1)) {
+        const int k = big[b];
+        const int n = items[k].n;
+        if (cusolverDnZheevd(S->solver[slot], CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, n,
+                             reinterpret_cast<cuDoubleComplex*>(A + items[k].off), n, d_w + items[k].woff,
+                             reinterpret_cast<cuDoubleComplex*>(d_work + slot * b_work), lwork,
+                             d_status + k) != CUSOLVER_STATUS_SUCCESS)
+          solver_failed = 1;
+      }
+    };
+    for (int i = 1; i < nthreads; ++i) workers.emplace_back(work, i);
+    if (nthreads > 0) work(0);  // this thread takes slot 0
+  }
+  for (auto& w : workers) w.join();
+  if (solver_failed) return fail(ctx, HH_ERR_NUMERIC, "cusolverDnZheevd failed");
   if (!big.empty()) {
     for (int i = 0; i < kPool && e == cudaSuccess; ++i) {
       e = cudaEventRecord(S->join[i], S->stream[i]);

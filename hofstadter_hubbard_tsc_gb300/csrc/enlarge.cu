@@ -54,18 +54,20 @@ __global__ void place_kernel(const Place* __restrict__ P) {
 inline double psign(int n) { return ((n / 2) & 1) ? -1.0 : 1.0; }
 long long addr_of(const hh_block* b, int j) { return (long long)(uintptr_t)(b->d + b->subs[j].off); }
 
+// Queued on the context stream: the placement list (copied from pageable
+// host memory, so the vector may go at once) returns to the pool in stream
+// order after the kernel; nothing waits for the device.
 int run_places(hh_ctx* ctx, const std::vector<Place>& P) {
   if (P.empty()) return HH_OK;
   Place* d = nullptr;
-  cudaError_t e = cudaMalloc(&d, P.size() * sizeof(Place));
+  cudaError_t e = dev_alloc(ctx, (void**)&d, P.size() * sizeof(Place));
   if (e == cudaSuccess) e = cudaMemcpyAsync(d, P.data(), P.size() * sizeof(Place), cudaMemcpyHostToDevice, ctx->stream);
   // placements into one destination sub-block never overlap in the
   // reference's loops except for accumulations of the same element, which are
   // serialised by launching in chunks that touch disjoint destinations
   if (e == cudaSuccess) place_kernel<<<(unsigned)P.size(), 256, 0, ctx->stream>>>(d);
   if (e == cudaSuccess) e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  if (d) cudaFree(d);
+  dev_free(ctx, d);
   return cuda_check(ctx, e, "placement");
 }
 
@@ -352,9 +354,8 @@ extern "C" int hh_ham_add_product(hh_ctx_t* ctx, hh_block_t* ham, const hh_block
         L.tiles.push_back(t);
       }
   }
-  L.upload(ctx->stream);
+  L.upload(ctx);
   cudaError_t e = launch_segment_gemm_fp64(L, nullptr, nullptr, ham->d, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   L.release();
   return cuda_check(ctx, e, "ham_add_product");
 }

@@ -1,10 +1,12 @@
 // Grouped segment GEMM in complex FP64 and the wave-vector kernels.
 //
-// One CTA owns one 64x64 output tile and accumulates every segment of its
-// tile (c_s * opP(P_s) * opQ(Q_s), or c_s * P_s for copies) in registers before
-// a single store: the sum over terms that the reference performs with
+// One CTA owns one 64x64 output tile (or one part of a tile split for
+// balance, see hh_gemm_list::upload) and accumulates every segment of it
+// (c_s * opP(P_s) * opQ(Q_s), or c_s * P_s for copies) in registers before a
+// single store: the sum over terms that the reference performs with
 // successive ZGEMM(beta=1) calls on the same output sub-block is done here
-// without atomics and in a fixed order.
+// without atomics and in a fixed order; the parts of a split tile are added
+// in slot order by seg_reduce_kernel.
 #include "hh_internal.h"
 
 namespace hh {
@@ -32,6 +34,7 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
                                                           const double2* __restrict__ bin,
                                                           double2* __restrict__ bscr,
                                                           double2* __restrict__ bout,
+                                                          double2* __restrict__ part,
                                                           long long sin, long long sscr, long long sout) {
   __shared__ double2 Ps[TK][TM + 1];
   __shared__ double2 Qs[TK][TN + 1];
@@ -126,6 +129,15 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
       __syncthreads();
     }
   }
+  if (t.part >= 0) {
+    // partial sum of a split tile: the whole 64x64 slot, column-major
+    double2* S = part + (long long)t.part * (TM * TN);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) S[(ty * 4 + i) + (tx * 4 + j) * TM] = acc[i][j];
+    return;
+  }
   double2* O = (t.obase == HH_BASE_SCR) ? scr : out;
   O += t.ooff;
 #pragma unroll
@@ -145,6 +157,34 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
         }
       }
     }
+}
+
+// out (+)= sum over the parts of a split tile, in slot order
+__global__ void __launch_bounds__(NT) seg_reduce_kernel(const hh_red* __restrict__ reds,
+                                                        const double2* __restrict__ part,
+                                                        double2* __restrict__ bscr, double2* __restrict__ bout) {
+  const hh_red r = reds[blockIdx.x];
+  const int mrem = min(TM, r.M - r.m0), nrem = min(TN, r.N - r.n0);
+  double2* O = ((r.obase == HH_BASE_SCR) ? bscr : bout) + r.ooff;
+  for (int e = threadIdx.x; e < TM * TN; e += NT) {
+    const int m = e % TM, n = e / TM;
+    if (m >= mrem || n >= nrem) continue;
+    double2 v = make_double2(0.0, 0.0);
+    for (int p = 0; p < r.nparts; ++p) {
+      const double2 x = part[(long long)(r.part0 + p) * (TM * TN) + e];
+      v.x += x.x;
+      v.y += x.y;
+    }
+    const long long idx = (long long)(r.m0 + m) + (long long)(r.n0 + n) * r.ldo;
+    if (r.accumulate) {
+      double2 o = O[idx];
+      o.x += v.x;
+      o.y += v.y;
+      O[idx] = o;
+    } else {
+      O[idx] = v;
+    }
+  }
 }
 
 // ----------------------------------------------------------- wave vectors
@@ -311,10 +351,11 @@ cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, c
 
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
                                      double2* base_out, cudaStream_t s) {
-  if (L.tiles.empty()) return cudaSuccess;
-  // grid.x = tiles; the 65535 limit applies to grid.y only
-  dim3 grid((unsigned)L.tiles.size(), 1);
-  seg_gemm_fp64_kernel<<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, 0, 0, 0);
+  if (L.n_work == 0) return cudaSuccess;
+  // grid.x = work tiles; the 65535 limit applies to grid.y only
+  dim3 grid((unsigned)L.n_work, 1);
+  seg_gemm_fp64_kernel<<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part, 0, 0, 0);
+  if (L.n_red > 0) seg_reduce_kernel<<<(unsigned)L.n_red, NT, 0, s>>>(L.d_reds, L.d_part, base_scr, base_out);
   return cudaGetLastError();
 }
 

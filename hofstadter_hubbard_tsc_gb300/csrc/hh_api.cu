@@ -23,10 +23,10 @@ int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what) {
 
 static int ensure_red(hh_ctx* ctx, size_t ndouble) {
   if (ctx->red_cap >= ndouble) return HH_OK;
-  if (ctx->d_red) cudaFree(ctx->d_red);
+  dev_free(ctx, ctx->d_red);
   ctx->d_red = nullptr;
   ctx->red_cap = 0;
-  cudaError_t e = cudaMalloc(&ctx->d_red, ndouble * sizeof(double));
+  cudaError_t e = dev_alloc(ctx, (void**)&ctx->d_red, ndouble * sizeof(double));
   if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(reduction)");
   ctx->red_cap = ndouble;
   return HH_OK;
@@ -43,25 +43,117 @@ static int ensure_hred(hh_ctx* ctx, size_t ndouble) {
   return HH_OK;
 }
 
+cudaError_t dev_alloc(hh_ctx* ctx, void** p, size_t bytes) {
+  *p = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes ? bytes : 256, ctx->pool, ctx->stream);
+  if (e == cudaSuccess && ((uintptr_t)*p & 255)) {
+    cudaFreeAsync(*p, ctx->stream);
+    *p = nullptr;
+    e = cudaErrorMisalignedAddress;
+  }
+  return e;
+}
+
+void dev_free(hh_ctx* ctx, void* p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
 }  // namespace hh
 
-void hh_gemm_list::upload(cudaStream_t s) {
+// Work list of the FP64 segment GEMM.  A GB300 SM retires about two FP64
+// FMAs per clock, so one 64x64 tile advancing 16 k takes about 70 us on one
+// SM: a list whose heavy tiles carry most of the k steps leaves most SMs idle.
+// Tiles whose cost exceeds the target (total cost / (4 x SMs), at least two
+// 16-k steps) are split: long segments into k ranges, then the segment list
+// into contiguous parts of similar cost; each part stores a partial sum and
+// hh_red items add the parts in slot order, so results do not depend on the
+// split's timing.
+void hh_gemm_list::upload(hh_ctx* ctx) {
   release();
-  if (!segs.empty()) {
-    cudaMalloc(&d_segs, segs.size() * sizeof(hh_seg));
-    cudaMemcpyAsync(d_segs, segs.data(), segs.size() * sizeof(hh_seg), cudaMemcpyHostToDevice, s);
+  actx = ctx;
+  const int sms = ctx->sm_count > 0 ? ctx->sm_count : 148;
+  auto seg_cost = [](const hh_seg& s) { return s.kind == HH_SEG_COPY ? 1.0 : 1.0 + (s.K + 15) / 16; };
+  double total = 0.0;
+  for (const auto& t : tiles)
+    for (int i = 0; i < t.nseg; ++i) total += seg_cost(segs[t.seg0 + i]);
+  const double target = std::max(2.0, total / (4.0 * sms));
+  std::vector<hh_seg> wsegs;
+  std::vector<hh_tile> work;
+  std::vector<hh_red> reds;
+  int nparts = 0;
+  const int kmax = (int)target * 16;  // longest k range of one piece
+  auto shift = [](long long off, int base, long long elems) {
+    return off + (base == HH_BASE_ABS ? elems * (long long)sizeof(double2) : elems);
+  };
+  for (const auto& t : tiles) {
+    double cost = 0.0;
+    for (int i = 0; i < t.nseg; ++i) cost += seg_cost(segs[t.seg0 + i]);
+    if (cost <= 1.5 * target) {
+      hh_tile w = t;
+      w.seg0 = (int)wsegs.size();
+      for (int i = 0; i < t.nseg; ++i) wsegs.push_back(segs[t.seg0 + i]);
+      w.part = -1;
+      work.push_back(w);
+      continue;
+    }
+    // k-range pieces of this tile's segments
+    std::vector<hh_seg> pieces;
+    for (int i = 0; i < t.nseg; ++i) {
+      const hh_seg& s = segs[t.seg0 + i];
+      if (s.kind == HH_SEG_COPY || s.K <= kmax) {
+        pieces.push_back(s);
+        continue;
+      }
+      for (int k0 = 0; k0 < s.K; k0 += kmax) {
+        hh_seg p = s;
+        p.K = std::min(kmax, s.K - k0);
+        p.poff = shift(s.poff, s.pbase, s.opP == HH_OP_N ? (long long)k0 * s.ldp : k0);
+        p.qoff = shift(s.qoff, s.qbase, s.opQ == HH_OP_N ? (long long)k0 : (long long)k0 * s.ldq);
+        pieces.push_back(p);
+      }
+    }
+    // contiguous parts of about `target` cost
+    hh_red r{t.ooff, t.obase, t.ldo, t.M, t.N, t.m0, t.n0, t.accumulate, nparts, 0};
+    size_t i = 0;
+    while (i < pieces.size()) {
+      hh_tile w = t;
+      w.seg0 = (int)wsegs.size();
+      double c = 0.0;
+      while (i < pieces.size() && (c == 0.0 || c + seg_cost(pieces[i]) <= target)) {
+        c += seg_cost(pieces[i]);
+        wsegs.push_back(pieces[i++]);
+      }
+      w.nseg = (int)wsegs.size() - w.seg0;
+      w.part = nparts++;
+      work.push_back(w);
+      ++r.nparts;
+    }
+    reds.push_back(r);
   }
-  if (!tiles.empty()) {
-    cudaMalloc(&d_tiles, tiles.size() * sizeof(hh_tile));
-    cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(hh_tile), cudaMemcpyHostToDevice, s);
-  }
+  n_work = (int)work.size();
+  n_red = (int)reds.size();
+  auto up = [&](void** dst, const void* src, size_t bytes) {
+    if (bytes && hh::dev_alloc(ctx, dst, bytes) == cudaSuccess)
+      cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  };
+  up((void**)&d_segs, wsegs.data(), wsegs.size() * sizeof(hh_seg));
+  up((void**)&d_tiles, work.data(), work.size() * sizeof(hh_tile));
+  up((void**)&d_reds, reds.data(), reds.size() * sizeof(hh_red));
+  if (nparts > 0) hh::dev_alloc(ctx, (void**)&d_part, (size_t)nparts * 64 * 64 * sizeof(double2));
 }
 
 void hh_gemm_list::release() {
-  if (d_segs) cudaFree(d_segs);
-  if (d_tiles) cudaFree(d_tiles);
+  if (actx) {
+    hh::dev_free(actx, d_segs);
+    hh::dev_free(actx, d_tiles);
+    hh::dev_free(actx, d_reds);
+    hh::dev_free(actx, d_part);
+  }
   d_segs = nullptr;
   d_tiles = nullptr;
+  d_reds = nullptr;
+  d_part = nullptr;
+  n_work = n_red = 0;
 }
 
 namespace hh {
@@ -180,6 +272,17 @@ int hh_init(int device, hh_ctx_t** out) {
     return HH_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  if (cudaMemPoolCreate(&c->pool, &props) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return HH_ERR_CUDA;
+  }
+  uint64_t keep = UINT64_MAX;  // freed memory stays in the pool for the next step
+  cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   *out = c;
   return HH_OK;
 }
@@ -188,9 +291,12 @@ int hh_finalize(hh_ctx_t* ctx) {
   if (!ctx) return HH_ERR_INVALID;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  if (ctx->d_red) cudaFree(ctx->d_red);
+  dev_free(ctx, ctx->d_red);
   if (ctx->h_red) cudaFreeHost(ctx->h_red);
   release_step_resources(ctx);
+  cudaStreamSynchronize(ctx->stream);
+  // memory still held by live blocks, waves or plans returns with the pool
+  cudaMemPoolDestroy(ctx->pool);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
   return HH_OK;
@@ -238,7 +344,7 @@ static int block_alloc(hh_ctx* ctx, int len, int up_dif, int down_dif, int nsub,
   b->nelem = off;
   b->build_index();
   if (off > 0) {
-    cudaError_t e = cudaMalloc(&b->d, off * sizeof(double2));
+    cudaError_t e = dev_alloc(ctx, (void**)&b->d, off * sizeof(double2));
     if (e != cudaSuccess) {
       delete b;
       return cuda_check(ctx, e, "cudaMalloc(block)");
@@ -320,10 +426,7 @@ int hh_block_download(const hh_block_t* b, double* data) {
 
 int hh_block_free(hh_block_t* b) {
   if (!b) return HH_ERR_INVALID;
-  if (b->d) {
-    cudaStreamSynchronize(b->ctx->stream);
-    cudaFree(b->d);
-  }
+  dev_free(b->ctx, b->d);  // ordered after every queued use of the block
   delete b;
   return HH_OK;
 }
@@ -443,7 +546,7 @@ int hh_wave_create(hh_ctx_t* ctx, int sys_len, int env_len, int nsec, const int*
     w->idx[key4(w->secs[i].su, w->secs[i].sd, w->secs[i].eu, w->secs[i].ed)] = i;
   w->nelem = off;
   if (off > 0) {
-    cudaError_t e = cudaMalloc(&w->d, (size_t)off * nbatch * sizeof(double2));
+    cudaError_t e = dev_alloc(ctx, (void**)&w->d, (size_t)off * nbatch * sizeof(double2));
     if (e != cudaSuccess) {
       delete w;
       return cuda_check(ctx, e, "cudaMalloc(wave)");
@@ -489,10 +592,7 @@ int hh_wave_copy(hh_wave_t* dst, const hh_wave_t* src) {
 
 int hh_wave_free(hh_wave_t* w) {
   if (!w) return HH_ERR_INVALID;
-  if (w->d) {
-    cudaStreamSynchronize(w->ctx->stream);
-    cudaFree(w->d);
-  }
+  dev_free(w->ctx, w->d);
   delete w;
   return HH_OK;
 }
@@ -556,14 +656,14 @@ int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* en
     return st;
   }
   if (p->scratch_elems > 0) {
-    cudaError_t e = cudaMalloc(&p->d_scratch, (size_t)p->scratch_elems * layout->nbatch * sizeof(double2));
+    cudaError_t e = dev_alloc(ctx, (void**)&p->d_scratch, (size_t)p->scratch_elems * layout->nbatch * sizeof(double2));
     if (e != cudaSuccess) {
       delete p;
       return cuda_check(ctx, e, "cudaMalloc(plan scratch)");
     }
   }
-  p->stage1.upload(ctx->stream);
-  p->stage2.upload(ctx->stream);
+  p->stage1.upload(ctx);
+  p->stage2.upload(ctx);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     hh_plan_free(p);
@@ -600,10 +700,10 @@ int hh_plan_free(hh_plan_t* p) {
   p->stage1.release();
   p->stage2.release();
   release_tc_plan(p);
-  if (p->d_scratch) cudaFree(p->d_scratch);
-  if (p->d_krylov) cudaFree(p->d_krylov);
-  if (p->d_host_in) cudaFree(p->d_host_in);
-  if (p->d_host_out) cudaFree(p->d_host_out);
+  dev_free(p->ctx, p->d_scratch);
+  dev_free(p->ctx, p->d_krylov);
+  dev_free(p->ctx, p->d_host_in);
+  dev_free(p->ctx, p->d_host_out);
   delete p;
   return HH_OK;
 }
@@ -635,8 +735,8 @@ int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision) {
   hh_ctx* ctx = p->ctx;
   size_t bytes = (size_t)p->nelem * sizeof(double2);
   cudaError_t e = cudaSuccess;
-  if (!p->d_host_in) e = cudaMalloc(&p->d_host_in, bytes ? bytes : 16);
-  if (e == cudaSuccess && !p->d_host_out) e = cudaMalloc(&p->d_host_out, bytes ? bytes : 16);
+  if (!p->d_host_in) e = dev_alloc(ctx, (void**)&p->d_host_in, bytes);
+  if (e == cudaSuccess && !p->d_host_out) e = dev_alloc(ctx, (void**)&p->d_host_out, bytes);
   if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(matvec_host)");
   e = cudaMemcpyAsync(p->d_host_in, in, bytes, cudaMemcpyHostToDevice, ctx->stream);
   int st = HH_OK;
@@ -721,10 +821,10 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
   const long long n = p->nelem;
   const int slots = maxit + 1;
   if (p->krylov_cap < slots) {
-    if (p->d_krylov) cudaFree(p->d_krylov);
+    dev_free(ctx, p->d_krylov);
     p->d_krylov = nullptr;
     p->krylov_cap = 0;
-    cudaError_t e = cudaMalloc(&p->d_krylov, (size_t)slots * n * sizeof(double2));
+    cudaError_t e = dev_alloc(ctx, (void**)&p->d_krylov, (size_t)slots * n * sizeof(double2));
     if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(Krylov basis)");
     p->krylov_cap = slots;
   }

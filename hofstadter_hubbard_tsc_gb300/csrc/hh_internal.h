@@ -36,6 +36,9 @@ struct hh_ctx {
   cudaStream_t stream = nullptr;
   std::string last_error;
   int sm_count = 0;
+  // stream-ordered memory pool of this context (memory stays cached in the
+  // pool for reuse; allocation and release never synchronise the device)
+  cudaMemPool_t pool = nullptr;
   // scratch reused by reductions (device)
   double* d_red = nullptr;
   size_t red_cap = 0;
@@ -134,15 +137,30 @@ struct hh_tile {
   int m0, n0;      // tile origin inside the rectangle
   int seg0, nseg;
   int accumulate;  // 1: out += acc, 0: out = acc
+  int part;        // -1: store to the output; >= 0: store the partial sum to slot `part`
+};
+
+// Sum, in slot order, of the partial sums of one split output tile.
+struct hh_red {
+  long long ooff;
+  int obase, ldo, M, N, m0, n0, accumulate;
+  int part0, nparts;
 };
 
 struct hh_gemm_list {
-  std::vector<hh_seg> segs;
+  std::vector<hh_seg> segs;     // as built: one tile per output tile
   std::vector<hh_tile> tiles;
+  // device copy (upload): the work list, where tiles heavier than the
+  // balance target are split by segment and k ranges into parts of similar
+  // cost, the reductions of the split tiles and their partial-sum slots
   hh_seg* d_segs = nullptr;
   hh_tile* d_tiles = nullptr;
+  hh_red* d_reds = nullptr;
+  double2* d_part = nullptr;
+  int n_work = 0, n_red = 0;
   double flops = 0.0;
-  void upload(cudaStream_t s);
+  hh_ctx* actx = nullptr;  // context whose pool holds the device copy
+  void upload(hh_ctx* ctx);
   void release();
 };
 
@@ -206,6 +224,10 @@ struct hh_plan {
 
 namespace hh {
 int fail(hh_ctx* ctx, int code, const std::string& msg);
+// device memory from the context's pool, ordered on its stream (256-byte
+// aligned; a misaligned pointer is returned as an error)
+cudaError_t dev_alloc(hh_ctx* ctx, void** p, size_t bytes);
+void dev_free(hh_ctx* ctx, void* p);
 int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what);
 // grouped segment GEMM (FP64); bases[4] = {abs(unused), in, scr, out}
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,

@@ -23,10 +23,11 @@ constexpr int TM = 64, TN = 64;
 // Device-side task lists used once per call.
 struct GemmRun {
   hh_gemm_list L;
+  // queued on the context stream; the task list returns to the pool in
+  // stream order, so nothing here waits for the device
   int run(hh_ctx* ctx, double2* base_in, double2* base_scr, double2* base_out) {
-    L.upload(ctx->stream);
+    L.upload(ctx);
     cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     L.release();
     return cuda_check(ctx, e, "step GEMM");
   }
@@ -280,14 +281,14 @@ extern "C" int hh_renormalize(hh_ctx_t* ctx, const hh_block_t* ori, const hh_blo
     scr += (long long)os.row * tr.sdim;
   }
   double2* d_scr = nullptr;
-  cudaError_t e = cudaMalloc(&d_scr, std::max<long long>(1, scr) * sizeof(double2));
+  cudaError_t e = dev_alloc(ctx, (void**)&d_scr, std::max<long long>(1, scr) * sizeof(double2));
   if (e != cudaSuccess) {
     hh_block_free(eff);
     return cuda_check(ctx, e, "renormalise scratch");
   }
   st = G1.run(ctx, nullptr, d_scr, eff->d);
   if (!st) st = G2.run(ctx, nullptr, d_scr, eff->d);
-  cudaFree(d_scr);
+  dev_free(ctx, d_scr);
   if (st) {
     hh_block_free(eff);
     return st;
@@ -404,15 +405,15 @@ extern "C" int hh_wave_transform(hh_ctx_t* ctx, int dir, const hh_basis_t* sys_b
     G2.add_rect(nw.off + (long long)ocol * nw.sdim + orow, HH_BASE_OUT, nw.sdim, M, N, rects[key], 0);
   }
   double2* d_scr = nullptr;
-  cudaError_t e = cudaMalloc(&d_scr, std::max<long long>(1, scr) * sizeof(double2));
+  cudaError_t e = dev_alloc(ctx, (void**)&d_scr, std::max<long long>(1, scr) * sizeof(double2));
   if (e == cudaSuccess) e = cudaMemsetAsync(new_wave->d, 0, (size_t)new_wave->nelem * sizeof(double2), ctx->stream);
   if (e != cudaSuccess) {
-    if (d_scr) cudaFree(d_scr);
+    dev_free(ctx, d_scr);
     return cuda_check(ctx, e, "wave transform scratch");
   }
   int st = G1.run(ctx, old_wave->d, d_scr, new_wave->d);
   if (!st) st = G2.run(ctx, old_wave->d, d_scr, new_wave->d);
-  cudaFree(d_scr);
+  dev_free(ctx, d_scr);
   if (st) return st;
   return hh_wave_normalize(new_wave);
 }

@@ -51,8 +51,7 @@ void release_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
                   t.d_tiles2, t.d_segs, t.d_csegs, t.d_err};
-  for (void* q : ptrs)
-    if (q) cudaFree(q);
+  for (void* q : ptrs) dev_free(p->ctx, q);
   t = hh_tc_plan();
 }
 
@@ -292,8 +291,8 @@ int build_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
   auto alloc = [&](void** ptr, size_t bytes) -> int {
     if (bytes == 0) bytes = 256;
-    cudaError_t e = cudaMalloc(ptr, bytes);
-    return e == cudaSuccess ? HH_OK : cuda_check(ctx, e, "cudaMalloc(tensor-core plan)");
+    cudaError_t e = dev_alloc(ctx, ptr, bytes);
+    return e == cudaSuccess ? HH_OK : cuda_check(ctx, e, "allocate tensor-core plan");
   };
   int st;
   if ((st = alloc(&t.d_op_img, a_op.size)) || (st = alloc(&t.d_x_img, a_x.size)) ||
