@@ -231,6 +231,32 @@ __global__ void axpy_kernel(double2* y, const double2* x, double a, long long n)
   }
 }
 
+__global__ void axpy_dev_kernel(double2* y, const double2* x, const double* sc, double sign, long long n) {
+  const double a = sign * sc[0];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = y[i], u = x[i];
+    v.x = fma(a, u.x, v.x);
+    v.y = fma(a, u.y, v.y);
+    y[i] = v;
+  }
+}
+
+__global__ void scale_rsqrt_kernel(double2* y, const double* sc, double* root, long long n) {
+  const double r = sqrt(sc[0]);
+  const double a = 1.0 / r;
+  if (root && blockIdx.x == 0 && threadIdx.x == 0) root[0] = r;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 v = y[i];
+    v.x *= a;
+    v.y *= a;
+    y[i] = v;
+  }
+}
+
+__global__ void divide_kernel(double* c, const double* d, int k) {
+  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] /= d[j];
+}
+
 __global__ void scale_kernel(double2* y, double a, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double2 v = y[i];
@@ -365,6 +391,30 @@ cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_
   if (g > 1024) g = 1024;
   dot_partial_kernel<<<g, RB, 0, s>>>(a, b, n, d_out + 1);
   sum_kernel<<<1, RB, 0, s>>>(d_out + 1, g, d_out);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_dot_into(const double2* a, const double2* b, long long n, double* result, double* part,
+                          cudaStream_t s) {
+  int g = grid_for(n, RB);
+  if (g > 1024) g = 1024;
+  dot_partial_kernel<<<g, RB, 0, s>>>(a, b, n, part);
+  sum_kernel<<<1, RB, 0, s>>>(part, g, result);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_axpy_dev(double2* y, const double2* x, const double* sc, double sign, long long n, cudaStream_t s) {
+  axpy_dev_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, x, sc, sign, n);
+  return cudaGetLastError();
+}
+
+cudaError_t wave_scale_rsqrt_dev(double2* y, const double* sc, double* root, long long n, cudaStream_t s) {
+  scale_rsqrt_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, sc, root, n);
+  return cudaGetLastError();
+}
+
+cudaError_t divide_dev(double* c, const double* d, int k, cudaStream_t s) {
+  if (k > 0) divide_kernel<<<1, 128, 0, s>>>(c, d, k);
   return cudaGetLastError();
 }
 

@@ -712,11 +712,11 @@ static int matvec_timed_tc(hh_plan* p, const double2* in, double2* out, int prec
   return matvec_tc(p, in, out, ms);
 }
 
-static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision) {
+static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision, bool check = true) {
   hh_ctx* ctx = p->ctx;
   if (precision != HH_PREC_FP64 && precision != HH_PREC_BF16X3)
     return fail(ctx, HH_ERR_INVALID, "unknown precision");
-  if (precision == HH_PREC_BF16X3) return matvec_tc(p, in, out, nullptr);
+  if (precision == HH_PREC_BF16X3) return matvec_tc(p, in, out, nullptr, check);
   cudaError_t e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
   if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
   if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
@@ -814,6 +814,10 @@ int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int prec
   return HH_OK;
 }
 
+// alpha, beta^2, the Krylov norms <v_j|v_j> and the Gram-Schmidt
+// coefficients stay on the device; one synchronisation per iteration brings
+// alpha_j and beta_j^2 (and the tensor-core error flag) to the host for the
+// breakdown test, the tridiagonal solve and the convergence test.
 static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int first_precision, int precision,
                         double* energy, int* iterations) {
   hh_ctx* ctx = p->ctx;
@@ -828,60 +832,89 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
     if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(Krylov basis)");
     p->krylov_cap = slots;
   }
-  int st = ensure_red(ctx, 128 + 600 * 128);
+  // d_red: [0, KRY) Gram-Schmidt coefficients and partials, then the scalars
+  constexpr size_t KRY = 128 + 600 * 128;
+  int st = ensure_red(ctx, KRY + 4 * 128 + 8 + 1024);
   if (st) return st;
   st = ensure_hred(ctx, 256);
   if (st) return st;
+  double* d_alpha = ctx->d_red + KRY;
+  double* d_beta2 = d_alpha + 128;
+  double* d_beta = d_beta2 + 128;
+  double* d_vv = d_beta + 128;
+  double* d_w2 = d_vv + 128;
+  double* d_part = d_w2 + 8;
+  const bool uses_tc = precision == HH_PREC_BF16X3 || first_precision == HH_PREC_BF16X3;
   double2* V = p->d_krylov;
   cudaStream_t s = ctx->stream;
   auto slot = [&](int j) { return V + (size_t)j * n; };
-  auto dot = [&](const double2* a, const double2* b, double* r) { return dot_dev(ctx, a, b, n, r); };
-  std::vector<double> alpha, beta, vv;
+  auto dot_into = [&](const double2* a, const double2* b, double* r) { return wave_dot_into(a, b, n, r, d_part, s); };
+  // fetch a few device scalars (and the tensor-core error flag) with one sync
+  int* h_err = reinterpret_cast<int*>(ctx->h_red + 8);
+  auto fetch = [&](std::initializer_list<const double*> src) -> int {
+    int i = 0;
+    cudaError_t e = cudaSuccess;
+    for (const double* q : src) {
+      if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_red + i, q, sizeof(double), cudaMemcpyDeviceToHost, s);
+      ++i;
+    }
+    *h_err = 0;
+    int* d_tcerr = uses_tc && p->tc.ready ? p->tc.d_err : nullptr;  // the plan is built by the first product
+    if (e == cudaSuccess && d_tcerr) e = cudaMemcpyAsync(h_err, d_tcerr, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos");
+    if (*h_err) {
+      cudaMemsetAsync(d_tcerr, 0, sizeof(int), s);
+      return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
+                                           std::to_string(*h_err) + ")");
+    }
+    return HH_OK;
+  };
+  std::vector<double> alpha, beta;
   cudaError_t e = cudaMemcpyAsync(slot(0), psi->d, n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos copy");
-  double nrm2 = 0.0;
-  if ((st = dot(slot(0), slot(0), &nrm2))) return st;
-  if (!(nrm2 > 0.0)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos start vector is zero");
-  wave_scale(slot(0), 1.0 / std::sqrt(nrm2), n, s);
-  if ((st = dot(slot(0), slot(0), &nrm2))) return st;
-  vv.push_back(nrm2);
+  if (e == cudaSuccess) e = dot_into(slot(0), slot(0), d_w2);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos start");
+  if ((st = fetch({d_w2}))) return st;
+  if (!(ctx->h_red[0] > 0.0)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos start vector is zero");
+  e = wave_scale_rsqrt_dev(slot(0), d_w2, nullptr, n, s);
+  if (e == cudaSuccess) e = dot_into(slot(0), slot(0), d_vv + 0);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos start");
   int last = 1;
-  if ((st = matvec_dev(p, slot(0), slot(1), first_precision))) return st;
-  double a0 = 0.0;
-  if ((st = dot(slot(0), slot(1), &a0))) return st;
-  alpha.push_back(a0);
-  double ritz = a0;
+  if ((st = matvec_dev(p, slot(0), slot(1), first_precision, false))) return st;
+  if ((e = dot_into(slot(0), slot(1), d_alpha + 0)) != cudaSuccess) return cuda_check(ctx, e, "Lanczos alpha");
+  if ((st = fetch({d_alpha}))) return st;
+  alpha.push_back(ctx->h_red[0]);
+  double ritz = alpha[0];
   while (last < maxit) {
+    double2* w = slot(last);
     // three-term recurrence (code/lanczos.f90:65-75)
-    wave_axpy(slot(last), slot(last - 1), -alpha[last - 1], n, s);
-    if (last >= 2) wave_axpy(slot(last), slot(last - 2), -beta[last - 2], n, s);
-    double b2 = 0.0;
-    if ((st = dot(slot(last), slot(last), &b2))) return st;
-    double b = std::sqrt(b2);
-    beta.push_back(b);
-    if (!std::isfinite(b)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos: non-finite beta");
-    if (std::fabs(b) <= lanzero) break;  // breakdown (code/lanczos.f90:78)
-    wave_scale(slot(last), 1.0 / b, n, s);
+    e = wave_axpy_dev(w, slot(last - 1), d_alpha + (last - 1), -1.0, n, s);
+    if (e == cudaSuccess && last >= 2) e = wave_axpy_dev(w, slot(last - 2), d_beta + (last - 2), -1.0, n, s);
+    // beta = ||w||, w /= beta
+    if (e == cudaSuccess) e = dot_into(w, w, d_beta2 + (last - 1));
+    if (e == cudaSuccess) e = wave_scale_rsqrt_dev(w, d_beta2 + (last - 1), d_beta + (last - 1), n, s);
     // Gram-Schmidt against all previous vectors, real inner product
     // (Gram_Schmidt_process, code/space_info.f90:1176-1214)
-    e = krylov_dots(V, last, n, slot(last), n, ctx->d_red, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_red, ctx->d_red, last * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos reorthogonalisation");
-    for (int j = 0; j < last; ++j) ctx->h_red[j] /= vv[j];
-    e = cudaMemcpyAsync(ctx->d_red, ctx->h_red, last * sizeof(double), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = krylov_update(V, last, n, slot(last), n, ctx->d_red, s);
-    if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos reorthogonalisation");
-    double w2 = 0.0;
-    if ((st = dot(slot(last), slot(last), &w2))) return st;
-    wave_scale(slot(last), 1.0 / std::sqrt(w2), n, s);
-    if ((st = dot(slot(last), slot(last), &w2))) return st;
-    vv.push_back(w2);
+    if (e == cudaSuccess) e = krylov_dots(V, last, n, w, n, ctx->d_red, s);
+    if (e == cudaSuccess) e = divide_dev(ctx->d_red, d_vv, last, s);
+    if (e == cudaSuccess) e = krylov_update(V, last, n, w, n, ctx->d_red, s);
+    if (e == cudaSuccess) e = dot_into(w, w, d_w2);
+    if (e == cudaSuccess) e = wave_scale_rsqrt_dev(w, d_w2, nullptr, n, s);
+    if (e == cudaSuccess) e = dot_into(w, w, d_vv + last);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos recurrence");
     ++last;
-    if ((st = matvec_dev(p, slot(last - 1), slot(last), precision))) return st;
-    double al = 0.0;
-    if ((st = dot(slot(last - 1), slot(last), &al))) return st;
-    alpha.push_back(al);
+    if ((st = matvec_dev(p, slot(last - 1), slot(last), precision, false))) return st;
+    if ((e = dot_into(slot(last - 1), slot(last), d_alpha + (last - 1))) != cudaSuccess)
+      return cuda_check(ctx, e, "Lanczos alpha");
+    if ((st = fetch({d_beta2 + (last - 2), d_alpha + (last - 1)}))) return st;
+    const double b = std::sqrt(ctx->h_red[0]);
+    beta.push_back(b);
+    if (!std::isfinite(b)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos: non-finite beta");
+    if (std::fabs(b) <= lanzero) {  // breakdown (code/lanczos.f90:78): the new vector is not kept
+      --last;
+      break;
+    }
+    alpha.push_back(ctx->h_red[1]);
     double d0 = 0.0;
     if ((st = tridiag_lowest(last, alpha.data(), beta.data(), &d0, nullptr)))
       return fail(ctx, st, "tridiagonal eigensolver did not converge");

@@ -234,6 +234,14 @@ cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, do
                                      double2* base_out, cudaStream_t s);
 // wave vector kernels
 cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_out, cudaStream_t s);
+// device-resident scalars (Lanczos): *result = Re<a|b> (part: >= 1024 partials),
+// y += sign * s[0] * x, y *= 1/sqrt(s[0]) (and root[0] = sqrt(s[0]) when
+// root != nullptr), c[j] /= d[j] for j < k
+cudaError_t wave_dot_into(const double2* a, const double2* b, long long n, double* result, double* part,
+                          cudaStream_t s);
+cudaError_t wave_axpy_dev(double2* y, const double2* x, const double* sc, double sign, long long n, cudaStream_t s);
+cudaError_t wave_scale_rsqrt_dev(double2* y, const double* sc, double* root, long long n, cudaStream_t s);
+cudaError_t divide_dev(double* c, const double* d, int k, cudaStream_t s);
 cudaError_t wave_axpy(double2* y, const double2* x, double a, long long n, cudaStream_t s);
 cudaError_t wave_scale(double2* y, double a, long long n, cudaStream_t s);
 cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, cudaStream_t s);
@@ -247,7 +255,9 @@ int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wav
                int nterm, const hh_term_t* terms, hh_plan* plan);
 int build_tc_plan(hh_plan* plan);
 void release_tc_plan(hh_plan* plan);
-int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms);
+// check = false: queue only; a bounded wait that ran out is left in the
+// plan's error flag (p->tc.d_err) for the caller to read
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check = true);
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
 int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
 // Eigenvalues (ascending, into *d_w: sector k's at the sum of the earlier

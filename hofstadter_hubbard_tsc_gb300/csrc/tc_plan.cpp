@@ -353,7 +353,7 @@ int build_tc_plan(hh_plan* p) {
   return HH_OK;
 }
 
-int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms) {
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check) {
   hh_ctx* ctx = p->ctx;
   if (!p->tc.ready) {
     int st = build_tc_plan(p);
@@ -372,6 +372,7 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms) {
   if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, out, t.d_err, false, ctx->stream);
   if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, ctx->stream);
   if (ms) cudaEventRecord(ev[3], ctx->stream);
+  if (!check && !ms) return cuda_check(ctx, e, "tensor-core matvec");  // caller reads the flag later
   int herr = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, t.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
