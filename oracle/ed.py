@@ -97,3 +97,79 @@ def free_fermion_energy(lat, n_elec):
         h[j - 1, i - 1] += np.conj(amp)
     eps = np.linalg.eigvalsh(h)
     return 2.0 * float(np.sum(eps[:n_elec // 2]))
+
+
+# ---------------------------------------------------------------- t-J model
+def _tj_apply(state, ops, nsite):
+    """Apply fermion operators right to left; ops = [(mode, dagger)], mode =
+    site (up) or nsite + site (down).  Returns (sign, state) or (0, None)."""
+    sign = 1.0
+    for mode, dag in reversed(ops):
+        occ = (state >> mode) & 1
+        if dag == occ:
+            return 0.0, None
+        if bin(state & ((1 << mode) - 1)).count("1") % 2:
+            sign = -sign
+        state ^= 1 << mode
+    return sign, state
+
+
+def tj_ground_energies(lat, n_up, n_dn, k=1):
+    """Lowest k levels of H = -t sum P(c+_is c_js + h.c.)P + J sum_<ij> (S_i.S_j - n_i n_j / 4)
+    in the (n_up, n_dn) sector, no double occupancy, same bonds and Peierls
+    factors as the Hubbard case."""
+    N = lat.N
+    confs = []
+    for ups in combinations(range(N), n_up):
+        u = sum(1 << b for b in ups)
+        for dns in combinations([x for x in range(N) if not (u >> x) & 1], n_dn):
+            confs.append(u | (sum(1 << b for b in dns) << N))
+    idx = {c: n for n, c in enumerate(confs)}
+    rows, cols, vals = [], [], []
+
+    def add(c, ops, amp):
+        s, c2 = _tj_apply(c, ops, N)
+        if c2 is None:
+            return
+        u, d = c2 & ((1 << N) - 1), c2 >> N
+        if u & d:
+            return  # projected out: double occupancy
+        rows.append(idx[c2]); cols.append(idx[c]); vals.append(s * amp)
+
+    for c in confs:
+        for (i, j) in _bonds(lat):
+            a, b = i - 1, j - 1
+            amp = -lat.t * lat.phase(i, j)
+            for sh in (0, N):
+                add(c, [(a + sh, 1), (b + sh, 0)], amp)
+                add(c, [(b + sh, 1), (a + sh, 0)], np.conj(amp))
+            # J (S_a.S_b - n_a n_b / 4): diagonal part Sz Sz - n n / 4
+            ua, da = (c >> a) & 1, (c >> (a + N)) & 1
+            ub, db = (c >> b) & 1, (c >> (b + N)) & 1
+            szz = 0.25 * (ua - da) * (ub - db)
+            nn = (ua + da) * (ub + db)
+            if szz - 0.25 * nn != 0.0:
+                rows.append(idx[c]); cols.append(idx[c]); vals.append(lat.J * (szz - 0.25 * nn))
+            # (S+_a S-_b + S-_a S+_b) / 2
+            add(c, [(a, 1), (a + N, 0), (b + N, 1), (b, 0)], 0.5 * lat.J)
+            add(c, [(a + N, 1), (a, 0), (b, 1), (b + N, 0)], 0.5 * lat.J)
+    m = len(confs)
+    H = sp.csr_matrix((vals, (rows, cols)), shape=(m, m), dtype=np.complex128)
+    if m <= 400:
+        return np.linalg.eigvalsh(H.toarray())[:k]
+    w = spla.eigsh(H, k=k, which="SA", return_eigenvectors=False, tol=1e-12)
+    return np.sort(w)
+
+
+def tj_singlet_ground_energy(lat, n_elec, k=10, tol=1e-7):
+    """Lowest S=0 energy of the t-J model (Sz=0 levels not matched by Sz=1 ones)."""
+    e0 = list(tj_ground_energies(lat, n_elec // 2, n_elec // 2, k=k))
+    e1 = list(tj_ground_energies(lat, n_elec // 2 + 1, n_elec // 2 - 1, k=k))
+    pool = list(e1)
+    for e in e0:
+        hit = [i for i, f in enumerate(pool) if abs(f - e) < tol]
+        if hit:
+            pool.pop(hit[0])
+            continue
+        return float(e)
+    raise RuntimeError("no singlet among the lowest levels; raise k")

@@ -12,10 +12,10 @@ pytestmark = pytest.mark.gpu
 RTOL = 1e-12  # relative to ||H psi||; complex FP64 on both sides
 
 
-def _check_case(device, W, L, ne, m, U=8.0, phi=0.25, stride=1):
-    lat, d = H.record_superblocks(W, L, ne, m, U=U, phi=phi)
+def _check_case(device, W, L, ne, m, U=8.0, phi=0.25, stride=1, model="hubbard", J=0.0):
+    lat, d = H.record_superblocks(W, L, ne, m, U=U, phi=phi, model=model, J=J)
     plat = H.product_lattice(lat)
-    st = SiteOps("hubbard")
+    st = SiteOps(model)
     worst = 0.0
     for idx, rec in enumerate(d.record[::stride]):
         sys, env, sys_bs, env_bs, geo, sup, guess = rec
@@ -38,6 +38,11 @@ def test_matvec_ladder_2x6(device):
 
 def test_matvec_cylinder_4x3(device):
     _check_case(device, 4, 3, 10, 24, U=4.0, stride=2)
+
+
+def test_matvec_tj_ladder_2x6(device):
+    """t-J terms (S.S and n n couplings, the v123 branch of model_wave)."""
+    _check_case(device, 2, 6, 10, 32, U=0.0, phi=1.0 / 6.0, model="tj", J=0.4)
 
 
 def test_matvec_hermitian(device):

@@ -22,6 +22,15 @@ def test_gpu_dmrg_exact(device, W, L, ne, U, phi):
     assert e == pytest.approx(es, abs=1e-8)
 
 
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_gpu_dmrg_tj_exact(device, precision):
+    lat = SquareLattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
+    d = GPUDMRG(device, lat, 6, kept_min=300, kept_max=300, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    e = d.run(sweeps=1)
+    es = ed.tj_singlet_ground_energy(Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0), 6)
+    assert e == pytest.approx(es, abs=1e-8)
+
+
 def test_gpu_dmrg_split_precision(device):
     lat = SquareLattice(2, 6, U=8.0, phi=0.25)
     d64 = GPUDMRG(device, lat, 10, kept_min=48, kept_max=48, trun_err=1e-14, lanzero=1e-10)

@@ -30,3 +30,13 @@ def test_hubbard_exact(W, L, ne, U, phi):
     # every finite-sweep step sees the same ground state
     finals = [r[2] for r in d.energies[-4:]]
     assert np.ptp(finals) < 1e-9
+
+
+@pytest.mark.parametrize("W,L,ne,phi", [(2, 3, 4, 1.0 / 6.0), (2, 4, 6, 1.0 / 6.0), (4, 2, 6, 0.25)])
+def test_tj_exact(W, L, ne, phi):
+    """t-J model (J = 0.4, the t-J configuration's coupling): the oracle DMRG
+    against a Fock-basis t-J diagonalisation with no double occupancy and
+    J (S_i.S_j - n_i n_j / 4) on every bond."""
+    lat = Lattice(W, L, model="tj", J=0.4, U=0.0, phi=phi)
+    e, _ = _dmrg(lat, ne, m=300, sweeps=1)
+    assert e == pytest.approx(ed.tj_singlet_ground_energy(lat, ne), abs=1e-9)
