@@ -288,30 +288,51 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
     ms = (C.c_float * 4)()
 
-    def step():
+    # launch autotuner (split precision): stage 1 / stage 2 persistent or per tile
+    tune_ms, tune_choice = np.zeros(4), C.c_int(0)
+    t0 = time.perf_counter()
+    dev.check(dev.lib.hh_plan_tune(sb.plan, prec, 3, tune_ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                   C.byref(tune_choice)))
+    tune_s = time.perf_counter() - t0
+
+    def staged():
         dev.check(dev.lib.hh_matvec_timed(sb.plan, w_in.h, w_out.h, prec, ms))
         return ms[0], ms[1], ms[2], ms[3]
 
-    for _ in range(args.warmup):
-        step()
+    # timed steps: the user-facing matvec (hh_matvec_async: one CUDA-graph
+    # replay on the library's stream), CUDA events on that stream, L2 flushed
+    # before each step outside the event window
+    for _ in range(max(args.warmup, 3)):
+        dev.check(dev.lib.hh_matvec_async(sb.plan, w_in.h, w_out.h, prec))
+    dev.check(dev.lib.hh_plan_check(sb.plan))
     if dist:
         dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = Clocks(local)
     clocks.start()
-    tot = s1 = s2 = s0 = 0.0
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("timed")
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
+    with torch.cuda.stream(stream):
+        for a, b in ev:
             flush.zero_()
-        a, b, c, d = step()
-        tot += a
-        s1 += b
-        s2 += c
-        s0 += d
+            a.record(stream)
+            dev.check(dev.lib.hh_matvec_async(sb.plan, w_in.h, w_out.h, prec))
+            b.record(stream)
+    dev.check(dev.lib.hh_plan_check(sb.plan))
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
+    tot = sum(a.elapsed_time(b) for a, b in ev)
+    # per-stage device times of the same matvec launched eagerly with events
+    # between the stages (same flush), for the roofline of the dominant kernel
+    s1 = s2 = s0 = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        _, b, c, d = staged()
+        s1 += b
+        s2 += c
+        s0 += d
     t_steps = tot / 1e3  # seconds, device time of the K matvecs
     if dist:
         t = torch.tensor([t_steps], dtype=torch.float64, device="cuda")
@@ -348,7 +369,7 @@ def main():
     peaks = measured_peaks()
     stage = 1 if s1 >= s2 else 2
     t_stage = (s1 if stage == 1 else s2) / args.steps * 1e-3
-    counts = np.zeros(16)
+    counts = np.zeros(20)
     dev.check(dev.lib.hh_plan_stats(sb.plan, counts.ctypes.data_as(dp)))
     flops_stage = counts[8] if stage == 1 else counts[9]
     achieved = flops_stage / t_stage / 1e12
@@ -377,13 +398,19 @@ def main():
             "data": "synthetic",
             "config": dict(wl.describe(), **{"precision": args.precision, "l2": "flushed between steps (256 MB write)",
                                              "parallelism": f"replicas x{ws}",
+                                             "matvec_launch": ("one CUDA-graph replay per step (hh_matvec_async)"
+                                                               if prec != _lib.HH_PREC_FP64 else "eager"),
+                                             "autotune": ({"variants_ms": [round(x, 4) for x in tune_ms],
+                                                           "variant_index": "2*stage1_persistent+stage2_persistent",
+                                                           "chosen": int(tune_choice.value), "tune_s": round(tune_s, 3)}
+                                                          if prec != _lib.HH_PREC_FP64 else None),
                                              "ref_gflop_per_matvec": counts[0] / 1e9,
                                              "exec_gflop_per_matvec": counts[1] / 1e9,
                                              "plan_setup_s": setup_s}),
             "roofline": roofline, "e2e": e2e, "clocks": clk,
             "stage_ms": {"wave_images": s0 / args.steps, "stage1": s1 / args.steps,
                          "stage2_and_copy_terms": s2 / args.steps},
-            "gpu_launches": args.steps * (2 if prec == _lib.HH_PREC_FP64 else 4)}
+            "gpu_launches": int(args.steps * (counts[16] if prec == _lib.HH_PREC_FP64 else counts[17]))}
     if prec != _lib.HH_PREC_FP64:
         w_in.upload(psi)
         dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, _lib.HH_PREC_FP64))

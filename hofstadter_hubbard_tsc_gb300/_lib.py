@@ -84,6 +84,9 @@ SIGNATURES = {
     "hh_matvec": (I, [P, P, P, I]),
     "hh_matvec_host": (I, [P, DP, DP, I]),
     "hh_lanczos": (I, [P, P, D, I, I, DP, IP]),
+    "hh_plan_tune": (I, [P, I, I, DP, IP]),
+    "hh_matvec_async": (I, [P, P, P, I]),
+    "hh_plan_check": (I, [P]),
     "hh_matvec_timed": (I, [P, P, P, I, C.POINTER(C.c_float)]),
     "hh_matvec_noalloc": (I, [P, P, P]),
     "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP]),

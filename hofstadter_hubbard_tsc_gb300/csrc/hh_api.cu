@@ -691,6 +691,13 @@ int hh_plan_stats(const hh_plan_t* p, double* c) {
   c[13] = p->tc.mma_flops2;
   c[14] = p->tc.bytes_op + p->tc.bytes_x + p->tc.bytes_t;
   c[15] = p->tc.ready ? 1.0 : 0.0;
+  // kernels of one matvec: FP64 (two segment GEMMs and their reductions of
+  // split tiles) and split precision (graph replay: set_io, wave images,
+  // stage 1, zeroing, stage 2, copy terms)
+  c[16] = 2.0 + (p->stage1.n_red > 0) + (p->stage2.n_red > 0);
+  c[17] = 5.0 + (p->tc.n_cseg > 0);
+  c[18] = (double)(p->stage1.n_work + p->stage2.n_work);
+  c[19] = p->tc.persistent1 ? 1.0 : 0.0;
   return HH_OK;
 }
 
@@ -770,6 +777,42 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
   }
   for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
   return cuda_check(ctx, e, "matvec_timed");
+}
+
+int hh_matvec_async(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision) {
+  if (!p || !in || !out) return HH_ERR_INVALID;
+  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out)
+    return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
+  return matvec_dev(p, in->d, out->d, precision, false);
+}
+
+int hh_plan_check(hh_plan_t* p) {
+  if (!p) return HH_ERR_INVALID;
+  hh_ctx* ctx = p->ctx;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "plan check");
+  if (!p->tc.ready) return HH_OK;
+  int herr = 0;
+  e = cudaMemcpy(&herr, p->tc.d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "plan check");
+  if (herr) {
+    cudaMemset(p->tc.d_err, 0, sizeof(int));
+    return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
+                                         std::to_string(herr) + ")");
+  }
+  return HH_OK;
+}
+
+int hh_plan_tune(hh_plan_t* p, int precision, int reps, double* ms, int* choice) {
+  if (!p || reps < 1) return HH_ERR_INVALID;
+  if (precision == HH_PREC_FP64) {  // one launch shape: nothing to choose
+    if (choice) *choice = 0;
+    return HH_OK;
+  }
+  if (precision != HH_PREC_BF16X3) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
+  int st = tune_tc_plan(p, reps, ms);
+  if (st == HH_OK && choice) *choice = 2 * (int)p->tc.persistent1 + (int)p->tc.persistent2;
+  return st;
 }
 
 int hh_host_alloc(long long bytes, void** ptr) {

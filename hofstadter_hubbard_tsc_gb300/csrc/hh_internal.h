@@ -182,7 +182,7 @@ struct hh_contrib {
   double cre, cim;
 };
 
-namespace hh { namespace tc { struct ImgTask; struct Seg; struct Tile; } }
+namespace hh { namespace tc { struct ImgTask; struct Seg; struct Tile; struct IoPtrs; } }
 
 struct hh_tc_plan {
   bool ready = false;
@@ -198,6 +198,14 @@ struct hh_tc_plan {
   hh::tc::Seg* d_segs = nullptr;
   hh_seg* d_csegs = nullptr;
   int* d_err = nullptr;
+  // the matvec captured as a CUDA graph (after the first, eager call); the
+  // graph's kernels read the vectors from d_io, set before each replay
+  hh::tc::IoPtrs* d_io = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int calls = 0;
+  // launch choices (hh_plan_tune): stage 1 / stage 2 on the persistent kernel
+  bool persistent1 = true, persistent2 = false;
   double bytes_op = 0, bytes_x = 0, bytes_t = 0;
   double mma_flops1 = 0, mma_flops2 = 0;  // tensor FLOPs issued (bf16), padding included
 };
@@ -258,6 +266,7 @@ void release_tc_plan(hh_plan* plan);
 // check = false: queue only; a bounded wait that ran out is left in the
 // plan's error flag (p->tc.d_err) for the caller to read
 int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check = true);
+int tune_tc_plan(hh_plan* p, int reps, double* ms);
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
 int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
 // Eigenvalues (ascending, into *d_w: sector k's at the sum of the earlier

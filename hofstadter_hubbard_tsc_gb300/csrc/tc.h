@@ -45,19 +45,31 @@ struct Tile {
   int pad;
 };
 
+// Input and output waves of a matvec, read by the kernels from device memory
+// when a captured graph replays the matvec for new vectors (io != nullptr);
+// the explicit pointer arguments serve the eager launches.
+struct IoPtrs {
+  const double2* in;
+  double2* out;
+};
+
 size_t tile_smem_bytes();
 
 }  // namespace tc
 
 // fp32: scale and split in FP32 (wave images) instead of FP64 (operator images)
 cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
-                            cudaStream_t s);
+                            cudaStream_t s, const tc::IoPtrs* io = nullptr);
 // adds the FP64 copy terms of the stage-2 tiles to their output rectangles
 cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
-                          double2* base_out, cudaStream_t s);
+                          double2* base_out, cudaStream_t s, const tc::IoPtrs* io = nullptr);
+// writes the vectors of the next graph replay (one thread; arguments by value)
+cudaError_t tc_set_io(tc::IoPtrs* d_io, const double2* in, double2* out, cudaStream_t s);
+// zeroes n complex elements of io->out (graph replays) or of out
+cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoPtrs* io = nullptr);
 // tile GEMM over ntile tiles: persistent (one CTA per SM, CTA b takes tiles
 // b, b + G, ...: the list must be ordered for balance) or one CTA per tile
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s);
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io = nullptr);
 
 }  // namespace hh

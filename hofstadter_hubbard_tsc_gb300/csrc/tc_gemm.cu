@@ -159,7 +159,9 @@ __device__ __forceinline__ size_t img_off(int r8, int r, int k) {
 // its FP64 rate.  Operator images (built once per plan) keep the FP64 split.
 template <bool kFp32>
 __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __restrict__ tasks,
-                                                           const double2* __restrict__ base_in) {
+                                                           const double2* __restrict__ base_in,
+                                                           const IoPtrs* __restrict__ io) {
+  if (io) base_in = io->in;
   const ImgTask t = tasks[blockIdx.x];
   const double2* src = t.sbase == HH_BASE_IN ? base_in + t.src : reinterpret_cast<const double2*>(t.src);
   uint8_t* dst = reinterpret_cast<uint8_t*>(t.dst);
@@ -225,7 +227,9 @@ __device__ __forceinline__ void flag_error(int* err, int code) {
 template <int STAGES>
 __global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* __restrict__ tiles,
                                                                   const Seg* __restrict__ segs,
-                                                                  double2* __restrict__ base_out, int* err) {
+                                                                  double2* __restrict__ base_out, int* err,
+                                                                  const IoPtrs* __restrict__ io) {
+  if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
   const Tile t = tiles[blockIdx.x];
   const int stage_bytes = kStageA + 6 * 128 * 32;
@@ -422,7 +426,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 template <int STAGES>
 __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __restrict__ tiles, int ntile,
                                                              const Seg* __restrict__ segs,
-                                                             double2* __restrict__ base_out, int* err) {
+                                                             double2* __restrict__ base_out, int* err,
+                                                             const IoPtrs* __restrict__ io) {
+  if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
   const int stage_bytes = kStageA + 6 * 128 * 32;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
@@ -653,7 +659,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
 __global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict__ tiles,
                                                          const hh_seg* __restrict__ csegs,
                                                          const double2* __restrict__ base_in,
-                                                         double2* __restrict__ base_out) {
+                                                         double2* __restrict__ base_out,
+                                                         const IoPtrs* __restrict__ io) {
+  if (io) {
+    base_in = io->in;
+    base_out = io->out;
+  }
   const Tile t = tiles[blockIdx.x];
   if (t.mode != 0 || t.ncseg == 0) return;
   double2* O = base_out + t.out;
@@ -671,6 +682,17 @@ __global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict_
   }
 }
 
+__global__ void set_io_kernel(IoPtrs* io, const double2* in, double2* out) {
+  io->in = in;
+  io->out = out;
+}
+
+__global__ void zero_out_kernel(double2* out, long long n, const IoPtrs* __restrict__ io) {
+  if (io) out = io->out;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = make_double2(0.0, 0.0);
+}
+
 constexpr int kStages = 4;
 
 size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8 * (2 * kStages + 3) + 64; }
@@ -678,24 +700,37 @@ size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8
 }  // namespace tc
 
 cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
-                            cudaStream_t s) {
+                            cudaStream_t s, const tc::IoPtrs* io) {
   if (ntask <= 0) return cudaSuccess;
   if (fp32)
-    tc::build_images_kernel<true><<<ntask, 256, 0, s>>>(d_tasks, base_in);
+    tc::build_images_kernel<true><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
   else
-    tc::build_images_kernel<false><<<ntask, 256, 0, s>>>(d_tasks, base_in);
+    tc::build_images_kernel<false><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
   return cudaGetLastError();
 }
 
 cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
-                          double2* base_out, cudaStream_t s) {
+                          double2* base_out, cudaStream_t s, const tc::IoPtrs* io) {
   if (ntile <= 0) return cudaSuccess;
-  tc::copy_terms_kernel<<<ntile, 256, 0, s>>>(d_tiles, d_csegs, base_in, base_out);
+  tc::copy_terms_kernel<<<ntile, 256, 0, s>>>(d_tiles, d_csegs, base_in, base_out, io);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_set_io(tc::IoPtrs* d_io, const double2* in, double2* out, cudaStream_t s) {
+  tc::set_io_kernel<<<1, 1, 0, s>>>(d_io, in, out);
+  return cudaGetLastError();
+}
+
+cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoPtrs* io) {
+  if (n <= 0) return cudaSuccess;
+  long long g = (n + 255) / 256;
+  if (g > 4096) g = 4096;
+  tc::zero_out_kernel<<<(unsigned)g, 256, 0, s>>>(out, n, io);
   return cudaGetLastError();
 }
 
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s) {
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io) {
   if (ntile <= 0) return cudaSuccess;
   const size_t smem = tc::tile_smem_bytes();
   static int sms = 0;
@@ -712,9 +747,9 @@ cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_se
   }
   if (persistent && ntile > sms) {
     // one CTA per SM: shared memory and the 512 TMEM columns allow no second
-    tc::tc_tile_kernel<tc::kStages><<<sms, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err);
+    tc::tc_tile_kernel<tc::kStages><<<sms, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io);
   } else {
-    tc::tc_tile_once_kernel<tc::kStages><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err);
+    tc::tc_tile_once_kernel<tc::kStages><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io);
   }
   return cudaGetLastError();
 }

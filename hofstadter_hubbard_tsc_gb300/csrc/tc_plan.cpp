@@ -49,8 +49,10 @@ struct Arena {
 
 void release_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
+  if (t.graph_exec) cudaGraphExecDestroy(t.graph_exec);
+  if (t.graph) cudaGraphDestroy(t.graph);
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
-                  t.d_tiles2, t.d_segs, t.d_csegs, t.d_err};
+                  t.d_tiles2, t.d_segs, t.d_csegs, t.d_err, t.d_io};
   for (void* q : ptrs) dev_free(p->ctx, q);
   t = hh_tc_plan();
 }
@@ -327,7 +329,7 @@ int build_tc_plan(hh_plan* p) {
       (st = upload((void**)&t.d_tiles2, tiles2.data(), tiles2.size() * sizeof(tc::Tile))) ||
       (st = upload((void**)&t.d_segs, segs.data(), segs.size() * sizeof(tc::Seg))) ||
       (st = upload((void**)&t.d_csegs, csegs.data(), csegs.size() * sizeof(hh_seg))) ||
-      (st = alloc((void**)&t.d_err, sizeof(int)))) {
+      (st = alloc((void**)&t.d_err, sizeof(int))) || (st = alloc((void**)&t.d_io, sizeof(tc::IoPtrs)))) {
     release_tc_plan(p);
     return st;
   }
@@ -353,6 +355,24 @@ int build_tc_plan(hh_plan* p) {
   return HH_OK;
 }
 
+// The launch sequence of one split-precision matvec: wave images, stage 1,
+// zeroed output, stage 2, copy terms.  Explicit vectors (io == nullptr) or
+// the vectors in t.d_io (graph capture).
+static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const tc::IoPtrs* io, cudaEvent_t* ev) {
+  hh_tc_plan& t = p->tc;
+  cudaStream_t s = p->ctx->stream;
+  if (ev) cudaEventRecord(ev[0], s);
+  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io);
+  if (ev) cudaEventRecord(ev[1], s);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, out, t.d_err, t.persistent1, s, io);
+  if (ev) cudaEventRecord(ev[2], s);
+  if (e == cudaSuccess) e = tc_zero_out(out, p->nelem, s, io);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, out, t.d_err, t.persistent2, s, io);
+  if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, s, io);
+  if (ev) cudaEventRecord(ev[3], s);
+  return e;
+}
+
 int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check) {
   hh_ctx* ctx = p->ctx;
   if (!p->tc.ready) {
@@ -360,38 +380,96 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check
     if (st != HH_OK) return st;
   }
   hh_tc_plan& t = p->tc;
-  cudaEvent_t ev[4];
-  if (ms)
+  cudaError_t e = cudaSuccess;
+  if (ms) {
+    // eager launches with events between the stages
+    cudaEvent_t ev[4];
     for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
-  if (ms) cudaEventRecord(ev[0], ctx->stream);
-  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, ctx->stream);
-  if (ms) cudaEventRecord(ev[1], ctx->stream);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, out, t.d_err, true, ctx->stream);
-  if (ms) cudaEventRecord(ev[2], ctx->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, out, t.d_err, false, ctx->stream);
-  if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, ctx->stream);
-  if (ms) cudaEventRecord(ev[3], ctx->stream);
+    e = enqueue_tc(p, in, out, nullptr, ev);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    if (e == cudaSuccess) {
+      cudaEventElapsedTime(&ms[0], ev[0], ev[3]);
+      cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
+      cudaEventElapsedTime(&ms[2], ev[2], ev[3]);
+      cudaEventElapsedTime(&ms[3], ev[0], ev[1]);
+    }
+    for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  } else if (t.calls++ == 0) {
+    // the first call runs eagerly (and initialises the kernels' attributes)
+    e = enqueue_tc(p, in, out, nullptr, nullptr);
+  } else {
+    if (!t.graph_exec) {
+      e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t eq = enqueue_tc(p, nullptr, nullptr, t.d_io, nullptr);
+        e = cudaStreamEndCapture(ctx->stream, &t.graph);
+        if (e == cudaSuccess) e = eq;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&t.graph_exec, t.graph, 0);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_check(ctx, e, "capture the tensor-core matvec graph");
+      }
+    }
+    e = tc_set_io(t.d_io, in, out, ctx->stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(t.graph_exec, ctx->stream);
+  }
   if (!check && !ms) return cuda_check(ctx, e, "tensor-core matvec");  // caller reads the flag later
   int herr = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, t.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  if (ms && e == cudaSuccess) {
-    cudaEventElapsedTime(&ms[0], ev[0], ev[3]);
-    cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
-    cudaEventElapsedTime(&ms[2], ev[2], ev[3]);
-    float conv = 0.f;
-    cudaEventElapsedTime(&conv, ev[0], ev[1]);
-    ms[3] = conv;
-  }
-  if (ms)
-    for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   if (e != cudaSuccess) return cuda_check(ctx, e, "tensor-core matvec");
   if (herr != 0) {
     cudaMemsetAsync(t.d_err, 0, sizeof(int), ctx->stream);
     return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
                                          std::to_string(herr) + ")");
   }
+  return HH_OK;
+}
+
+// Times the launch variants of the tile GEMM (stage 1 / stage 2 on the
+// persistent kernel or one CTA per tile) on this plan's own task lists, reps
+// timed runs each after one warm-up, and keeps the fastest; ms[v] receives
+// the mean time of variant v = 2 * persistent1 + persistent2.
+int tune_tc_plan(hh_plan* p, int reps, double* ms) {
+  hh_ctx* ctx = p->ctx;
+  if (!p->tc.ready) {
+    int st = build_tc_plan(p);
+    if (st != HH_OK) return st;
+  }
+  hh_tc_plan& t = p->tc;
+  const size_t bytes = (size_t)p->nelem * sizeof(double2);
+  cudaError_t e = cudaSuccess;
+  if (!p->d_host_in) e = dev_alloc(ctx, (void**)&p->d_host_in, bytes);
+  if (e == cudaSuccess && !p->d_host_out) e = dev_alloc(ctx, (void**)&p->d_host_out, bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->d_host_in, 0, bytes, ctx->stream);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "tune buffers");
+  double best = 1e300;
+  int best_v = 2 * (int)t.persistent1 + (int)t.persistent2;
+  for (int v = 0; v < 4; ++v) {
+    t.persistent1 = (v >> 1) & 1;
+    t.persistent2 = v & 1;
+    double sum = 0.0;
+    for (int r = 0; r <= reps; ++r) {
+      float m[4];
+      int st = matvec_tc(p, p->d_host_in, p->d_host_out, m, true);
+      if (st) return st;
+      if (r > 0) sum += m[0];
+    }
+    const double mean = reps > 0 ? sum / reps : 0.0;
+    if (ms) ms[v] = mean;
+    if (mean < best) {
+      best = mean;
+      best_v = v;
+    }
+  }
+  t.persistent1 = (best_v >> 1) & 1;
+  t.persistent2 = best_v & 1;
+  // the next graph is captured with the chosen kernels
+  if (t.graph_exec) cudaGraphExecDestroy(t.graph_exec);
+  if (t.graph) cudaGraphDestroy(t.graph);
+  t.graph_exec = nullptr;
+  t.graph = nullptr;
   return HH_OK;
 }
 

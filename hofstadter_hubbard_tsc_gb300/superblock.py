@@ -247,11 +247,12 @@ class Superblock:
         return h
 
     def stats(self):
-        c = np.zeros(16)
+        c = np.zeros(20)
         self.dev.check(self.dev.lib.hh_plan_stats(self.plan, c.ctypes.data_as(C.POINTER(C.c_double))))
         keys = ["ref_flops", "exec_flops", "tiles", "segments", "stage1", "scratch_bytes", "op_bytes",
                 "wave_bytes", "exec_flops_s1", "exec_flops_s2", "ref_flops_first", "ref_flops_rest",
-                "tc_flops_s1", "tc_flops_s2", "tc_image_bytes", "tc_ready"]
+                "tc_flops_s1", "tc_flops_s2", "tc_image_bytes", "tc_ready", "fp64_launches", "tc_launches",
+                "fp64_work_tiles", "tc_stage1_persistent"]
         return dict(zip(keys, c.tolist()))
 
     def matvec(self, w_in: DWave, w_out: DWave, precision=None):

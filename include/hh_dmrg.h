@@ -143,7 +143,11 @@ int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* en
  * first GEMM of the two-GEMM terms, [11] the remaining reference FLOPs,
  * [12], [13] BF16 tensor FLOPs issued by the split-precision stages 1 and 2
  * (padding included), [14] bytes of its operand images, [15] 1 once the
- * split-precision schedule has been built (first BF16X3 matvec).          */
+ * split-precision schedule has been built (first BF16X3 matvec), [16] kernel
+ * launches of one FP64 matvec, [17] of one split-precision matvec (graph
+ * replay included), [18] FP64 work tiles after balancing, [19] 1 when stage
+ * 1 of the split-precision matvec runs on the persistent kernel.  counts
+ * holds 20 doubles.                                                        */
 int hh_plan_stats(const hh_plan_t* p, double* counts);
 int hh_plan_free(hh_plan_t* p);
 
@@ -172,6 +176,18 @@ int hh_matvec_noalloc(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out);
 int hh_host_alloc(long long bytes, void** ptr);
 int hh_host_free(void* ptr);
 
+/* hh_matvec without the wait: queued on the context stream (the tensor-core
+ * path as one CUDA-graph replay after its first call); a bounded wait that
+ * ran out is reported by the next hh_plan_check, which waits for the stream. */
+int hh_matvec_async(hh_plan_t* plan, const hh_wave_t* in, hh_wave_t* out, int precision);
+int hh_plan_check(hh_plan_t* plan);
+/* Autotuner of the split-precision launch: times the four variants of the
+ * tile GEMM (stage 1 / stage 2 on the persistent kernel or one CTA per tile)
+ * on this plan, reps runs each after a warm-up, and keeps the fastest for
+ * the plan's later matvecs.  ms (may be NULL) receives the four mean times
+ * in ms, index 2 * stage1_persistent + stage2_persistent; *choice (may be
+ * NULL) the kept index.  FP64 plans have nothing to tune (choice 0).      */
+int hh_plan_tune(hh_plan_t* plan, int precision, int reps, double* ms, int* choice);
 /* lanczos_memo_new (code/lanczos.f90:4-177), levels = 1.  psi is the start
  * vector on entry and the ground state on exit; lanzero is the breakdown and
  * convergence threshold; maxit <= 100 is loop_in.  With HH_PREC_BF16X3 the
