@@ -159,6 +159,7 @@ class DWave:
         self.h = h
         dev.adopt(self)
         self.nbatch = nbatch
+        self.sys_len, self.env_len = sys_len, env_len
         self.nelem = int(sum(int(r[4]) * int(r[5]) for r in self.layout))
 
     def upload(self, z):

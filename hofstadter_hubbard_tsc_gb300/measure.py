@@ -1,0 +1,105 @@
+"""Measurements on the GPU DMRG state: site profiles and cross-cut correlations
+of diagonal (rank-0) site operators (code/measure.f90, code/correlation.f90).
+
+measure_operator_dia (code/measure.f90:3-62): <O_i> for every site.  The
+operator of block site i is carried to the block of the current superblock as
+Get_sys_oper_dia / Get_env_oper_dia do (code/get_ham.f90:1244-1380): embedded
+in the enlarged basis of length i (update_site_dia), truncated, then for each
+longer block embedded as a block operator (update_block_dia) and truncated,
+with the bases and truncation operators the sweep left on the device.  Then
+phi_i = (O_i x 1) psi is one matvec of a one-term plan (the block_vec_dia /
+vec_block_dia / site_vec_site_dia kernels of model_wave: measure_sys_block and
+its siblings, code/measure.f90:611-862), and <O_i> = Re <psi|phi_i>.
+
+Cross-cut correlations <O_a O_b>, a on the system half and b on the
+environment half (the cross part of Get_density_cor, code/correlation.f90:43):
+Re <phi_a|chi_b> with chi_b = (1 x O_b) psi, one dot product per pair on the
+device.  Sites are numbered like the reference's output: system block site i
+is site i, environment block site j is site N - j + 1.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .device import DBlock, DWave
+from .step import update_trun
+
+
+def _embed(dev, mode, op, dbasis, side):
+    h = C.c_void_p()
+    dev.check(dev.lib.hh_enlarge_operator(dev.h, mode, op.h, dbasis.h, ord("B"), side, C.byref(h)))
+    return DBlock.from_handle(dev, h)
+
+
+def _carry(dev, op, i, length, bases, truns, side):
+    """Operator of block site i in the truncated block of `length` sites."""
+    cur = op if i <= 1 else update_trun(dev, _embed(dev, 1, op, bases[i][1], side), truns[i], dia=True)
+    for L in range(i + 1, length + 1):
+        cur = update_trun(dev, _embed(dev, 0, cur, bases[L][1], side), truns[L], dia=True)
+    return cur
+
+
+class Measurement:
+    """Measurements on the current superblock of a ``GPUDMRG`` (its last
+    Lanczos state and the bases and truncations it keeps on the device)."""
+
+    def __init__(self, dmrg):
+        self.d = dmrg
+        self.dev = dmrg.dev
+        self.wave, sup = dmrg.wave
+        self.N = dmrg.lat.N
+        self.sys_bs = dmrg.sys_bases[sup.sys_len][1]
+        self.env_bs = dmrg.env_bases[sup.env_len][1]
+        self.Ls, self.Le = sup.sys_len - 1, sup.env_len - 1
+
+    def _apply(self, kind, op0, op1=None):
+        """(one term) psi as a new device wave."""
+        dev, w = self.dev, self.wave
+        t = (_lib.HHTerm * 1)()
+        t[0] = _lib.HHTerm(kind, ord("B"), ord("B"), 0, 0, op0.h, op1.h if op1 is not None else None, 1.0, 0.0)
+        plan = C.c_void_p()
+        dev.check(dev.lib.hh_plan_create(dev.h, self.sys_bs.h, self.env_bs.h, w.h, 1, t, C.byref(plan)))
+        out = DWave(dev, w.layout, w.sys_len, w.env_len)
+        try:
+            dev.check(dev.lib.hh_matvec(plan, w.h, out.h, _lib.HH_PREC_FP64))
+        finally:
+            dev.lib.hh_plan_free(plan)
+        return out
+
+    def site_vectors(self, name):
+        """{site: (side, phi)} with phi = O_site psi (side 0 system half, 1
+        environment half); name is a site operator of the sweep ("num_elec",
+        "double", ...)."""
+        d, dev = self.d, self.dev
+        op, one = d.d_st[name], d.d_st["si"]
+        out = {}
+        for i in range(1, self.Ls + 1):
+            o = _carry(dev, op, i, self.Ls, d.sys_bases, d.sys_truns, 0)
+            out[i] = (0, self._apply(_lib.BLOCK_VEC_DIA, o))
+        out[self.Ls + 1] = (0, self._apply(_lib.SITE_VEC_SITE_DIA, op, one))
+        out[self.N - self.Le] = (1, self._apply(_lib.SITE_VEC_SITE_DIA, one, op))
+        for j in range(1, self.Le + 1):
+            o = _carry(dev, op, j, self.Le, d.env_bases, d.env_truns, 1)
+            out[self.N - j + 1] = (1, self._apply(_lib.VEC_BLOCK_DIA, o))
+        return out
+
+    def site_profile(self, name="num_elec"):
+        """measure_operator_dia: <O_i>, i = 1..N."""
+        prof = np.zeros(self.N)
+        for s, (_, phi) in self.site_vectors(name).items():
+            prof[s - 1] = self.wave.dot(phi)
+            phi.free()
+        return prof
+
+    def cross_correlations(self, name_a="num_elec", name_b="num_elec"):
+        """<O_a O_b>, a on the system half, b on the environment half:
+        (sites_a, sites_b, matrix)."""
+        va = self.site_vectors(name_a)
+        vb = va if name_b == name_a else self.site_vectors(name_b)
+        sa = sorted(s for s, (side, _) in va.items() if side == 0)
+        sb = sorted(s for s, (side, _) in vb.items() if side == 1)
+        m = np.array([[va[a][1].dot(vb[b][1]) for b in sb] for a in sa])
+        for v in {id(x[1]): x[1] for x in list(va.values()) + list(vb.values())}.values():
+            v.free()
+        return sa, sb, m

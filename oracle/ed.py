@@ -173,3 +173,32 @@ def tj_singlet_ground_energy(lat, n_elec, k=10, tol=1e-7):
             continue
         return float(e)
     raise RuntimeError("no singlet among the lowest levels; raise k")
+
+
+def hubbard_density_correlations(lat, n_up, n_dn):
+    """Lowest state of the (n_up, n_dn) sector: energy, <n_i> and <n_i n_j>
+    (Fock-basis exact diagonalisation, sites in lattice order)."""
+    N = lat.N
+    cu = _configs(N, n_up)
+    cd = _configs(N, n_dn)
+    hu = _spin_hop(lat, cu)
+    hd = _spin_hop(lat, cd)
+    H = sp.kron(hu, sp.identity(len(cd)), format="csr") + sp.kron(sp.identity(len(cu)), hd, format="csr")
+    au = np.array(cu, dtype=np.int64)
+    ad = np.array(cd, dtype=np.int64)
+    if lat.U != 0.0:
+        dbl = np.array([[bin(int(x & y)).count("1") for y in ad] for x in au], dtype=np.float64).ravel()
+        H = H + sp.diags(lat.U * dbl)
+    if H.shape[0] <= 2000:
+        w, v = np.linalg.eigh(H.toarray())
+        e0, psi = w[0], v[:, 0]
+    else:
+        w, v = spla.eigsh(H, k=1, which="SA", tol=1e-13)
+        e0, psi = w[0], v[:, 0]
+    p = np.abs(psi) ** 2
+    occ_u = np.array([[(c >> s) & 1 for s in range(N)] for c in au], dtype=np.float64)
+    occ_d = np.array([[(c >> s) & 1 for s in range(N)] for c in ad], dtype=np.float64)
+    n = (occ_u[:, None, :] + occ_d[None, :, :]).reshape(-1, N)   # occupation per basis state
+    dens = p @ n
+    corr = (n * p[:, None]).T @ n
+    return float(e0), dens, corr

@@ -1,0 +1,78 @@
+"""Site profiles and cross-cut correlations of diagonal (rank-0) site operators
+(test infrastructure, restating code/measure.f90).
+
+measure_operator_dia (code/measure.f90:3-62): <O_i> for every site.  The
+operator of block site i is carried to the block of the superblock the way
+Get_sys_oper_dia / Get_env_oper_dia (code/get_ham.f90:1244-1380) do: embedded
+in the enlarged basis of length i (update_site_dia) and truncated, then for each
+longer block embedded as a block operator (update_block_dia) and truncated;
+<O_i> = <psi|(O_i x 1)|psi> is measure_sys_block / measure_env_block
+(code/measure.f90:611-862), and the two middle sites are site terms.
+
+Cross-cut correlations <O_a O_b> with a on the system side and b on the
+environment side (the cross part of Get_density_cor, code/correlation.f90:43):
+with phi_a = (O_a x 1) psi and chi_b = (1 x O_b) psi, <psi|O_a O_b|psi> =
+Re <phi_a|chi_b>, since the two operators act on different halves and are
+Hermitian.  Sites are numbered like the reference's output: system block site
+i is site i, environment block site j is site N - j + 1.
+"""
+import numpy as np
+
+from .blocks import update_site_dia, update_block_dia, update_trun_dia, wave_product
+from .matvec import block_vec_dia, vec_block_dia, site_vec_site_dia
+
+
+def _carry(op, i, length, bases, truns):
+    """Operator of block site i in the truncated block of `length` sites."""
+    cur = op.copy() if i <= 1 else update_trun_dia(update_site_dia(op, bases[i]), truns[i])
+    for L in range(i + 1, length + 1):
+        cur = update_trun_dia(update_block_dia(cur, bases[L]), truns[L])
+    return cur
+
+
+def site_vectors(d, name):
+    """{site: (side, phi)} with phi = O_site psi on the current superblock of an
+    oracle DMRG ``d`` (side 0 system half, 1 environment half)."""
+    wave = d.wave
+    N = d.lat.N
+    st = d.st
+    op, one = getattr(st, name), st.si
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    out = {}
+    for i in range(1, Ls + 1):
+        o = _carry(op, i, Ls, d.sys_bases, d.sys_truns)
+        phi = wave.zeros_like()
+        block_vec_dia(o, sys_bs, wave, phi, 1.0)
+        out[i] = (0, phi)
+    phi = wave.zeros_like()
+    site_vec_site_dia(op, one, sys_bs, env_bs, wave, phi, 1.0)
+    out[Ls + 1] = (0, phi)
+    phi = wave.zeros_like()
+    site_vec_site_dia(one, op, sys_bs, env_bs, wave, phi, 1.0)
+    out[N - Le] = (1, phi)
+    for j in range(1, Le + 1):
+        o = _carry(op, j, Le, d.env_bases, d.env_truns)
+        phi = wave.zeros_like()
+        vec_block_dia(o, env_bs, wave, phi, 1.0)
+        out[N - j + 1] = (1, phi)
+    return out
+
+
+def site_profile(d, name="num_elec"):
+    """measure_operator_dia: <O_i>, i = 1..N."""
+    vec = site_vectors(d, name)
+    prof = np.zeros(d.lat.N)
+    for s, (_, phi) in vec.items():
+        prof[s - 1] = wave_product(d.wave, phi)
+    return prof
+
+
+def cross_correlations(d, name_a="num_elec", name_b="num_elec"):
+    """<O_a O_b> for a on the system half and b on the environment half:
+    (sites_a, sites_b, matrix)."""
+    va, vb = site_vectors(d, name_a), site_vectors(d, name_b)
+    sa = sorted(s for s, (side, _) in va.items() if side == 0)
+    sb = sorted(s for s, (side, _) in vb.items() if side == 1)
+    m = np.array([[wave_product(va[a][1], vb[b][1]) for b in sb] for a in sa])
+    return sa, sb, m

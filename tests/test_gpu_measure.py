@@ -1,0 +1,48 @@
+"""Measurements on the GPU DMRG state (measure_operator_dia and the cross-cut
+part of Get_density_cor) against the exact ground state, and the sum rule on a
+truncated run."""
+import numpy as np
+import pytest
+
+from oracle import ed
+from oracle.lattice import Lattice
+from hofstadter_hubbard_tsc_gb300 import _lib
+from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
+from hofstadter_hubbard_tsc_gb300.measure import Measurement
+from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_density_profile_and_correlations_exact(device, precision):
+    W, L, ne, U, phi = 2, 4, 6, 8.0, 0.25
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    d.run(sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    _, dens, corr = ed.hubbard_density_correlations(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
+    m = Measurement(d)
+    prof = m.site_profile("num_elec")
+    assert prof.sum() == pytest.approx(ne, abs=1e-9)
+    np.testing.assert_allclose(prof, dens, atol=1e-6)
+    sa, sb, c = m.cross_correlations("num_elec", "num_elec")
+    np.testing.assert_allclose(c, corr[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
+
+
+def test_profile_sum_rules_truncated(device):
+    """m = 48 on a 2x8 ladder: <n_i> sums to N_e, <n_a n_b> summed over the
+    environment half equals <n_a N_env>, and double occupancy stays in [0, <n_i>/2]."""
+    lat = SquareLattice(2, 8, U=8.0, phi=0.25)
+    d = GPUDMRG(device, lat, 14, kept_min=48, kept_max=48, trun_err=1e-12, lanzero=1e-10)
+    d.run(sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    m = Measurement(d)
+    n = m.site_profile("num_elec")
+    assert n.sum() == pytest.approx(14.0, abs=1e-8)
+    dbl = m.site_profile("double")
+    assert np.all(dbl >= -1e-10) and np.all(dbl <= n / 2 + 1e-10)
+    sa, sb, c = m.cross_correlations()
+    assert np.all(np.isfinite(c))
+    # sum_b <n_a n_b> <= <n_a> * max particles on the environment side
+    assert np.all(c.sum(axis=1) <= n[np.array(sa) - 1] * 2 * len(sb) + 1e-8)

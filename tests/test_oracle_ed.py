@@ -40,3 +40,19 @@ def test_tj_exact(W, L, ne, phi):
     lat = Lattice(W, L, model="tj", J=0.4, U=0.0, phi=phi)
     e, _ = _dmrg(lat, ne, m=300, sweeps=1)
     assert e == pytest.approx(ed.tj_singlet_ground_energy(lat, ne), abs=1e-9)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_measurements_exact(W, L, ne, U, phi):
+    """measure_operator_dia and the cross-cut density correlations of the
+    oracle against the exact ground state (Fock basis)."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    _, dens, corr = ed.hubbard_density_correlations(lat, ne // 2, ne // 2)
+    _, d = _dmrg(lat, ne, sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    prof = om.site_profile(d)
+    assert prof.sum() == pytest.approx(ne, abs=1e-10)
+    np.testing.assert_allclose(prof, dens, atol=1e-6)
+    sa, sb, m = om.cross_correlations(d)
+    np.testing.assert_allclose(m, corr[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
