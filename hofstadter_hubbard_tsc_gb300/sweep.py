@@ -8,6 +8,8 @@ Models, truncations and waves stay in device memory between steps, where the
 reference writes them to disk per length.
 """
 import ctypes as C
+import json
+import os
 import time
 from collections import defaultdict
 from contextlib import contextmanager
@@ -19,7 +21,8 @@ from .device import DBlock, DBasis, DWave
 from .sites import SiteOperators
 from .step import density_truncate, update_trun, wave_trans, SYS, ENV
 from .superblock import Superblock
-from .types import TotalBlock, SubBlock, get_basis, get_super_basis
+from .types import TotalBlock, SubBlock, TotalModel, SuperBasis, SuperSector, Wavefunction, get_basis, get_super_basis
+from . import disk
 
 F, B = ord("F"), ord("B")
 
@@ -367,6 +370,77 @@ class GPUDMRG:
         trains there) see the finished sweep; runs outside the sweep timer."""
         if self.guess_hook is not None and hasattr(self.guess_hook, "end_sweep"):
             self.guess_hook.end_sweep(self)
+
+    # ------------------------------------------------------------ checkpoints
+    def _op_names(self):
+        names = ["elec_up", "elec_down"]
+        if self.lat.tjmodel:
+            names.append("spin_sd")
+        if self.lat.v123:
+            names.append("num_sn")
+        return names
+
+    def save(self, path):
+        """Writes the sweep state in the reference's on-disk formats
+        (model_to_disk, truns_to_disk, basis_to_disk, wave_to_disk;
+        code/space_info.f90:1406-1762), one file per block length and side,
+        plus state.json with the driver's bookkeeping."""
+        os.makedirs(path, exist_ok=True)
+        names = self._op_names()
+        state = {"n_elec": self.n_elec, "nrand": self._nrand, "guess_kind": self.guess_kind,
+                 "energies": [list(e) for e in self.energies], "models": {}, "truns": {}, "bases": {}}
+        for side, models, truns, bases in (("sys", self.sys_models, self.sys_truns, self.sys_bases),
+                                           ("env", self.env_models, self.env_truns, self.env_bases)):
+            state["models"][side] = {}
+            for L, m in models.items():
+                tm = TotalModel(m.len, m.ham.download(), {ii: {nm: d[nm].download() for nm in names}
+                                                          for ii, d in m.sub.items()})
+                disk.model_to_disk(tm, os.path.join(path, f"{side}_model_{L}.dat"), names)
+                state["models"][side][str(L)] = len(m.sub)
+            for L, t in truns.items():
+                disk.truns_to_disk(t.download(), os.path.join(path, f"{side}_trun_{L}.dat"))
+            for L, (b, _) in bases.items():
+                disk.basis_to_disk(b, os.path.join(path, f"{side}_basis_{L}.dat"))
+            state["truns"][side] = sorted(truns)
+            state["bases"][side] = sorted(bases)
+        if self.wave is not None:
+            wv, sup = self.wave
+            disk.wave_to_disk(Wavefunction.zeros(sup).set_flat(wv.download()), os.path.join(path, "wave.dat"))
+        with open(os.path.join(path, "state.json"), "w") as f:
+            json.dump(state, f)
+
+    def load(self, path):
+        """Restores a state written by ``save`` (same lattice and parameters)."""
+        with open(os.path.join(path, "state.json")) as f:
+            state = json.load(f)
+        dev, names = self.dev, self._op_names()
+        self.energies = [tuple(e) for e in state["energies"]]
+        self._nrand, self.guess_kind = state["nrand"], state["guess_kind"]
+        for side, models, truns, bases in (("sys", self.sys_models, self.sys_truns, self.sys_bases),
+                                           ("env", self.env_models, self.env_truns, self.env_bases)):
+            models.clear()
+            truns.clear()
+            bases.clear()
+            for L, nleg in state["models"][side].items():
+                tm = disk.model_from_disk(os.path.join(path, f"{side}_model_{L}.dat"), nleg, names)
+                models[int(L)] = GModel(tm.len, DBlock.upload(dev, tm.ham),
+                                        {ii: {nm: DBlock.upload(dev, b) for nm, b in d.items()}
+                                         for ii, d in tm.sub.items()})
+            for L in state["truns"][side]:
+                truns[L] = DBlock.upload(dev, disk.truns_from_disk(os.path.join(path, f"{side}_trun_{L}.dat")))
+            for L in state["bases"][side]:
+                b = disk.basis_from_disk(os.path.join(path, f"{side}_basis_{L}.dat"))
+                bases[L] = (b, DBasis(dev, b))
+        self.wave = None
+        wpath = os.path.join(path, "wave.dat")
+        if os.path.exists(wpath):
+            w = disk.wave_from_disk(wpath)
+            sup = SuperBasis(w.sys_len, w.env_len, [SuperSector(s.sys_num_up, s.sys_num_down, s.env_num_up,
+                                                                s.env_num_down, s.sys_dim, s.env_dim)
+                                                    for s in w.subs])
+            dw = self._new_wave(sup)
+            dw.upload(w.flat())
+            self.wave = (dw, sup)
 
     def run(self, sweeps=2):
         """Get_Ground_State with trun_idx = 1 (code/quantum.f90:179-288)."""

@@ -39,3 +39,20 @@ def test_gpu_dmrg_split_precision(device):
                   precision=_lib.HH_PREC_BF16X3)
     emx = dmx.run(sweeps=1)
     assert abs(emx - e64) / abs(e64) < 1e-8, (emx, e64)
+
+
+def test_checkpoint_resume(device, tmp_path):
+    """save after the half sweeps, load into a fresh driver, sweep both: the
+    resumed run reproduces the uninterrupted one."""
+    lat = SquareLattice(2, 6, U=8.0, phi=0.25)
+    kw = dict(kept_min=32, kept_max=32, trun_err=1e-12, lanzero=1e-10, precision=_lib.HH_PREC_BF16X3)
+    a = GPUDMRG(device, lat, 10, **kw)
+    a.run(sweeps=0)
+    a.save(str(tmp_path / "ckpt"))
+    b = GPUDMRG(device, lat, 10, **kw)
+    b.load(str(tmp_path / "ckpt"))
+    a.sweep()
+    b.sweep()
+    ea = [r[2] for r in a.energies[-2 * (lat.N - 3):]]
+    eb = [r[2] for r in b.energies[-2 * (lat.N - 3):]]
+    np.testing.assert_allclose(eb, ea, rtol=0, atol=1e-12)
