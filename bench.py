@@ -47,7 +47,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample", type=int, default=1, help="matvecs in the CPU baseline sample")
     p.add_argument("--no-sweep", action="store_true", help="skip the sweep-time measurement")
-    p.add_argument("--sweeps", type=int, default=1, help="finite sweeps timed per precision")
+    p.add_argument("--sweep-m", type=int, nargs="+", default=[256, 512],
+                   help="kept multiplets of the sweep measurements (one timed finite sweep per precision)")
     p.add_argument("--energy-check", action="store_true",
                    help="also run Lanczos (100 vectors) in FP64 and in split precision from one start "
                         "vector and report |dE/E| (outside the timed region)")
@@ -191,40 +192,60 @@ def cpu_matvec_timer(wl, psi_flat, nrep):
 
 
 def sweep_bench(dev, args):
-    """Sweep time on the plain-method configuration: Hubbard 2x16 ladder, phi=1/4
-    (Landau gauge), t=1, U=8, N_e=28 (1/8 hole doping), singlet, m=256 kept
-    multiplets; warm-up plus the first two half sweeps, then ``args.sweeps``
-    timed finite sweeps, in FP64 and in split precision with the learned guess
-    corrector, both with Lanczos tol 1e-10 (the split solver iterates on the
-    tensor-core matvec to 1e-8, its noise floor, then restarts with one FP64
-    product).  The corrector trains between sweeps, outside the sweep timer;
-    its training time is reported."""
+    """Sweep time on the plain-method lattice: Hubbard 2x16 ladder, phi = 1/4
+    (Landau gauge), t = 1, U = 8, N_e = 28 (1/8 hole doping), singlet, Lanczos
+    tol 1e-10, at m = 256 (the plain-method configuration) and m = 512 kept
+    multiplets.  For each m the warm-up and the two half sweeps run once (split
+    precision, untimed) and are checkpointed through the reference's on-disk
+    formats; the FP64 arm and the split-precision arm with the learned guess
+    corrector are both restored from that checkpoint and time one finite sweep
+    each.  The split solver iterates on the tensor-core matvec to 1e-8, its
+    noise floor, then restarts with one FP64 product.  The corrector trains
+    between sweeps, outside the sweep timer."""
+    import shutil
+    import tempfile
     from hofstadter_hubbard_tsc_gb300 import _lib
     from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
     from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
-    lat = SquareLattice(2, 16, U=8.0, phi=0.25)
-    out = {"config": "hubbard-ladder-2x16-phi0.25-U8-Ne28-m256", "sweeps_timed": args.sweeps}
     from hofstadter_hubbard_tsc_gb300.guess import LearnedGuess
-    for name, prec, tol in (("fp64", _lib.HH_PREC_FP64, 1e-10), ("split", _lib.HH_PREC_BF16X3, 1e-10)):
-        hook = LearnedGuess(dev, lat.N, 28) if name == "split" else None
-        d = GPUDMRG(dev, lat, 28, kept_min=256, kept_max=256, trun_err=1e-12, lanzero=tol, precision=prec, seed=11,
-                    guess_hook=hook)
+    lat = SquareLattice(2, 16, U=8.0, phi=0.25)
+    nstep = 2 * (lat.N - 3)
+    results = {}
+    for m in args.sweep_m:
+        kw = dict(kept_min=m, kept_max=m, trun_err=1e-12, lanzero=1e-10, seed=11)
+        hook = LearnedGuess(dev, lat.N, 28)
+        prep = GPUDMRG(dev, lat, 28, precision=_lib.HH_PREC_BF16X3, guess_hook=hook, **kw)
         t0 = time.perf_counter()
-        e = d.run(sweeps=args.sweeps)
-        its = [r[3] for r in d.energies[-2 * (lat.N - 3):]]
-        out[name] = {"E0": e, "sweep_s": d.sweep_times, "total_s": time.perf_counter() - t0,
-                     "lanczos_iterations_last_sweep": int(np.sum(its)), "lanzero": tol,
-                     "phase_s_last_sweep": {k: round(v, 4) for k, v in d.phase_s.items()}}
-        if hook is not None:
-            out[name]["learned_guess"] = {
+        prep.run(sweeps=0)
+        prep_s = time.perf_counter() - t0
+        ckpt = tempfile.mkdtemp(prefix="hh_ckpt_")
+        try:
+            prep.save(ckpt)
+            out = {"config": f"hubbard-ladder-2x16-phi0.25-U8-Ne28-m{m}", "prepare_s": round(prep_s, 3),
+                   "start": "warm-up + two half sweeps in split precision, checkpointed and restored by both arms"}
+            for name, prec in (("fp64", _lib.HH_PREC_FP64), ("split", _lib.HH_PREC_BF16X3)):
+                d = GPUDMRG(dev, lat, 28, precision=prec, guess_hook=hook if name == "split" else None, **kw)
+                d.load(ckpt)
+                d.phase_s.clear()
+                t0 = time.perf_counter()
+                d.sweep()
+                dt = time.perf_counter() - t0
+                its = [r[3] for r in d.energies[-nstep:]]
+                out[name] = {"E0": d.energies[-1][2], "sweep_s": dt,
+                             "lanczos_iterations": int(np.sum(its)), "lanzero": 1e-10,
+                             "phase_s": {k: round(v, 4) for k, v in d.phase_s.items()}}
+            out["split"]["learned_guess"] = {
                 "samples": int(len(hook.data()[1])), "train_s": round(hook.train_s, 4),
                 "held_out_hellinger_corrected": hook.val[0] if hook.val else None,
                 "held_out_hellinger_plain": hook.val[1] if hook.val else None,
                 "applied": bool(hook.enabled), "corrected_steps": int(sum(1 for r in hook.log if r[2]))}
+            out["rel_dE"] = abs(out["split"]["E0"] - out["fp64"]["E0"]) / abs(out["fp64"]["E0"])
+            out["sweep_speedup_split_vs_fp64"] = out["fp64"]["sweep_s"] / out["split"]["sweep_s"]
+            results[f"m{m}"] = out
+        finally:
+            shutil.rmtree(ckpt, ignore_errors=True)
             hook.free()
-    out["rel_dE"] = abs(out["split"]["E0"] - out["fp64"]["E0"]) / abs(out["fp64"]["E0"])
-    out["sweep_speedup_split_vs_fp64"] = out["fp64"]["sweep_s"][-1] / out["split"]["sweep_s"][-1]
-    return out
+    return results
 
 
 def run_reference(args, rank, ws, dist):
