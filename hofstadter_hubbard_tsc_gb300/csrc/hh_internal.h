@@ -195,6 +195,7 @@ struct hh_tc_plan {
   hh::tc::Tile* d_tiles1 = nullptr;
   hh::tc::Tile* d_tiles2 = nullptr;
   int n_tiles1 = 0, n_tiles2 = 0, n_cseg = 0;
+  int n_narrow1 = 0, n_narrow2 = 0;  // leading tiles at most 64 wide (64-wide kernels)
   hh::tc::Seg* d_segs = nullptr;
   hh_seg* d_csegs = nullptr;
   int* d_err = nullptr;

@@ -53,7 +53,8 @@ struct IoPtrs {
   double2* out;
 };
 
-size_t tile_smem_bytes();
+// dynamic shared memory of the tile kernels for tiles at most nt (64 or 128) wide
+size_t tile_smem_bytes(int nt);
 
 }  // namespace tc
 
@@ -69,7 +70,8 @@ cudaError_t tc_set_io(tc::IoPtrs* d_io, const double2* in, double2* out, cudaStr
 cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoPtrs* io = nullptr);
 // tile GEMM over ntile tiles: persistent (one CTA per SM, CTA b takes tiles
 // b, b + G, ...: the list must be ordered for balance) or one CTA per tile
+// nt: the list's widest tile (<= 64: the 64-wide kernels, two CTAs per SM)
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s, const tc::IoPtrs* io = nullptr);
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io = nullptr, int nt = 128);
 
 }  // namespace hh

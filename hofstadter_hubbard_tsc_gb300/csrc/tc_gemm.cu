@@ -224,15 +224,16 @@ __device__ __forceinline__ void flag_error(int* err, int code) {
 // uneven tiles run faster this way than under the persistent kernel (0.50
 // against 0.54-0.62 ms on the m = 2000 workload, measured).  Every wait is
 // bounded and reports through *err.
-template <int STAGES>
-__global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* __restrict__ tiles,
+template <int STAGES, int NT>
+__global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kernel(const Tile* __restrict__ tiles,
                                                                   const Seg* __restrict__ segs,
                                                                   double2* __restrict__ base_out, int* err,
                                                                   const IoPtrs* __restrict__ io) {
   if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
   const Tile t = tiles[blockIdx.x];
-  const int stage_bytes = kStageA + 6 * 128 * 32;
+  constexpr int stage_bytes = kStageA + 6 * NT * 32;
+  constexpr uint32_t kCols = 4 * NT;  // main re, im, correction re, im
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   uint64_t* empty = full + STAGES;
   uint64_t* accf = empty + STAGES;
@@ -248,7 +249,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* _
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "n"(kCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* _
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t id_pos = idesc_bf16(t.ntile, false), id_neg = idesc_bf16(t.ntile, true);
-      const uint32_t d_re = tmem, d_im = tmem + 128, c_re = tmem + 256, c_im = tmem + 384;
+      const uint32_t d_re = tmem, d_im = tmem + NT, c_re = tmem + 2 * NT, c_im = tmem + 3 * NT;
       int it = 0;
       uint32_t acc = 0, acc_c = 0;
       bool ok = true;
@@ -348,9 +350,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* _
       float re[16], im[16], cr[16], cm[16];
       if (have) {
         tmem_ld16(lane_base + c0, re);
-        tmem_ld16(lane_base + 128 + c0, im);
-        tmem_ld16(lane_base + 256 + c0, cr);
-        tmem_ld16(lane_base + 384 + c0, cm);
+        tmem_ld16(lane_base + NT + c0, im);
+        tmem_ld16(lane_base + 2 * NT + c0, cr);
+        tmem_ld16(lane_base + 3 * NT + c0, cm);
       } else {
 #pragma unroll
         for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_once_kernel(const Tile* _
   __syncthreads();
   fence_after();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kCols) : "memory");
   }
 }
 
@@ -423,14 +425,15 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // between chunks, so the CTA winds down without another full-length wait per
 // remaining tile.  On the way out the producer waits (bounded) for the copies
 // it issued and the MMA warp for its MMAs (mdone) before TMEM is freed.
-template <int STAGES>
-__global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __restrict__ tiles, int ntile,
+template <int STAGES, int NT>
+__global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(const Tile* __restrict__ tiles, int ntile,
                                                              const Seg* __restrict__ segs,
                                                              double2* __restrict__ base_out, int* err,
                                                              const IoPtrs* __restrict__ io) {
   if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
-  const int stage_bytes = kStageA + 6 * 128 * 32;
+  constexpr int stage_bytes = kStageA + 6 * NT * 32;
+  constexpr uint32_t kCols = 4 * NT;  // main re, im, correction re, im
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   uint64_t* empty = full + STAGES;
   uint64_t* accf = empty + STAGES;
@@ -452,7 +455,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "n"(kCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -502,7 +506,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t d_re = tmem, d_im = tmem + 128, c_re = tmem + 256, c_im = tmem + 384;
+      const uint32_t d_re = tmem, d_im = tmem + NT, c_re = tmem + 2 * NT, c_im = tmem + 3 * NT;
       int it = 0, n = 0;  // n: tiles with MMAs so far
       bool issued = false;
       for (int ti = blockIdx.x; ti < ntile && !*abort_flag; ti += gridDim.x) {
@@ -589,9 +593,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
         float re[16], im[16], cr[16], cm[16];
         if (have) {
           tmem_ld16(lane_base + c0, re);
-          tmem_ld16(lane_base + 128 + c0, im);
-          tmem_ld16(lane_base + 256 + c0, cr);
-          tmem_ld16(lane_base + 384 + c0, cm);
+          tmem_ld16(lane_base + NT + c0, im);
+          tmem_ld16(lane_base + 2 * NT + c0, cr);
+          tmem_ld16(lane_base + 3 * NT + c0, cm);
         } else {
 #pragma unroll
           for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
@@ -649,7 +653,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tile_kernel(const Tile* __rest
   __syncthreads();
   fence_after();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kCols) : "memory");
   }
 }
 
@@ -693,9 +697,13 @@ __global__ void zero_out_kernel(double2* out, long long n, const IoPtrs* __restr
     out[i] = make_double2(0.0, 0.0);
 }
 
-constexpr int kStages = 4;
+constexpr int kStages = 4;     // 128-wide tiles: 4 x 48 KB, one CTA per SM
+constexpr int kStagesN = 3;    // 64-wide tiles: 3 x 36 KB and 256 TMEM columns, two CTAs per SM
 
-size_t tile_smem_bytes() { return (size_t)kStages * (kStageA + 6 * 128 * 32) + 8 * (2 * kStages + 3) + 64; }
+size_t tile_smem_bytes(int nt) {
+  const int st = nt == 64 ? kStagesN : kStages;
+  return (size_t)st * (kStageA + 6 * nt * 32) + 8 * (2 * st + 3) + 64;
+}
 
 }  // namespace tc
 
@@ -729,29 +737,37 @@ cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoP
   return cudaGetLastError();
 }
 
-cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s, const tc::IoPtrs* io) {
-  if (ntile <= 0) return cudaSuccess;
-  const size_t smem = tc::tile_smem_bytes();
+template <int ST, int NT>
+static cudaError_t launch_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out,
+                                int* d_err, bool persistent, cudaStream_t s, const tc::IoPtrs* io) {
+  constexpr int per_sm = NT == 64 ? 2 : 1;  // shared memory and TMEM columns of one SM
+  const size_t smem = tc::tile_smem_bytes(NT);
   static int sms = 0;
   if (!sms) {
-    cudaError_t e = cudaFuncSetAttribute(tc::tc_tile_kernel<tc::kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tc::tc_tile_kernel<ST, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(tc::tc_tile_once_kernel<tc::kStages>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(tc::tc_tile_once_kernel<ST, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem);
     int dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
   }
-  if (persistent && ntile > sms) {
-    // one CTA per SM: shared memory and the 512 TMEM columns allow no second
-    tc::tc_tile_kernel<tc::kStages><<<sms, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io);
-  } else {
-    tc::tc_tile_once_kernel<tc::kStages><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io);
-  }
+  const int resident = per_sm * sms;
+  if (persistent && ntile > resident)
+    tc::tc_tile_kernel<ST, NT><<<resident, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io);
+  else
+    tc::tc_tile_once_kernel<ST, NT><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io);
   return cudaGetLastError();
+}
+
+cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io, int nt) {
+  if (ntile <= 0) return cudaSuccess;
+  if (nt == 64)
+    return launch_tiles<tc::kStagesN, 64>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+  return launch_tiles<tc::kStages, 128>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
 }
 
 }  // namespace hh

@@ -264,30 +264,41 @@ int build_tc_plan(hh_plan* p) {
     }
 
   // ------------------------------------------------------- tile order
-  // Stage 1 (thousands of short tiles) runs on the persistent kernel, where
-  // CTA c of G takes tiles c, c + G, c + 2G, ...  Its tiles go longest first
-  // (MMA chunks x N, plus a fixed epilogue share), in a snake over the CTAs,
-  // so that every CTA receives a near-equal share.  Stage 2 (hundreds of long,
-  // uneven tiles) runs one CTA per tile in plan order, which keeps the tiles
-  // of one output sector together for L2 reuse and lets the hardware balance.
-  {
-    int sms = 148, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const size_t n = tiles1.size();
-    if (n > (size_t)sms) {
-      std::vector<std::pair<double, size_t>> cost(n);
-      for (size_t i = 0; i < n; ++i) cost[i] = {8.0 + tiles1[i].nchunk * (tiles1[i].ntile / 128.0), i};
-      std::stable_sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-      std::vector<tc::Tile> out(n);
-      for (size_t k = 0; k < n; ++k) {
-        const size_t round = k / sms, c = k % sms, base = round * sms;
-        const size_t cnt = std::min((size_t)sms, n - base);  // the last round may be partial
-        out[base + ((round & 1) ? cnt - 1 - c : c)] = tiles1[cost[k].second];
-      }
-      tiles1.swap(out);
+  // Stage 1 (thousands of short tiles) is split into tiles at most 64 wide,
+  // which run on the 64-wide kernels (256 TMEM columns, two CTAs per SM),
+  // followed by the wider ones, both on the persistent kernel, where CTA c of
+  // G resident CTAs takes tiles c, c + G, c + 2G, ...: within each part its
+  // tiles go longest first (MMA chunks x N, plus a fixed epilogue share), in
+  // a snake over the CTAs, so that every CTA receives a near-equal share.
+  // Stage 2 (hundreds of long, uneven tiles) stays one list in plan order on
+  // the 128-wide kernel, which keeps the tiles of one output sector together
+  // for L2 reuse (split like stage 1 it measured 0.55 against 0.50 ms on the
+  // m = 2000 workload).
+  int sms = 148, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  auto split_narrow = [](std::vector<tc::Tile>& tl) {
+    std::stable_partition(tl.begin(), tl.end(), [](const tc::Tile& x) { return x.ntile <= 64; });
+    return (int)std::count_if(tl.begin(), tl.end(), [](const tc::Tile& x) { return x.ntile <= 64; });
+  };
+  auto balance = [](std::vector<tc::Tile>& tl, size_t lo, size_t hi, size_t G) {
+    const size_t n = hi - lo;
+    if (n <= G) return;
+    std::vector<std::pair<double, size_t>> cost(n);
+    for (size_t i = 0; i < n; ++i) cost[i] = {8.0 + tl[lo + i].nchunk * (tl[lo + i].ntile / 128.0), lo + i};
+    std::stable_sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+    std::vector<tc::Tile> out(n);
+    for (size_t k = 0; k < n; ++k) {
+      const size_t round = k / G, c = k % G, base = round * G;
+      const size_t cnt = std::min(G, n - base);  // the last round may be partial
+      out[base + ((round & 1) ? cnt - 1 - c : c)] = tl[cost[k].second];
     }
-  }
+    std::copy(out.begin(), out.end(), tl.begin() + lo);
+  };
+  const int n1n = split_narrow(tiles1);
+  const int n2n = 0;
+  balance(tiles1, 0, n1n, 2 * (size_t)sms);
+  balance(tiles1, n1n, tiles1.size(), (size_t)sms);
 
   // --------------------------------------------------------------- device
   hh_tc_plan& t = p->tc;
@@ -338,6 +349,8 @@ int build_tc_plan(hh_plan* p) {
   t.n_x_tasks = (int)x_tasks.size();
   t.n_tiles1 = (int)tiles1.size();
   t.n_tiles2 = (int)tiles2.size();
+  t.n_narrow1 = n1n;
+  t.n_narrow2 = n2n;
   t.n_cseg = (int)csegs.size();
   t.bytes_op = (double)a_op.size;
   t.bytes_x = (double)a_x.size;
@@ -364,10 +377,16 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
   if (ev) cudaEventRecord(ev[0], s);
   cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io);
   if (ev) cudaEventRecord(ev[1], s);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_tiles1, t.d_segs, out, t.d_err, t.persistent1, s, io);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s, io, 64);
+  if (e == cudaSuccess)
+    e = tc_run_tiles(t.d_tiles1 + t.n_narrow1, t.n_tiles1 - t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s,
+                     io, 128);
   if (ev) cudaEventRecord(ev[2], s);
   if (e == cudaSuccess) e = tc_zero_out(out, p->nelem, s, io);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_tiles2, t.d_segs, out, t.d_err, t.persistent2, s, io);
+  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s, io, 64);
+  if (e == cudaSuccess)
+    e = tc_run_tiles(t.d_tiles2 + t.n_narrow2, t.n_tiles2 - t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s,
+                     io, 128);
   if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, s, io);
   if (ev) cudaEventRecord(ev[3], s);
   return e;
