@@ -33,13 +33,22 @@ METRIC = "matvecs/s & sweep time at fixed m, mixed+learned vs FP64 GPU, |dE/E|<=
 UNIT = "matvecs/s"
 
 
+def _prec_codes():
+    from hofstadter_hubbard_tsc_gb300 import _lib
+    return {"fp64": _lib.HH_PREC_FP64, "bf16x6": _lib.HH_PREC_BF16X6, "bf16x3": _lib.HH_PREC_BF16X3}
+
+
+PREC = _prec_codes()
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x3"])
+    p.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x6", "bf16x3"],
+                   help="bf16x3: two BF16 parts, three products per real product; bf16x6: three parts, six")
     p.add_argument("--m", type=int, default=2000)
     p.add_argument("--W", type=int, default=4)
     p.add_argument("--L", type=int, default=32)
@@ -210,11 +219,12 @@ def sweep_bench(dev, args):
     from hofstadter_hubbard_tsc_gb300.guess import LearnedGuess
     lat = SquareLattice(2, 16, U=8.0, phi=0.25)
     nstep = 2 * (lat.N - 3)
+    split = PREC[args.precision] if args.precision != "fp64" else _lib.HH_PREC_BF16X3
     results = {}
     for m in args.sweep_m:
         kw = dict(kept_min=m, kept_max=m, trun_err=1e-12, lanzero=1e-10, seed=11)
         hook = LearnedGuess(dev, lat.N, 28)
-        prep = GPUDMRG(dev, lat, 28, precision=_lib.HH_PREC_BF16X3, guess_hook=hook, **kw)
+        prep = GPUDMRG(dev, lat, 28, precision=split, guess_hook=hook, **kw)
         t0 = time.perf_counter()
         prep.run(sweeps=0)
         prep_s = time.perf_counter() - t0
@@ -223,7 +233,7 @@ def sweep_bench(dev, args):
             prep.save(ckpt)
             out = {"config": f"hubbard-ladder-2x16-phi0.25-U8-Ne28-m{m}", "prepare_s": round(prep_s, 3),
                    "start": "warm-up + two half sweeps in split precision, checkpointed and restored by both arms"}
-            for name, prec in (("fp64", _lib.HH_PREC_FP64), ("split", _lib.HH_PREC_BF16X3)):
+            for name, prec in (("fp64", _lib.HH_PREC_FP64), ("split", split)):
                 d = GPUDMRG(dev, lat, 28, precision=prec, guess_hook=hook if name == "split" else None, **kw)
                 d.load(ckpt)
                 d.phase_s.clear()
@@ -292,7 +302,7 @@ def main():
     from hofstadter_hubbard_tsc_gb300.superblock import Superblock
     from hofstadter_hubbard_tsc_gb300.synth import Workload
 
-    prec = _lib.HH_PREC_FP64 if args.precision == "fp64" else _lib.HH_PREC_BF16X3
+    prec = PREC[args.precision]
     t0 = time.perf_counter()
     wl = Workload(W=args.W, L=args.L, n_elec=args.ne, m=args.m)
     dev = Device(local)
@@ -398,8 +408,9 @@ def main():
         peak = fp64_peak_tflops()
         peak_note = "dense FP64 (cuBLAS DGEMM 4096^3, best of 5, measured in this run): GB300 has no FP64 tensor path"
     else:
-        peak = peaks["bf16_tflops"] / 6.0
-        peak_note = "measured bf16 burst / 6 (three-way split: six bf16 products per real product)"
+        nprod = 6 if prec == _lib.HH_PREC_BF16X6 else 3
+        peak = peaks["bf16_tflops"] / nprod
+        peak_note = (f"measured bf16 burst / {nprod} ({args.precision}: {nprod} bf16 products per real product)")
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if peak else None, "traffic": None,
                 "kernel": (f"seg_gemm_fp64 stage {stage}" if prec == _lib.HH_PREC_FP64
@@ -408,14 +419,14 @@ def main():
                 "algorithmic_flops_per_launch": flops_stage,
                 "kernel_ms_per_launch": t_stage * 1e3}
     if prec != _lib.HH_PREC_FP64:
-        issued = counts[12] if stage == 1 else counts[13]
+        issued = (counts[12] if stage == 1 else counts[13]) * (1.0 if prec == _lib.HH_PREC_BF16X6 else 0.5)
         roofline["bf16_flops_issued_per_launch"] = issued
         roofline["tensor_pipe_frac_of_measured_bf16"] = issued / t_stage / 1e12 / peaks["bf16_tflops"]
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128" if prec == _lib.HH_PREC_FP64 else "bf16x3(c128 io)",
+            "dtype": "c128" if prec == _lib.HH_PREC_FP64 else f"{args.precision}(c128 io)",
             "data": "synthetic",
             "config": dict(wl.describe(), **{"precision": args.precision, "l2": "flushed between steps (256 MB write)",
                                              "parallelism": f"replicas x{ws}",

@@ -12,7 +12,8 @@ LIB_PATH = os.path.join(HERE, "libhh_dmrg.so")
 
 HH_OK = 0
 HH_PREC_FP64 = 0
-HH_PREC_BF16X3 = 1
+HH_PREC_BF16X6 = 1  # three BF16 parts, six products: ~2^-24 per product
+HH_PREC_BF16X3 = 2  # two BF16 parts, three products: ~2^-16 per product
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
           -4: "quantum number mismatch", -5: "bounded device wait timed out",
@@ -89,7 +90,7 @@ SIGNATURES = {
     "hh_plan_check": (I, [P]),
     "hh_matvec_timed": (I, [P, P, P, I, C.POINTER(C.c_float)]),
     "hh_matvec_noalloc": (I, [P, P, P]),
-    "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP]),
+    "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP, I]),
     "hh_density_truncate": (I, [P, P, I, I, I, D, PP, IP, DP, DP, DP]),
     "hh_enlarge_operator": (I, [P, I, P, P, I, I, PP]),
     "hh_ham_add_bond": (I, [P, P, P, P, I, P, DP, I, I]),

@@ -716,15 +716,10 @@ int hh_plan_free(hh_plan_t* p) {
   return HH_OK;
 }
 
-static int matvec_timed_tc(hh_plan* p, const double2* in, double2* out, int precision, float* ms) {
-  return matvec_tc(p, in, out, ms);
-}
-
 static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision, bool check = true) {
   hh_ctx* ctx = p->ctx;
-  if (precision != HH_PREC_FP64 && precision != HH_PREC_BF16X3)
-    return fail(ctx, HH_ERR_INVALID, "unknown precision");
-  if (precision == HH_PREC_BF16X3) return matvec_tc(p, in, out, nullptr, check);
+  if (precision != HH_PREC_FP64 && !split_of(precision)) return fail(ctx, HH_ERR_INVALID, "unknown precision");
+  if (precision != HH_PREC_FP64) return matvec_tc(p, in, out, nullptr, check, split_of(precision));
   cudaError_t e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
   if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
   if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
@@ -760,7 +755,10 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
   if (!p || !in || !out || !ms || in == out || in->nelem != p->nelem || out->nelem != p->nelem)
     return HH_ERR_INVALID;
   hh_ctx* ctx = p->ctx;
-  if (precision != HH_PREC_FP64) return matvec_timed_tc(p, in->d, out->d, precision, ms);
+  if (precision != HH_PREC_FP64) {
+    if (!split_of(precision)) return fail(ctx, HH_ERR_INVALID, "unknown precision");
+    return matvec_tc(p, in->d, out->d, ms, true, split_of(precision));
+  }
   cudaEvent_t ev[3];
   for (int i = 0; i < 3; ++i) cudaEventCreate(&ev[i]);
   cudaError_t e = cudaMemsetAsync(out->d, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
@@ -810,8 +808,8 @@ int hh_plan_tune(hh_plan_t* p, int precision, int reps, double* ms, int* choice)
     if (choice) *choice = 0;
     return HH_OK;
   }
-  if (precision != HH_PREC_BF16X3) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
-  int st = tune_tc_plan(p, reps, ms);
+  if (!split_of(precision)) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
+  int st = tune_tc_plan(p, reps, ms, split_of(precision));
   if (st == HH_OK && choice) *choice = 2 * (int)p->tc.persistent1 + (int)p->tc.persistent2;
   return st;
 }
@@ -837,7 +835,7 @@ int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int prec
   if (!p || !psi || !energy || psi->nelem != p->nelem || maxit < 1) return HH_ERR_INVALID;
   if (precision == HH_PREC_FP64)
     return lanczos_core(p, psi, lanzero, maxit, precision, precision, energy, iterations);
-  if (precision != HH_PREC_BF16X3) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
+  if (!split_of(precision)) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
   // Split precision, two passes.  (1) Lanczos on the tensor-core matvec down
   // to its noise floor: Ritz value change <= max(lanzero, 1e-8).  (2) Lanczos
   // restarted from that vector psi_m whose first product H psi_m is FP64 and
@@ -888,7 +886,7 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
   double* d_vv = d_beta + 128;
   double* d_w2 = d_vv + 128;
   double* d_part = d_w2 + 8;
-  const bool uses_tc = precision == HH_PREC_BF16X3 || first_precision == HH_PREC_BF16X3;
+  const bool uses_tc = split_of(precision) || split_of(first_precision);
   double2* V = p->d_krylov;
   cudaStream_t s = ctx->stream;
   auto slot = [&](int j) { return V + (size_t)j * n; };

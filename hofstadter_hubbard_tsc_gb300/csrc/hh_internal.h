@@ -205,6 +205,7 @@ struct hh_tc_plan {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int calls = 0;
+  int graph_split = 0;  // BF16 parts per operand of the captured graph
   // launch choices (hh_plan_tune): stage 1 / stage 2 on the persistent kernel
   bool persistent1 = true, persistent2 = false;
   double bytes_op = 0, bytes_x = 0, bytes_t = 0;
@@ -266,8 +267,13 @@ int build_tc_plan(hh_plan* plan);
 void release_tc_plan(hh_plan* plan);
 // check = false: queue only; a bounded wait that ran out is left in the
 // plan's error flag (p->tc.d_err) for the caller to read
-int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check = true);
-int tune_tc_plan(hh_plan* p, int reps, double* ms);
+// split: BF16 parts per operand (3: BF16x6, 2: BF16x3)
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check = true, int split = 3);
+int tune_tc_plan(hh_plan* p, int reps, double* ms, int split);
+// BF16 parts per operand of a split precision, 0 for FP64 or an unknown code
+inline int split_of(int precision) {
+  return precision == HH_PREC_BF16X6 ? 3 : precision == HH_PREC_BF16X3 ? 2 : 0;
+}
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
 int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
 // Eigenvalues (ascending, into *d_w: sector k's at the sum of the earlier

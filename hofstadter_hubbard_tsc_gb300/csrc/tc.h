@@ -53,14 +53,16 @@ struct IoPtrs {
   double2* out;
 };
 
-// dynamic shared memory of the tile kernels for tiles at most nt (64 or 128) wide
-size_t tile_smem_bytes(int nt);
+// dynamic shared memory of the tile kernels for tiles at most nt (64 or 128)
+// wide using split (2 or 3) BF16 parts per operand
+size_t tile_smem_bytes(int nt, int split);
 
 }  // namespace tc
 
-// fp32: scale and split in FP32 (wave images) instead of FP64 (operator images)
+// fp32: scale and split in FP32 (wave images, the first `split` parts)
+// instead of FP64 (operator images, all three parts)
 cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
-                            cudaStream_t s, const tc::IoPtrs* io = nullptr);
+                            cudaStream_t s, const tc::IoPtrs* io = nullptr, int split = 3);
 // adds the FP64 copy terms of the stage-2 tiles to their output rectangles
 cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
                           double2* base_out, cudaStream_t s, const tc::IoPtrs* io = nullptr);
@@ -70,8 +72,10 @@ cudaError_t tc_set_io(tc::IoPtrs* d_io, const double2* in, double2* out, cudaStr
 cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoPtrs* io = nullptr);
 // tile GEMM over ntile tiles: persistent (one CTA per SM, CTA b takes tiles
 // b, b + G, ...: the list must be ordered for balance) or one CTA per tile
-// nt: the list's widest tile (<= 64: the 64-wide kernels, two CTAs per SM)
+// nt: the list's widest tile (<= 64: the 64-wide kernels, two CTAs per SM);
+// split: BF16 parts per operand, 3 (six products) or 2 (three products)
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s, const tc::IoPtrs* io = nullptr, int nt = 128);
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io = nullptr, int nt = 128,
+                         int split = 3);
 
 }  // namespace hh

@@ -2,15 +2,20 @@
 //
 // Every complex FP64 operand is carried as six BF16 planes: re0 re1 re2 im0
 // im1 im2 with x = x0 + x1 + x2 (x0 = bf16(x), x1 = bf16(x - x0), ...), i.e.
-// 24 significand bits.  A complex tile product keeps the six split products
-// with i + j <= 2 for each of the four real products (re.re, im.im, re.im,
-// im.re): 24 tcgen05.mma (M=128, K=16, FP32 accumulate in TMEM) per 16 complex
-// k.  The dropped products are below 2^-24 relative.  The tensor core rounds
+// 24 significand bits.  The kernels use the first SPLIT parts of each:
+//   SPLIT = 3 (BF16x6): the six split products with i + j <= 2 for each of
+//     the four real products (re.re, im.im, re.im, im.re), 24 tcgen05.mma
+//     (M=128, K=16, FP32 accumulate in TMEM) per 16 complex k; the dropped
+//     products are below 2^-24 relative;
+//   SPLIT = 2 (BF16x3): x0 y0 + x0 y1 + x1 y0, 12 MMAs per 16 complex k and
+//     two thirds of the operand bytes; dropped terms about 2^-16 relative.
+// Both read the same images (planes re0 re1 im0 im1 of the six).  The tensor core rounds
 // every accumulation toward zero, so the leading products x0 y0 and the five
 // correction products go to separate accumulators (main: TMEM columns
-// [0,256), correction: [256,512), re then im): the correction terms, 2^-8 of
+// [0,2NT), correction: [2NT,4NT), re then im): the correction terms, 2^-8 of
 // the main ones, then cost no accumulator precision, and the bias of the main
-// accumulator grows with 2 instead of 12 accumulations per 16 complex k.  The
+// accumulator grows with 2 instead of 4 (SPLIT 2) or 12 (SPLIT 3)
+// accumulations per 16 complex k.  The
 // epilogue adds the two in FP64.  The -im.im product uses the negate-A bit of
 // the instruction descriptor.
 //
@@ -146,6 +151,10 @@ __device__ __forceinline__ uint4 pack8(const __nv_bfloat16* v) {
   return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
+// image plane holding shared-memory plane p when SPLIT parts are used: the
+// SPLIT re parts, then the SPLIT im parts (image planes 3, 4, ...)
+__host__ __device__ constexpr int img_plane(int p, int split) { return p < split ? p : 3 + p - split; }
+
 __device__ __forceinline__ size_t img_off(int r8, int r, int k) {
   // byte offset of the 16-byte row chunk (row r, k rounded down to 8) in a plane-0 image
   return ((size_t)((k >> 4) * 6) * (r8 >> 3) + (r >> 3)) * 256 + ((k >> 3) & 1) * 128 + (r & 7) * 16;
@@ -153,11 +162,12 @@ __device__ __forceinline__ size_t img_off(int r8, int r, int k) {
 
 // ------------------------------------------------------------------ image build
 // One CTA per task: value(r,k) = coef * (conj?) src[trans ? k + r*ld : r + k*ld]
-// for r < rows, k < kc, zero in the padding; written as six BF16 planes.
-// The value is rounded to FP32 first and scaled and split in FP32: three BF16
-// parts hold FP32's 24 significand bits, and GB300 retires FP32 at 64 times
-// its FP64 rate.  Operator images (built once per plan) keep the FP64 split.
-template <bool kFp32>
+// for r < rows, k < kc, zero in the padding; the first SPLIT BF16 parts of
+// re and im are written (planes p and 3 + p).  The value is rounded to FP32
+// first and scaled and split in FP32: three BF16 parts hold FP32's 24
+// significand bits, and GB300 retires FP32 at 64 times its FP64 rate.
+// Operator images (built once per plan, all three parts) keep the FP64 split.
+template <bool kFp32, int SPLIT>
 __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __restrict__ tasks,
                                                            const double2* __restrict__ base_in,
                                                            const IoPtrs* __restrict__ io) {
@@ -202,7 +212,7 @@ __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __rest
     }
     const size_t o = img_off(r8, r, k0);
 #pragma unroll
-    for (int p = 0; p < 3; ++p) {
+    for (int p = 0; p < SPLIT; ++p) {
       *reinterpret_cast<uint4*>(dst + o + (size_t)p * plane) = pack8(re[p]);
       *reinterpret_cast<uint4*>(dst + o + (size_t)(p + 3) * plane) = pack8(im[p]);
     }
@@ -211,11 +221,107 @@ __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __rest
 
 // ------------------------------------------------------------------ tile GEMM
 constexpr int kPlaneA = 128 * 32;            // 128 rows x 16 bf16
-constexpr int kStageA = 6 * kPlaneA;         // 24 KB
 constexpr int kThreads = 192;                // producer, MMA, 4 epilogue warps
+
+// one pipeline stage: 2*SPLIT planes of A (128 rows) and of B (NT rows)
+__host__ __device__ constexpr int stage_bytes_of(int nt, int split) { return 2 * split * (kPlaneA + nt * 32); }
 
 __device__ __forceinline__ void flag_error(int* err, int code) {
   if (err) atomicCAS(err, 0, code);
+}
+
+// Copies of chunk kc of segment sg into one stage (A planes from sa, B planes
+// after them), completing on bar.
+template <int SPLIT>
+__device__ __forceinline__ void load_chunk(uint8_t* sa, int ntile, const Seg& sg, int kc, uint64_t* bar) {
+  uint8_t* sb = sa + 2 * SPLIT * kPlaneA;
+  mbar_expect_tx(bar, 2u * SPLIT * (sg.a_bytes + sg.b_bytes));
+  const uint8_t* ga = reinterpret_cast<const uint8_t*>(sg.a) + (size_t)kc * 6 * sg.a_plane;
+  const uint8_t* gb = reinterpret_cast<const uint8_t*>(sg.b) + (size_t)kc * 6 * sg.b_plane;
+#pragma unroll
+  for (int p = 0; p < 2 * SPLIT; ++p) {
+    const int ip = img_plane(p, SPLIT);
+    bulk_g2s(sa + p * kPlaneA, ga + (size_t)ip * sg.a_plane, sg.a_bytes, bar);
+    bulk_g2s(sb + p * (ntile * 32), gb + (size_t)ip * sg.b_plane, sg.b_bytes, bar);
+  }
+}
+
+// The split products of one staged chunk: parts i + j < SPLIT of the four
+// real products; x0 y0 into the main accumulators (columns [0, 2NT)), the
+// others into the correction accumulators ([2NT, 4NT)).  acc / acc_c: 0 for
+// the first chunk of a tile (overwrite), then 1.
+template <int SPLIT, int NT>
+__device__ __forceinline__ void mma_chunk(uint32_t sa, int ntile, uint32_t tmem, uint32_t id_pos, uint32_t id_neg,
+                                          uint32_t& acc, uint32_t& acc_c) {
+  const uint32_t sb = sa + 2 * SPLIT * kPlaneA;
+  const uint32_t d_re = tmem, d_im = tmem + NT, c_re = tmem + 2 * NT, c_im = tmem + 3 * NT;
+#pragma unroll
+  for (int i = 0; i < SPLIT; ++i) {
+#pragma unroll
+    for (int j = 0; j < SPLIT - i; ++j) {
+      const uint64_t are = smem_desc(sa + i * kPlaneA), aim = smem_desc(sa + (SPLIT + i) * kPlaneA);
+      const uint64_t bre = smem_desc(sb + j * ntile * 32), bim = smem_desc(sb + (SPLIT + j) * ntile * 32);
+      if (i + j == 0) {
+        mma_bf16(d_re, are, bre, id_pos, acc);
+        mma_bf16(d_re, aim, bim, id_neg, 1u);
+        mma_bf16(d_im, are, bim, id_pos, acc);
+        mma_bf16(d_im, aim, bre, id_pos, 1u);
+        acc = 1u;
+      } else {
+        mma_bf16(c_re, are, bre, id_pos, acc_c);
+        mma_bf16(c_re, aim, bim, id_neg, 1u);
+        mma_bf16(c_im, are, bim, id_pos, acc_c);
+        mma_bf16(c_im, aim, bre, id_pos, 1u);
+        acc_c = 1u;
+      }
+    }
+  }
+}
+
+// Epilogue of accumulator columns [c0, c0 + 16) for one row of the tile:
+// main + correction summed in FP32 (one rounding at 2^-24), then either
+// stored to the output wave (mode 0; the FP64 copy terms follow in
+// copy_terms_kernel) or split into the T image (mode 1: rows of T, k = T
+// columns, zero outside the valid rectangle, the SPLIT parts the next stage
+// reads).
+template <int SPLIT>
+__device__ __forceinline__ void epilogue16(const Tile& t, int row, int c0, const float* re, const float* im,
+                                           const float* cr, const float* cm, double2* base_out) {
+  if (t.mode == 0) {
+    if (row < t.mrem) {
+      double2* O = base_out + t.out;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int col = c0 + j;
+        if (col < t.nrem) O[(long long)row + (long long)col * t.ldo] = make_double2(re[j] + cr[j], im[j] + cm[j]);
+      }
+    }
+    return;
+  }
+  const int r = t.m0 + row;
+  if (r >= t.t_r8) return;
+  uint8_t* img = reinterpret_cast<uint8_t*>(t.out);
+  const size_t plane = (size_t)(t.t_r8 >> 3) * 256;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    __nv_bfloat16 pr[3][8], pi[3][8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int cc = c0 + h * 8 + j;
+      const bool valid = row < t.mrem && cc < t.nrem;
+      __nv_bfloat16 s3[3];
+      split3f(valid ? re[h * 8 + j] + cr[h * 8 + j] : 0.f, s3);
+      pr[0][j] = s3[0]; pr[1][j] = s3[1]; pr[2][j] = s3[2];
+      split3f(valid ? im[h * 8 + j] + cm[h * 8 + j] : 0.f, s3);
+      pi[0][j] = s3[0]; pi[1][j] = s3[1]; pi[2][j] = s3[2];
+    }
+    const size_t o = img_off(t.t_r8, r, t.n0 + c0 + h * 8);
+#pragma unroll
+    for (int p = 0; p < SPLIT; ++p) {
+      *reinterpret_cast<uint4*>(img + o + (size_t)p * plane) = pack8(pr[p]);
+      *reinterpret_cast<uint4*>(img + o + (size_t)(p + 3) * plane) = pack8(pi[p]);
+    }
+  }
 }
 
 // One CTA per tile (grid = number of tiles; the hardware hands tiles to SMs
@@ -224,7 +330,7 @@ __device__ __forceinline__ void flag_error(int* err, int code) {
 // uneven tiles run faster this way than under the persistent kernel (0.50
 // against 0.54-0.62 ms on the m = 2000 workload, measured).  Every wait is
 // bounded and reports through *err.
-template <int STAGES, int NT>
+template <int STAGES, int NT, int SPLIT>
 __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kernel(const Tile* __restrict__ tiles,
                                                                   const Seg* __restrict__ segs,
                                                                   double2* __restrict__ base_out, int* err,
@@ -232,7 +338,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
   if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
   const Tile t = tiles[blockIdx.x];
-  constexpr int stage_bytes = kStageA + 6 * NT * 32;
+  constexpr int stage_bytes = stage_bytes_of(NT, SPLIT);
   constexpr uint32_t kCols = 4 * NT;  // main re, im, correction re, im
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   uint64_t* empty = full + STAGES;
@@ -272,23 +378,13 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
             ok = false;
             break;
           }
-          uint8_t* sa = smem + s * stage_bytes;
-          uint8_t* sb = sa + kStageA;
-          mbar_expect_tx(&full[s], 6u * (sg.a_bytes + sg.b_bytes));
-          const uint8_t* ga = reinterpret_cast<const uint8_t*>(sg.a) + (size_t)kc * 6 * sg.a_plane;
-          const uint8_t* gb = reinterpret_cast<const uint8_t*>(sg.b) + (size_t)kc * 6 * sg.b_plane;
-#pragma unroll
-          for (int p = 0; p < 6; ++p) {
-            bulk_g2s(sa + p * kPlaneA, ga + (size_t)p * sg.a_plane, sg.a_bytes, &full[s]);
-            bulk_g2s(sb + p * (t.ntile * 32), gb + (size_t)p * sg.b_plane, sg.b_bytes, &full[s]);
-          }
+          load_chunk<SPLIT>(smem + s * stage_bytes, t.ntile, sg, kc, &full[s]);
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t id_pos = idesc_bf16(t.ntile, false), id_neg = idesc_bf16(t.ntile, true);
-      const uint32_t d_re = tmem, d_im = tmem + NT, c_re = tmem + 2 * NT, c_im = tmem + 3 * NT;
       int it = 0;
       uint32_t acc = 0, acc_c = 0;
       bool ok = true;
@@ -302,29 +398,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
             break;
           }
           fence_after();
-          const uint32_t sa = smem_u32(smem + s * stage_bytes);
-          const uint32_t sb = sa + kStageA;
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-#pragma unroll
-            for (int j = 0; j < 3 - i; ++j) {
-              const uint64_t are = smem_desc(sa + i * kPlaneA), aim = smem_desc(sa + (3 + i) * kPlaneA);
-              const uint64_t bre = smem_desc(sb + j * t.ntile * 32), bim = smem_desc(sb + (3 + j) * t.ntile * 32);
-              if (i + j == 0) {
-                mma_bf16(d_re, are, bre, id_pos, acc);
-                mma_bf16(d_re, aim, bim, id_neg, 1u);
-                mma_bf16(d_im, are, bim, id_pos, acc);
-                mma_bf16(d_im, aim, bre, id_pos, 1u);
-                acc = 1u;
-              } else {
-                mma_bf16(c_re, are, bre, id_pos, acc_c);
-                mma_bf16(c_re, aim, bim, id_neg, 1u);
-                mma_bf16(c_im, are, bim, id_pos, acc_c);
-                mma_bf16(c_im, aim, bre, id_pos, 1u);
-                acc_c = 1u;
-              }
-            }
-          }
+          mma_chunk<SPLIT, NT>(smem_u32(smem + s * stage_bytes), t.ntile, tmem, id_pos, id_neg, acc, acc_c);
           mma_commit(&empty[s]);
         }
       }
@@ -357,45 +431,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
 #pragma unroll
         for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
       }
-      if (t.mode == 0) {
-        // main + correction in FP32 (one rounding at 2^-24), one conversion;
-        // the FP64 copy terms follow in copy_terms_kernel
-        if (row < t.mrem) {
-          double2* O = base_out + t.out;
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int col = c0 + j;
-            if (col < t.nrem) O[(long long)row + (long long)col * t.ldo] = make_double2(re[j] + cr[j], im[j] + cm[j]);
-          }
-        }
-      } else {
-        // T image: rows of T, k = T columns; zero outside the valid rectangle
-        const int r = t.m0 + row;
-        if (r < t.t_r8) {
-          uint8_t* img = reinterpret_cast<uint8_t*>(t.out);
-          const size_t plane = (size_t)(t.t_r8 >> 3) * 256;
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            __nv_bfloat16 pr[3][8], pi[3][8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int cc = c0 + h * 8 + j;
-              const bool valid = row < t.mrem && cc < t.nrem;
-              __nv_bfloat16 s[3];
-              split3f(valid ? re[h * 8 + j] + cr[h * 8 + j] : 0.f, s);
-              pr[0][j] = s[0]; pr[1][j] = s[1]; pr[2][j] = s[2];
-              split3f(valid ? im[h * 8 + j] + cm[h * 8 + j] : 0.f, s);
-              pi[0][j] = s[0]; pi[1][j] = s[1]; pi[2][j] = s[2];
-            }
-            const size_t o = img_off(t.t_r8, r, t.n0 + c0 + h * 8);
-#pragma unroll
-            for (int p = 0; p < 3; ++p) {
-              *reinterpret_cast<uint4*>(img + o + (size_t)p * plane) = pack8(pr[p]);
-              *reinterpret_cast<uint4*>(img + o + (size_t)(p + 3) * plane) = pack8(pi[p]);
-            }
-          }
-        }
-      }
+      epilogue16<SPLIT>(t, row, c0, re, im, cr, cm, base_out);
     }
   }
   fence_before();
@@ -425,14 +461,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // between chunks, so the CTA winds down without another full-length wait per
 // remaining tile.  On the way out the producer waits (bounded) for the copies
 // it issued and the MMA warp for its MMAs (mdone) before TMEM is freed.
-template <int STAGES, int NT>
+template <int STAGES, int NT, int SPLIT>
 __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(const Tile* __restrict__ tiles, int ntile,
                                                              const Seg* __restrict__ segs,
                                                              double2* __restrict__ base_out, int* err,
                                                              const IoPtrs* __restrict__ io) {
   if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr int stage_bytes = kStageA + 6 * NT * 32;
+  constexpr int stage_bytes = stage_bytes_of(NT, SPLIT);
   constexpr uint32_t kCols = 4 * NT;  // main re, im, correction re, im
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
   uint64_t* empty = full + STAGES;
@@ -486,16 +522,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
               give_up(1);
               break;
             }
-            uint8_t* sa = smem + s * stage_bytes;
-            uint8_t* sb = sa + kStageA;
-            mbar_expect_tx(&full[s], 6u * (sg.a_bytes + sg.b_bytes));
-            const uint8_t* ga = reinterpret_cast<const uint8_t*>(sg.a) + (size_t)kc * 6 * sg.a_plane;
-            const uint8_t* gb = reinterpret_cast<const uint8_t*>(sg.b) + (size_t)kc * 6 * sg.b_plane;
-#pragma unroll
-            for (int p = 0; p < 6; ++p) {
-              bulk_g2s(sa + p * kPlaneA, ga + (size_t)p * sg.a_plane, sg.a_bytes, &full[s]);
-              bulk_g2s(sb + p * (t.ntile * 32), gb + (size_t)p * sg.b_plane, sg.b_bytes, &full[s]);
-            }
+            load_chunk<SPLIT>(smem + s * stage_bytes, t.ntile, sg, kc, &full[s]);
           }
         }
       }
@@ -506,7 +533,6 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t d_re = tmem, d_im = tmem + NT, c_re = tmem + 2 * NT, c_im = tmem + 3 * NT;
       int it = 0, n = 0;  // n: tiles with MMAs so far
       bool issued = false;
       for (int ti = blockIdx.x; ti < ntile && !*abort_flag; ti += gridDim.x) {
@@ -534,29 +560,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
               break;
             }
             fence_after();
-            const uint32_t sa = smem_u32(smem + s * stage_bytes);
-            const uint32_t sb = sa + kStageA;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-#pragma unroll
-              for (int j = 0; j < 3 - i; ++j) {
-                const uint64_t are = smem_desc(sa + i * kPlaneA), aim = smem_desc(sa + (3 + i) * kPlaneA);
-                const uint64_t bre = smem_desc(sb + j * t.ntile * 32), bim = smem_desc(sb + (3 + j) * t.ntile * 32);
-                if (i + j == 0) {
-                  mma_bf16(d_re, are, bre, id_pos, acc);
-                  mma_bf16(d_re, aim, bim, id_neg, 1u);
-                  mma_bf16(d_im, are, bim, id_pos, acc);
-                  mma_bf16(d_im, aim, bre, id_pos, 1u);
-                  acc = 1u;
-                } else {
-                  mma_bf16(c_re, are, bre, id_pos, acc_c);
-                  mma_bf16(c_re, aim, bim, id_neg, 1u);
-                  mma_bf16(c_im, are, bim, id_pos, acc_c);
-                  mma_bf16(c_im, aim, bre, id_pos, 1u);
-                  acc_c = 1u;
-                }
-              }
-            }
+            mma_chunk<SPLIT, NT>(smem_u32(smem + s * stage_bytes), t.ntile, tmem, id_pos, id_neg, acc, acc_c);
             mma_commit(&empty[s]);
             issued = true;
           }
@@ -600,46 +604,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
 #pragma unroll
           for (int j = 0; j < 16; ++j) re[j] = im[j] = cr[j] = cm[j] = 0.f;
         }
-        if (t.mode == 0) {
-          // main + correction in FP32 (one rounding at 2^-24), one conversion;
-          // the FP64 copy terms follow in copy_terms_kernel
-          if (row < t.mrem) {
-            double2* O = base_out + t.out;
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int col = c0 + j;
-              if (col < t.nrem)
-                O[(long long)row + (long long)col * t.ldo] = make_double2(re[j] + cr[j], im[j] + cm[j]);
-            }
-          }
-        } else {
-          // T image: rows of T, k = T columns; zero outside the valid rectangle
-          const int r = t.m0 + row;
-          if (r < t.t_r8) {
-            uint8_t* img = reinterpret_cast<uint8_t*>(t.out);
-            const size_t plane = (size_t)(t.t_r8 >> 3) * 256;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              __nv_bfloat16 pr[3][8], pi[3][8];
-#pragma unroll
-              for (int j = 0; j < 8; ++j) {
-                const int cc = c0 + h * 8 + j;
-                const bool valid = row < t.mrem && cc < t.nrem;
-                __nv_bfloat16 s3[3];
-                split3f(valid ? re[h * 8 + j] + cr[h * 8 + j] : 0.f, s3);
-                pr[0][j] = s3[0]; pr[1][j] = s3[1]; pr[2][j] = s3[2];
-                split3f(valid ? im[h * 8 + j] + cm[h * 8 + j] : 0.f, s3);
-                pi[0][j] = s3[0]; pi[1][j] = s3[1]; pi[2][j] = s3[2];
-              }
-              const size_t o = img_off(t.t_r8, r, t.n0 + c0 + h * 8);
-#pragma unroll
-              for (int p = 0; p < 3; ++p) {
-                *reinterpret_cast<uint4*>(img + o + (size_t)p * plane) = pack8(pr[p]);
-                *reinterpret_cast<uint4*>(img + o + (size_t)(p + 3) * plane) = pack8(pi[p]);
-              }
-            }
-          }
-        }
+        epilogue16<SPLIT>(t, row, c0, re, im, cr, cm, base_out);
       }
       // accumulators read: release them to the MMA warp
       if (mmas) {
@@ -697,23 +662,29 @@ __global__ void zero_out_kernel(double2* out, long long n, const IoPtrs* __restr
     out[i] = make_double2(0.0, 0.0);
 }
 
-constexpr int kStages = 4;     // 128-wide tiles: 4 x 48 KB, one CTA per SM
-constexpr int kStagesN = 3;    // 64-wide tiles: 3 x 36 KB and 256 TMEM columns, two CTAs per SM
+// Pipeline depth: 128-wide tiles (one CTA per SM) fill 192 KB of shared
+// memory, 4 x 48 KB (SPLIT 3) or 6 x 32 KB (SPLIT 2); 64-wide tiles (256 TMEM
+// columns, two CTAs per SM) about 100 KB each, 3 x 36 KB or 4 x 24 KB.
+__host__ __device__ constexpr int stages_of(int nt, int split) {
+  return nt == 64 ? (split == 3 ? 3 : 4) : (split == 3 ? 4 : 6);
+}
 
-size_t tile_smem_bytes(int nt) {
-  const int st = nt == 64 ? kStagesN : kStages;
-  return (size_t)st * (kStageA + 6 * nt * 32) + 8 * (2 * st + 3) + 64;
+size_t tile_smem_bytes(int nt, int split) {
+  const int st = stages_of(nt, split);
+  return (size_t)st * stage_bytes_of(nt, split) + 8 * (2 * st + 3) + 64;
 }
 
 }  // namespace tc
 
 cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
-                            cudaStream_t s, const tc::IoPtrs* io) {
+                            cudaStream_t s, const tc::IoPtrs* io, int split) {
   if (ntask <= 0) return cudaSuccess;
-  if (fp32)
-    tc::build_images_kernel<true><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
+  if (!fp32)
+    tc::build_images_kernel<false, 3><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
+  else if (split == 2)
+    tc::build_images_kernel<true, 2><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
   else
-    tc::build_images_kernel<false><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
+    tc::build_images_kernel<true, 3><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
   return cudaGetLastError();
 }
 
@@ -737,17 +708,18 @@ cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoP
   return cudaGetLastError();
 }
 
-template <int ST, int NT>
+template <int NT, int SPLIT>
 static cudaError_t launch_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out,
                                 int* d_err, bool persistent, cudaStream_t s, const tc::IoPtrs* io) {
+  constexpr int ST = tc::stages_of(NT, SPLIT);
   constexpr int per_sm = NT == 64 ? 2 : 1;  // shared memory and TMEM columns of one SM
-  const size_t smem = tc::tile_smem_bytes(NT);
+  const size_t smem = tc::tile_smem_bytes(NT, SPLIT);
   static int sms = 0;
   if (!sms) {
-    cudaError_t e = cudaFuncSetAttribute(tc::tc_tile_kernel<ST, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(tc::tc_tile_kernel<ST, NT, SPLIT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(tc::tc_tile_once_kernel<ST, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      e = cudaFuncSetAttribute(tc::tc_tile_once_kernel<ST, NT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem);
     int dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
@@ -756,18 +728,22 @@ static cudaError_t launch_tiles(const tc::Tile* d_tiles, int ntile, const tc::Se
   }
   const int resident = per_sm * sms;
   if (persistent && ntile > resident)
-    tc::tc_tile_kernel<ST, NT><<<resident, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io);
+    tc::tc_tile_kernel<ST, NT, SPLIT>
+        <<<resident, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io);
   else
-    tc::tc_tile_once_kernel<ST, NT><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io);
+    tc::tc_tile_once_kernel<ST, NT, SPLIT><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io);
   return cudaGetLastError();
 }
 
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s, const tc::IoPtrs* io, int nt) {
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io, int nt, int split) {
   if (ntile <= 0) return cudaSuccess;
-  if (nt == 64)
-    return launch_tiles<tc::kStagesN, 64>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
-  return launch_tiles<tc::kStages, 128>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+  if (split == 2) {
+    if (nt == 64) return launch_tiles<64, 2>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+    return launch_tiles<128, 2>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+  }
+  if (nt == 64) return launch_tiles<64, 3>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+  return launch_tiles<128, 3>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
 }
 
 }  // namespace hh

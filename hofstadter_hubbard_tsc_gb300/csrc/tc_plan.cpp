@@ -1,5 +1,5 @@
 // Schedule of the split-precision tensor-core matvec, built from the plan's
-// contribution list on the first BF16X3 matvec of a plan.
+// contribution list on the first split-precision matvec of a plan.
 //
 //   operator images  built once: one per (operator sub-block, role, op, coef);
 //                    the coefficient of a segment is folded into the image of
@@ -45,12 +45,18 @@ struct Arena {
   }
 };
 
+void destroy_graph(hh_tc_plan& t) {
+  if (t.graph_exec) cudaGraphExecDestroy(t.graph_exec);
+  if (t.graph) cudaGraphDestroy(t.graph);
+  t.graph_exec = nullptr;
+  t.graph = nullptr;
+}
+
 }  // namespace
 
 void release_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
-  if (t.graph_exec) cudaGraphExecDestroy(t.graph_exec);
-  if (t.graph) cudaGraphDestroy(t.graph);
+  destroy_graph(t);
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
                   t.d_tiles2, t.d_segs, t.d_csegs, t.d_err, t.d_io};
   for (void* q : ptrs) dev_free(p->ctx, q);
@@ -371,28 +377,31 @@ int build_tc_plan(hh_plan* p) {
 // The launch sequence of one split-precision matvec: wave images, stage 1,
 // zeroed output, stage 2, copy terms.  Explicit vectors (io == nullptr) or
 // the vectors in t.d_io (graph capture).
-static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const tc::IoPtrs* io, cudaEvent_t* ev) {
+static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const tc::IoPtrs* io, cudaEvent_t* ev,
+                              int split) {
   hh_tc_plan& t = p->tc;
   cudaStream_t s = p->ctx->stream;
   if (ev) cudaEventRecord(ev[0], s);
-  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io);
+  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io, split);
   if (ev) cudaEventRecord(ev[1], s);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles1, t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s, io, 64);
+  if (e == cudaSuccess)
+    e = tc_run_tiles(t.d_tiles1, t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s, io, 64, split);
   if (e == cudaSuccess)
     e = tc_run_tiles(t.d_tiles1 + t.n_narrow1, t.n_tiles1 - t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s,
-                     io, 128);
+                     io, 128, split);
   if (ev) cudaEventRecord(ev[2], s);
   if (e == cudaSuccess) e = tc_zero_out(out, p->nelem, s, io);
-  if (e == cudaSuccess) e = tc_run_tiles(t.d_tiles2, t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s, io, 64);
+  if (e == cudaSuccess)
+    e = tc_run_tiles(t.d_tiles2, t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s, io, 64, split);
   if (e == cudaSuccess)
     e = tc_run_tiles(t.d_tiles2 + t.n_narrow2, t.n_tiles2 - t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s,
-                     io, 128);
+                     io, 128, split);
   if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, s, io);
   if (ev) cudaEventRecord(ev[3], s);
   return e;
 }
 
-int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check) {
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check, int split) {
   hh_ctx* ctx = p->ctx;
   if (!p->tc.ready) {
     int st = build_tc_plan(p);
@@ -404,7 +413,7 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check
     // eager launches with events between the stages
     cudaEvent_t ev[4];
     for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
-    e = enqueue_tc(p, in, out, nullptr, ev);
+    e = enqueue_tc(p, in, out, nullptr, ev, split);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
     if (e == cudaSuccess) {
       cudaEventElapsedTime(&ms[0], ev[0], ev[3]);
@@ -413,14 +422,17 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check
       cudaEventElapsedTime(&ms[3], ev[0], ev[1]);
     }
     for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
-  } else if (t.calls++ == 0) {
-    // the first call runs eagerly (and initialises the kernels' attributes)
-    e = enqueue_tc(p, in, out, nullptr, nullptr);
+  } else if (t.calls++ == 0 || split != t.graph_split) {
+    // the first call at a split runs eagerly (and initialises the kernels'
+    // attributes); the graph is captured again at the new split next time
+    destroy_graph(t);
+    t.graph_split = split;
+    e = enqueue_tc(p, in, out, nullptr, nullptr, split);
   } else {
     if (!t.graph_exec) {
       e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
-        cudaError_t eq = enqueue_tc(p, nullptr, nullptr, t.d_io, nullptr);
+        cudaError_t eq = enqueue_tc(p, nullptr, nullptr, t.d_io, nullptr, split);
         e = cudaStreamEndCapture(ctx->stream, &t.graph);
         if (e == cudaSuccess) e = eq;
       }
@@ -450,7 +462,7 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check
 // persistent kernel or one CTA per tile) on this plan's own task lists, reps
 // timed runs each after one warm-up, and keeps the fastest; ms[v] receives
 // the mean time of variant v = 2 * persistent1 + persistent2.
-int tune_tc_plan(hh_plan* p, int reps, double* ms) {
+int tune_tc_plan(hh_plan* p, int reps, double* ms, int split) {
   hh_ctx* ctx = p->ctx;
   if (!p->tc.ready) {
     int st = build_tc_plan(p);
@@ -471,7 +483,7 @@ int tune_tc_plan(hh_plan* p, int reps, double* ms) {
     double sum = 0.0;
     for (int r = 0; r <= reps; ++r) {
       float m[4];
-      int st = matvec_tc(p, p->d_host_in, p->d_host_out, m, true);
+      int st = matvec_tc(p, p->d_host_in, p->d_host_out, m, true, split);
       if (st) return st;
       if (r > 0) sum += m[0];
     }
@@ -485,10 +497,7 @@ int tune_tc_plan(hh_plan* p, int reps, double* ms) {
   t.persistent1 = (best_v >> 1) & 1;
   t.persistent2 = best_v & 1;
   // the next graph is captured with the chosen kernels
-  if (t.graph_exec) cudaGraphExecDestroy(t.graph_exec);
-  if (t.graph) cudaGraphDestroy(t.graph);
-  t.graph_exec = nullptr;
-  t.graph = nullptr;
+  destroy_graph(t);
   return HH_OK;
 }
 
@@ -497,9 +506,10 @@ int tune_tc_plan(hh_plan* p, int reps, double* ms) {
 // ---------------------------------------------------------------------------
 // Self-test of the tensor-core tile path on one dense complex product
 // C = A B (column-major, interleaved complex), used by the unit tests.
-extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C) {
+extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C,
+                              int precision) {
   using namespace hh;
-  if (!ctx || M < 1 || N < 1 || K < 1 || !A || !B || !C) return HH_ERR_INVALID;
+  if (!ctx || M < 1 || N < 1 || K < 1 || !A || !B || !C || !split_of(precision)) return HH_ERR_INVALID;
   const long long ia = img_bytes(M, K), ib = img_bytes(N, K);
   void *dA = nullptr, *dB = nullptr, *dC = nullptr, *dimg = nullptr, *dtask = nullptr, *dtile = nullptr,
        *dseg = nullptr, *derr = nullptr;
@@ -566,7 +576,8 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
   if (e == cudaSuccess) e = cudaMemcpyAsync(dseg, segs.data(), segs.size() * sizeof(tc::Seg), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = tc_build_images((tc::ImgTask*)dtask, 2, nullptr, false, s);
   if (e == cudaSuccess)
-    e = tc_run_tiles((tc::Tile*)dtile, (int)tiles.size(), (tc::Seg*)dseg, (double2*)dC, (int*)derr, true, s);
+    e = tc_run_tiles((tc::Tile*)dtile, (int)tiles.size(), (tc::Seg*)dseg, (double2*)dC, (int*)derr, true, s,
+                     nullptr, 128, split_of(precision));
   int herr = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(C, dC, (size_t)M * N * 16, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s);

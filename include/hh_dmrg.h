@@ -35,7 +35,10 @@ extern "C" {
 
 /* precision of the superblock matvec */
 #define HH_PREC_FP64 0        /* complex FP64 on the CUDA cores                   */
-#define HH_PREC_BF16X3 1      /* three-way BF16 split, FP32 accumulate (tcgen05)  */
+#define HH_PREC_BF16X6 1      /* three BF16 parts, six products per real product,
+                                 FP32 accumulate (tcgen05): ~2^-24 per product    */
+#define HH_PREC_BF16X3 2      /* two BF16 parts, three products (x0y0 + x0y1 +
+                                 x1y0), FP32 accumulate: ~2^-16 per product       */
 
 typedef struct hh_ctx hh_ctx_t;
 typedef struct hh_block hh_block_t;
@@ -142,8 +145,9 @@ int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* en
  * [8] executed FLOPs of stage 1, [9] of stage 2, [10] reference FLOPs of the
  * first GEMM of the two-GEMM terms, [11] the remaining reference FLOPs,
  * [12], [13] BF16 tensor FLOPs issued by the split-precision stages 1 and 2
- * (padding included), [14] bytes of its operand images, [15] 1 once the
- * split-precision schedule has been built (first BF16X3 matvec), [16] kernel
+ * at HH_PREC_BF16X6 (padding included; HH_PREC_BF16X3 issues half),
+ * [14] bytes of its operand images, [15] 1 once the split-precision
+ * schedule has been built (first split-precision matvec), [16] kernel
  * launches of one FP64 matvec, [17] of one split-precision matvec (graph
  * replay included), [18] FP64 work tiles after balancing, [19] 1 when stage
  * 1 of the split-precision matvec runs on the persistent kernel.  counts
@@ -183,14 +187,15 @@ int hh_matvec_async(hh_plan_t* plan, const hh_wave_t* in, hh_wave_t* out, int pr
 int hh_plan_check(hh_plan_t* plan);
 /* Autotuner of the split-precision launch: times the four variants of the
  * tile GEMM (stage 1 / stage 2 on the persistent kernel or one CTA per tile)
- * on this plan, reps runs each after a warm-up, and keeps the fastest for
- * the plan's later matvecs.  ms (may be NULL) receives the four mean times
+ * on this plan at the given split precision, reps runs each after a
+ * warm-up, and keeps the fastest for the plan's later matvecs.  ms (may be NULL) receives the four mean times
  * in ms, index 2 * stage1_persistent + stage2_persistent; *choice (may be
  * NULL) the kept index.  FP64 plans have nothing to tune (choice 0).      */
 int hh_plan_tune(hh_plan_t* plan, int precision, int reps, double* ms, int* choice);
 /* lanczos_memo_new (code/lanczos.f90:4-177), levels = 1.  psi is the start
  * vector on entry and the ground state on exit; lanzero is the breakdown and
- * convergence threshold; maxit <= 100 is loop_in.  With HH_PREC_BF16X3 the
+ * convergence threshold; maxit <= 100 is loop_in.  With a split precision
+ * (HH_PREC_BF16X6, HH_PREC_BF16X3) the
  * Krylov recurrence first runs on the split-precision matvec until the Ritz
  * value moves by <= max(lanzero, 1e-8); a second Lanczos restarted from that
  * vector takes its first product in FP64 and the rest in split precision and
@@ -276,8 +281,10 @@ int hh_wave_sector_norms(const hh_wave_t* w, double* norms2);
 int hh_wave_scale_sectors(hh_wave_t* w, const double* scale);
 
 /* Diagnostic: C = A B for dense complex column-major A (M x K), B (K x N)
- * through the split-precision tensor-core tile kernel (host buffers).     */
-int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C);
+ * through the split-precision tensor-core tile kernel (host buffers) at a
+ * split precision (HH_PREC_BF16X6 or HH_PREC_BF16X3).                     */
+int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C,
+                   int precision);
 
 #ifdef __cplusplus
 }

@@ -22,7 +22,7 @@ def test_gpu_dmrg_exact(device, W, L, ne, U, phi):
     assert e == pytest.approx(es, abs=1e-8)
 
 
-@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X6, _lib.HH_PREC_BF16X3])
 def test_gpu_dmrg_tj_exact(device, precision):
     lat = SquareLattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
     d = GPUDMRG(device, lat, 6, kept_min=300, kept_max=300, trun_err=1e-14, lanzero=1e-11, precision=precision)
@@ -31,12 +31,13 @@ def test_gpu_dmrg_tj_exact(device, precision):
     assert e == pytest.approx(es, abs=1e-8)
 
 
-def test_gpu_dmrg_split_precision(device):
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_BF16X6, _lib.HH_PREC_BF16X3])
+def test_gpu_dmrg_split_precision(device, precision):
     lat = SquareLattice(2, 6, U=8.0, phi=0.25)
     d64 = GPUDMRG(device, lat, 10, kept_min=48, kept_max=48, trun_err=1e-14, lanzero=1e-10)
     e64 = d64.run(sweeps=1)
     dmx = GPUDMRG(device, lat, 10, kept_min=48, kept_max=48, trun_err=1e-14, lanzero=1e-8,
-                  precision=_lib.HH_PREC_BF16X3)
+                  precision=precision)
     emx = dmx.run(sweeps=1)
     assert abs(emx - e64) / abs(e64) < 1e-8, (emx, e64)
 

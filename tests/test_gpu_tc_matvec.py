@@ -1,5 +1,6 @@
-"""Split-precision (three-way BF16, tcgen05) model_wave against the FP64 path on
-oracle DMRG superblocks, and its Lanczos energy against the FP64 Lanczos."""
+"""Split-precision (BF16x6: three BF16 parts, BF16x3: two; tcgen05) model_wave
+against the FP64 path on oracle DMRG superblocks, and its Lanczos energy
+against the FP64 Lanczos."""
 import ctypes as C
 
 import numpy as np
@@ -11,10 +12,14 @@ from tests import helpers as H
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 5e-6  # FP32-level: 24-bit split operands, FP32 accumulation
+# BF16x6: 24-bit split operands, FP32 accumulation (FP32 level); BF16x3:
+# dropped x1 y1 terms and 16-bit operands, about 2^-16 per product
+RTOL = {_lib.HH_PREC_BF16X6: 5e-6, _lib.HH_PREC_BF16X3: 2e-5}
+SPLITS = [_lib.HH_PREC_BF16X6, _lib.HH_PREC_BF16X3]
 
 
-def test_tc_matvec_matches_fp64(device):
+@pytest.mark.parametrize("precision", SPLITS)
+def test_tc_matvec_matches_fp64(device, precision):
     lat, d = H.record_superblocks(2, 6, 10, 32)
     plat = H.product_lattice(lat)
     for idx, rec in enumerate(d.record[::2]):
@@ -23,13 +28,14 @@ def test_tc_matvec_matches_fp64(device):
                         H.superbasis(sup), plat.geometry(sys.len, env.len))
         x = H.wave(H.random_wave(sup, idx))
         a = sb.model_wave(x, precision=_lib.HH_PREC_FP64).flat()
-        b = sb.model_wave(x, precision=_lib.HH_PREC_BF16X3).flat()
+        b = sb.model_wave(x, precision=precision).flat()
         err = np.linalg.norm(a - b) / np.linalg.norm(a)
-        assert err < RTOL, (idx, err)
+        assert err < RTOL[precision], (idx, err)
         sb.free()
 
 
-def test_tc_matvec_synthetic_m200(device):
+@pytest.mark.parametrize("precision", SPLITS)
+def test_tc_matvec_synthetic_m200(device, precision):
     from hofstadter_hubbard_tsc_gb300.synth import Workload
     wl = Workload(W=4, L=8, n_elec=28, m=200)
     sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
@@ -38,13 +44,20 @@ def test_tc_matvec_synthetic_m200(device):
     sb.w_in.upload(psi)
     device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
     ref = sb.w_out.download()
-    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_BF16X3))
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, precision))
     got = sb.w_out.download()
-    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < RTOL
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < RTOL[precision]
+    # switching precision on one plan re-captures the matvec graph
+    for pr in (precision, SPLITS[0] if precision != SPLITS[0] else SPLITS[1], precision):
+        device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, pr))
+        got = sb.w_out.download()
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < RTOL[pr]
+    assert device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, 7) == -1
     sb.free()
 
 
-def test_tc_lanczos_energy(device):
+@pytest.mark.parametrize("precision", SPLITS)
+def test_tc_lanczos_energy(device, precision):
     lat, d = H.record_superblocks(2, 6, 10, 32)
     plat = H.product_lattice(lat)
     rec = d.record[-3]
@@ -53,6 +66,6 @@ def test_tc_lanczos_energy(device):
                     H.superbasis(sup), plat.geometry(sys.len, env.len))
     start = H.wave(H.random_wave(sup, 9))
     e64, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_FP64)
-    emx, _, _ = sb.lanczos_memo_new(start, 1e-8, precision=_lib.HH_PREC_BF16X3)
+    emx, _, _ = sb.lanczos_memo_new(start, 1e-8, precision=precision)
     assert abs(emx - e64) / abs(e64) < 1e-8, (emx, e64)
     sb.free()

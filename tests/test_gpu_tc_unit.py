@@ -1,15 +1,20 @@
 """The split-precision tensor-core tile kernel on dense complex products,
-against an FP64 product: the BF16 three-way split must reach FP32-level
-accuracy (relative error < 2e-6 of ||A|| ||B||)."""
+against an FP64 product: the three-part BF16 split (BF16x6) must reach
+FP32-level accuracy (error < 2e-6 of max|A| max|B| sqrt(K)), the two-part
+split (BF16x3, dropped terms ~2^-16 per product) < 2e-5."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
+from hofstadter_hubbard_tsc_gb300 import _lib
+
 pytestmark = pytest.mark.gpu
 
+TOL = {_lib.HH_PREC_BF16X6: 2e-6, _lib.HH_PREC_BF16X3: 2e-5}
 
-def _run(device, M, N, K, seed):
+
+def _run(device, M, N, K, seed, precision):
     rng = np.random.default_rng(seed)
     A = (rng.normal(size=(M, K)) + 1j * rng.normal(size=(M, K)))
     B = (rng.normal(size=(K, N)) + 1j * rng.normal(size=(K, N)))
@@ -18,13 +23,22 @@ def _run(device, M, N, K, seed):
     c = np.zeros(2 * M * N)
     dp = C.POINTER(C.c_double)
     device.check(device.lib.hh_tc_selftest(device.h, M, N, K, a.ctypes.data_as(dp), b.ctypes.data_as(dp),
-                                           c.ctypes.data_as(dp)))
+                                           c.ctypes.data_as(dp), precision))
     got = c.view(np.complex128).reshape((M, N), order="F")
     ref = A @ B
     return np.abs(got - ref).max() / (np.abs(A).max() * np.abs(B).max() * np.sqrt(K))
 
 
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_BF16X6, _lib.HH_PREC_BF16X3])
 @pytest.mark.parametrize("M,N,K", [(128, 16, 16), (128, 128, 64), (40, 24, 37), (300, 200, 150), (8, 8, 8)])
-def test_tc_tile_product(device, M, N, K):
-    err = _run(device, M, N, K, seed=M + N + K)
-    assert err < 2e-6, err
+def test_tc_tile_product(device, M, N, K, precision):
+    err = _run(device, M, N, K, seed=M + N + K, precision=precision)
+    assert err < TOL[precision], err
+
+
+def test_tc_selftest_rejects_fp64(device):
+    z = np.zeros(2 * 64)
+    dp = C.POINTER(C.c_double)
+    st = device.lib.hh_tc_selftest(device.h, 8, 8, 8, z.ctypes.data_as(dp), z.ctypes.data_as(dp),
+                                   z.ctypes.data_as(dp), _lib.HH_PREC_FP64)
+    assert st == -1
