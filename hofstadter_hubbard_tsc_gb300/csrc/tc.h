@@ -15,7 +15,7 @@ struct ImgTask {
   int sbase;
   int ld;
   int rows, kc;    // logical extent (complex)
-  int r8, k16;     // padded extent
+  int rpad, k16;   // padded extent (rows to a multiple of 16, k to 16)
   int trans, conj;
   double cre, cim;
   long long dst;   // absolute address of the image (256-byte aligned)
@@ -25,7 +25,7 @@ struct ImgTask {
 // [n0, n0+ntile) for nkc chunks of 16 complex k
 struct Seg {
   long long a, b;        // address of plane 0, chunk 0 at the tile's first row
-  long long a_plane, b_plane;  // bytes between planes (= R8/8 * 256 of the image)
+  long long a_plane, b_plane;  // bytes between planes (= Rpad/8 * 256 of the image)
   int a_bytes, b_bytes;  // bytes per plane copy (rows * 32)
   int nkc;
   int pad;
@@ -39,11 +39,20 @@ struct Tile {
   int mrem, nrem;        // valid rows / columns of the tile
   long long out;         // mode 0: element offset of (m0, n0) in the output wave; mode 1: image address
   int ldo;
-  int t_r8;              // mode 1: padded rows of the T image
+  int t_rpad;            // mode 1: padded rows of the T image
   int m0, n0;            // tile origin inside its rectangle
   int nchunk;            // sum of the segments' nkc (MMA chunks of the tile)
+  int stack;             // 1: at most 64 rows (every segment's A copy too): re and im parts of A
+                         // stacked in one 128-row operand, one MMA per part pair (tc_gemm.cu)
+  int pack;              // bit 0: every segment's A copy is its whole image height (one copy
+                         // of all planes per chunk); bit 1: the same for B with planes ntile rows
+  int a_pair, a_im;      // shared memory of A plane q: (q / 2) * a_pair + (q % 2) * a_im bytes
   int pad;
 };
+
+// Fills a finished tile's nchunk, stack, pack, a_pair and a_im from its
+// segments (tc_plan.cpp).
+void finish_tile(Tile& t, const Seg* segs);
 
 // Input and output waves of a matvec, read by the kernels from device memory
 // when a captured graph replays the matvec for new vectors (io != nullptr);

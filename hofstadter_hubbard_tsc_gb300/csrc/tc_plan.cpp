@@ -24,10 +24,12 @@ namespace hh {
 
 namespace {
 
-inline int r8(int r) { return (r + 7) & ~7; }
+// image rows are padded to 16 so that a B image spanning one tile has planes
+// exactly ntile rows high (packed loads, tc_gemm.cu)
+inline int rpad(int r) { return (r + 15) & ~15; }
 inline int k16(int k) { return (k + 15) & ~15; }
 inline long long img_bytes(int rows, int kc) {
-  long long b = (long long)r8(rows) * k16(kc) * 12;  // six bf16 planes
+  long long b = (long long)rpad(rows) * k16(kc) * 12;  // six bf16 planes
   return (b + 255) & ~255LL;
 }
 
@@ -45,6 +47,18 @@ struct Arena {
   }
 };
 
+// MMA cycles of one 16-k chunk of a tile, in units of a plain 128-wide
+// chunk: a K = 16 MMA costs about max(45, N/2) cycles whatever its M; plain
+// tiles issue four of width ntile per part pair, stacked tiles one of width
+// 2 ntile
+double chunk_cost(const tc::Tile& x) {
+  const double n = x.ntile;
+  return x.stack ? std::max(45.0, n) / 256.0 : 4.0 * std::max(45.0, n / 2.0) / 256.0;
+}
+
+// MMA work of a tile plus a fixed share for its set-up and epilogue
+double tile_cost(const tc::Tile& x) { return x.nchunk * chunk_cost(x) + 4.0; }
+
 void destroy_graph(hh_tc_plan& t) {
   if (t.graph_exec) cudaGraphExecDestroy(t.graph_exec);
   if (t.graph) cudaGraphDestroy(t.graph);
@@ -53,6 +67,42 @@ void destroy_graph(hh_tc_plan& t) {
 }
 
 }  // namespace
+
+namespace tc {
+
+// A tile is stacked when it has at most 64 rows and every segment copies at
+// most 64 rows of A; packed in A when every segment's A copy is its whole
+// image (one plane stride for all), packed in B when every B copy is a
+// whole image exactly ntile rows high.  The A plane offsets in shared
+// memory follow: packed -> the image's plane stride, else 128-row slots
+// (64-row halves when stacked).
+void finish_tile(Tile& t, const Seg* segs) {
+  t.nchunk = 0;
+  bool stack = t.mode == 0 && t.mrem <= 64 && t.nseg > 0, pa = t.nseg > 0, pb = t.nseg > 0;
+  const long long a_plane = t.nseg > 0 ? segs[t.seg0].a_plane : 0;
+  for (int si = 0; si < t.nseg; ++si) {
+    const Seg& sg = segs[t.seg0 + si];
+    t.nchunk += sg.nkc;
+    stack = stack && sg.a_bytes <= 64 * 32;
+    pa = pa && sg.a_bytes == sg.a_plane && sg.a_plane == a_plane;
+    pb = pb && sg.b_bytes == sg.b_plane && sg.b_plane == (long long)t.ntile * 32;
+  }
+  t.stack = stack ? 1 : 0;
+  t.pack = (pa ? 1 : 0) | (pb ? 2 : 0);
+  constexpr int kSlot = 128 * 32;  // one 128-row plane slot
+  if (pa) {
+    t.a_pair = (int)(2 * a_plane);
+    t.a_im = (int)a_plane;
+  } else if (stack) {
+    t.a_pair = kSlot;
+    t.a_im = kSlot / 2;
+  } else {
+    t.a_pair = 2 * kSlot;
+    t.a_im = kSlot;
+  }
+}
+
+}  // namespace tc
 
 void release_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
@@ -86,7 +136,7 @@ int build_tc_plan(hh_plan* p) {
     t.ld = m.ld;
     t.rows = rows;
     t.kc = kc;
-    t.r8 = r8(rows);
+    t.rpad = rpad(rows);
     t.k16 = k16(kc);
     // A, op N: O[r + k ld]; A, op C: conj O[k + r ld]; B, op N: O[k + n ld]; B, op C: conj O[n + k ld]
     t.trans = (role == 0) ? (m.op == HH_OP_C) : (m.op == HH_OP_N);
@@ -114,7 +164,7 @@ int build_tc_plan(hh_plan* p) {
     t.ld = w.sdim;
     t.rows = r.rows;
     t.kc = r.kc;
-    t.r8 = r8(r.rows);
+    t.rpad = rpad(r.rows);
     t.k16 = k16(r.kc);
     t.trans = role == 1 ? 1 : 0;
     t.conj = 0;
@@ -137,13 +187,13 @@ int build_tc_plan(hh_plan* p) {
   double mma1 = 0.0, mma2 = 0.0;
   auto make_seg = [&](long long a, const ImgRef& ai, int m0, long long b, const ImgRef& bi, int n0, int ntile) {
     tc::Seg s{};
-    const int ar8 = r8(ai.rows), br8 = r8(bi.rows);
+    const int ar = rpad(ai.rows), br = rpad(bi.rows);
     s.a = a + (long long)(m0 / 8) * 256;
     s.b = b + (long long)(n0 / 8) * 256;
-    s.a_plane = (long long)(ar8 / 8) * 256;
-    s.b_plane = (long long)(br8 / 8) * 256;
-    s.a_bytes = std::min(128, ar8 - m0) * 32;
-    s.b_bytes = std::min(ntile, br8 - n0) * 32;
+    s.a_plane = (long long)(ar / 8) * 256;
+    s.b_plane = (long long)(br / 8) * 256;
+    s.a_bytes = std::min(128, ar - m0) * 32;
+    s.b_bytes = std::min(ntile, br - n0) * 32;
     s.nkc = k16(ai.kc) / 16;
     return s;
   };
@@ -178,11 +228,10 @@ int build_tc_plan(hh_plan* p) {
         tl.mrem = std::min(128, c.M - m0);
         tl.nrem = std::min(128, c.Kb - n0);
         tl.out = tag(T.off, 2);
-        tl.t_r8 = r8(c.M);
+        tl.t_rpad = rpad(c.M);
         tl.m0 = m0;
         tl.n0 = n0;
         tiles1.push_back(tl);
-        mma1 += 8.0 * 128 * ntile * (double)k16(c.Ka) * 6.0;
       }
   }
 
@@ -217,17 +266,14 @@ int build_tc_plan(hh_plan* p) {
             const ImgRef& T = contrib_t[ci];
             ImgRef bi = op_img(c.B, 1, c.N, c.Kb, c.cre, c.cim);
             segs.push_back(make_seg(tag(T.off, 2), T, m0, tag(bi.off, 0), bi, n0, ntile));
-            mma2 += 8.0 * 128 * ntile * (double)k16(c.Kb) * 6.0;
           } else if (c.hasA) {
             ImgRef ai = op_img(c.A, 0, c.M, c.Ka, c.cre, c.cim);
             ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.N, 1);
             segs.push_back(make_seg(tag(ai.off, 0), ai, m0, tag(xi.off, 1), xi, n0, ntile));
-            mma2 += 8.0 * 128 * ntile * (double)k16(c.Ka) * 6.0;
           } else if (c.hasB) {
             ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.M, c.Kb, 0);
             ImgRef bi = op_img(c.B, 1, c.N, c.Kb, c.cre, c.cim);
             segs.push_back(make_seg(tag(xi.off, 1), xi, m0, tag(bi.off, 0), bi, n0, ntile));
-            mma2 += 8.0 * 128 * ntile * (double)k16(c.Kb) * 6.0;
           } else {
             hh_seg cs{};
             const hh_wsec& wi = L->secs[c.i_in];
@@ -263,10 +309,15 @@ int build_tc_plan(hh_plan* p) {
       }
   }
 
+  // chunk counts and load / MMA forms of every tile; BF16 tensor FLOPs
+  // issued per matvec (counted at six split products: four MMAs of width
+  // ntile per part pair, or one of 2 ntile when stacked)
+  mma1 = mma2 = 0.0;
   for (auto* tl : {&tiles1, &tiles2})
     for (auto& x : *tl) {
-      x.nchunk = 0;
-      for (int si = 0; si < x.nseg; ++si) x.nchunk += segs[x.seg0 + si].nkc;
+      tc::finish_tile(x, segs.data());
+      const double f = (double)x.nchunk * 16 * 128 * 2.0 * (x.stack ? 2.0 : 4.0) * x.ntile * 6.0;
+      (tl == &tiles1 ? mma1 : mma2) += f;
     }
 
   // ------------------------------------------------------- tile order
@@ -291,7 +342,7 @@ int build_tc_plan(hh_plan* p) {
     const size_t n = hi - lo;
     if (n <= G) return;
     std::vector<std::pair<double, size_t>> cost(n);
-    for (size_t i = 0; i < n; ++i) cost[i] = {8.0 + tl[lo + i].nchunk * (tl[lo + i].ntile / 128.0), lo + i};
+    for (size_t i = 0; i < n; ++i) cost[i] = {8.0 + tl[lo + i].nchunk * chunk_cost(tl[lo + i]), lo + i};
     std::stable_sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
     std::vector<tc::Tile> out(n);
     for (size_t k = 0; k < n; ++k) {
@@ -303,6 +354,9 @@ int build_tc_plan(hh_plan* p) {
   };
   const int n1n = split_narrow(tiles1);
   const int n2n = 0;
+  std::stable_sort(tiles2.begin(), tiles2.end(), [](const tc::Tile& a, const tc::Tile& b) {
+    return tile_cost(a) > tile_cost(b);
+  });
   balance(tiles1, 0, n1n, 2 * (size_t)sms);
   balance(tiles1, n1n, tiles1.size(), (size_t)sms);
 
@@ -533,9 +587,9 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
   cudaMemsetAsync(derr, 0, sizeof(int), s);
   tc::ImgTask tk[2] = {};
   tk[0].src = (long long)(uintptr_t)dA; tk[0].sbase = HH_BASE_ABS; tk[0].ld = M; tk[0].rows = M; tk[0].kc = K;
-  tk[0].r8 = r8(M); tk[0].k16 = k16(K); tk[0].trans = 0; tk[0].cre = 1.0; tk[0].dst = (long long)(uintptr_t)dimg;
+  tk[0].rpad = rpad(M); tk[0].k16 = k16(K); tk[0].trans = 0; tk[0].cre = 1.0; tk[0].dst = (long long)(uintptr_t)dimg;
   tk[1].src = (long long)(uintptr_t)dB; tk[1].sbase = HH_BASE_ABS; tk[1].ld = K; tk[1].rows = N; tk[1].kc = K;
-  tk[1].r8 = r8(N); tk[1].k16 = k16(K); tk[1].trans = 1; tk[1].cre = 1.0;
+  tk[1].rpad = rpad(N); tk[1].k16 = k16(K); tk[1].trans = 1; tk[1].cre = 1.0;
   tk[1].dst = (long long)(uintptr_t)dimg + ia;
   std::vector<tc::Seg> segs;
   std::vector<tc::Tile> tiles;
@@ -545,18 +599,17 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
     for (int n0 = 0; n0 < N; n0 += 128) {
       const int ntile = k16(std::min(128, N - n0));
       tc::Seg sg{};
-      const int ar8 = r8(M), br8 = r8(N);
+      const int ar = rpad(M), br = rpad(N);
       sg.a = tk[0].dst + (long long)(m0 / 8) * 256;
       sg.b = tk[1].dst + (long long)(n0 / 8) * 256;
-      sg.a_plane = (long long)(ar8 / 8) * 256;
-      sg.b_plane = (long long)(br8 / 8) * 256;
-      sg.a_bytes = std::min(128, ar8 - m0) * 32;
-      sg.b_bytes = std::min(ntile, br8 - n0) * 32;
+      sg.a_plane = (long long)(ar / 8) * 256;
+      sg.b_plane = (long long)(br / 8) * 256;
+      sg.a_bytes = std::min(128, ar - m0) * 32;
+      sg.b_bytes = std::min(ntile, br - n0) * 32;
       sg.nkc = k16(K) / 16;
       tc::Tile tl{};
       tl.seg0 = (int)segs.size();
       tl.nseg = 1;
-      tl.nchunk = sg.nkc;
       segs.push_back(sg);
       tl.mode = 0;
       tl.ntile = ntile;
@@ -566,6 +619,7 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
       tl.ldo = M;
       tl.m0 = m0;
       tl.n0 = n0;
+      tc::finish_tile(tl, segs.data());
       tiles.push_back(tl);
     }
   e = cudaMalloc(&dtask, sizeof(tk));
