@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 
 struct hh_seg;
 
@@ -69,9 +70,14 @@ size_t tile_smem_bytes(int nt, int split);
 }  // namespace tc
 
 // fp32: scale and split in FP32 (wave images, the first `split` parts)
-// instead of FP64 (operator images, all three parts)
+// instead of FP64 (operator images, all three parts); d_blocks (from
+// tc_image_blocks) spreads the tasks' row groups evenly over the CTAs,
+// without it one CTA converts one task
 cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
-                            cudaStream_t s, const tc::IoPtrs* io = nullptr, int split = 3);
+                            cudaStream_t s, const tc::IoPtrs* io = nullptr, int split = 3,
+                            const int2* d_blocks = nullptr, int nblocks = 0);
+// block list of tc_build_images for host tasks: (task, first row group) per CTA
+int tc_image_blocks(const tc::ImgTask* tasks, int ntask, std::vector<int2>& out);
 // adds the FP64 copy terms of the stage-2 tiles to their output rectangles
 cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
                           double2* base_out, cudaStream_t s, const tc::IoPtrs* io = nullptr);

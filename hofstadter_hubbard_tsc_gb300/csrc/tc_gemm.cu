@@ -50,6 +50,7 @@
 // q * ntile rows (packed B needs planes exactly ntile rows high).
 #include <cuda_bf16.h>
 #include <cstdint>
+#include <vector>
 
 #include "hh_internal.h"
 #include "tc.h"
@@ -183,19 +184,28 @@ __device__ __forceinline__ size_t img_off(int rpad, int r, int k) {
 // first and scaled and split in FP32: three BF16 parts hold FP32's 24
 // significand bits, and GB300 retires FP32 at 64 times its FP64 rate.
 // Operator images (built once per plan, all three parts) keep the FP64 split.
+// With a block list (blocks != nullptr), block b converts row groups
+// [blocks[b].y, blocks[b].y + kImgGroupsPerBlock) of task blocks[b].x, so
+// that large and small images spread evenly over the SMs; without one, block
+// b converts all of task b.
+constexpr int kImgGroupsPerBlock = 1024;
+
 template <bool kFp32, int SPLIT>
 __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __restrict__ tasks,
+                                                           const int2* __restrict__ blocks,
                                                            const double2* __restrict__ base_in,
                                                            const IoPtrs* __restrict__ io) {
   if (io) base_in = io->in;
-  const ImgTask t = tasks[blockIdx.x];
+  const int2 bw = blocks ? blocks[blockIdx.x] : make_int2((int)blockIdx.x, 0);
+  const ImgTask t = tasks[bw.x];
   const double2* src = t.sbase == HH_BASE_IN ? base_in + t.src : reinterpret_cast<const double2*>(t.src);
   uint8_t* dst = reinterpret_cast<uint8_t*>(t.dst);
   const int rpad = t.rpad, k16 = t.k16;
   const size_t plane = (size_t)(rpad >> 3) * 256;
   const int ngroups = rpad * (k16 >> 3);
+  const int g_end = blocks ? min(ngroups, bw.y + kImgGroupsPerBlock) : ngroups;
   const float fre = (float)t.cre, fim = (float)t.cim;
-  for (int idx = threadIdx.x; idx < ngroups; idx += blockDim.x) {
+  for (int idx = bw.y + threadIdx.x; idx < g_end; idx += blockDim.x) {
     const int r = idx % rpad, k0 = (idx / rpad) * 8;
     __nv_bfloat16 re[3][8], im[3][8];
 #pragma unroll
@@ -786,15 +796,26 @@ size_t tile_smem_bytes(int nt, int split) {
 }  // namespace tc
 
 cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2* base_in, bool fp32,
-                            cudaStream_t s, const tc::IoPtrs* io, int split) {
+                            cudaStream_t s, const tc::IoPtrs* io, int split, const int2* d_blocks, int nblocks) {
   if (ntask <= 0) return cudaSuccess;
+  const int grid = d_blocks ? nblocks : ntask;
+  if (grid <= 0) return cudaSuccess;
   if (!fp32)
-    tc::build_images_kernel<false, 3><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
+    tc::build_images_kernel<false, 3><<<grid, 256, 0, s>>>(d_tasks, d_blocks, base_in, io);
   else if (split == 2)
-    tc::build_images_kernel<true, 2><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
+    tc::build_images_kernel<true, 2><<<grid, 256, 0, s>>>(d_tasks, d_blocks, base_in, io);
   else
-    tc::build_images_kernel<true, 3><<<ntask, 256, 0, s>>>(d_tasks, base_in, io);
+    tc::build_images_kernel<true, 3><<<grid, 256, 0, s>>>(d_tasks, d_blocks, base_in, io);
   return cudaGetLastError();
+}
+
+int tc_image_blocks(const tc::ImgTask* tasks, int ntask, std::vector<int2>& out) {
+  out.clear();
+  for (int i = 0; i < ntask; ++i) {
+    const int ngroups = tasks[i].rpad * (tasks[i].k16 >> 3);
+    for (int g = 0; g < ngroups; g += tc::kImgGroupsPerBlock) out.push_back(make_int2(i, g));
+  }
+  return (int)out.size();
 }
 
 cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,

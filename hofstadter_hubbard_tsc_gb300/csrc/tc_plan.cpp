@@ -108,7 +108,7 @@ void release_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
   destroy_graph(t);
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
-                  t.d_tiles2, t.d_segs, t.d_csegs, t.d_err, t.d_io};
+                  t.d_tiles2, t.d_tiles2b, t.d_segs, t.d_csegs, t.d_err, t.d_io, t.d_x_blocks};
   for (void* q : ptrs) dev_free(p->ctx, q);
   t = hh_tc_plan();
 }
@@ -327,10 +327,11 @@ int build_tc_plan(hh_plan* p) {
   // G resident CTAs takes tiles c, c + G, c + 2G, ...: within each part its
   // tiles go longest first (MMA chunks x N, plus a fixed epilogue share), in
   // a snake over the CTAs, so that every CTA receives a near-equal share.
-  // Stage 2 (hundreds of long, uneven tiles) stays one list in plan order on
-  // the 128-wide kernel, which keeps the tiles of one output sector together
-  // for L2 reuse (split like stage 1 it measured 0.55 against 0.50 ms on the
-  // m = 2000 workload).
+  // Stage 2 (hundreds of long, uneven tiles) stays one list on the 128-wide
+  // kernels, in two orders: longest first for one CTA per tile (the hardware
+  // then hands the next tile to the first free SM: list scheduling; 0.28
+  // against 0.34 ms in plan order at m = 2000), and snake-balanced like
+  // stage 1 for the persistent kernel; the launch autotuner picks.
   int sms = 148, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -353,12 +354,18 @@ int build_tc_plan(hh_plan* p) {
     std::copy(out.begin(), out.end(), tl.begin() + lo);
   };
   const int n1n = split_narrow(tiles1);
-  const int n2n = 0;
-  std::stable_sort(tiles2.begin(), tiles2.end(), [](const tc::Tile& a, const tc::Tile& b) {
-    return tile_cost(a) > tile_cost(b);
-  });
+  const int n2n = 0;  // narrow stage-2 tiles on the two-CTA kernels: 0.29 against 0.24 ms (two tails)
+  auto longest_first = [](std::vector<tc::Tile>& tl, size_t lo, size_t hi) {
+    std::stable_sort(tl.begin() + lo, tl.begin() + hi,
+                     [](const tc::Tile& a, const tc::Tile& b) { return tile_cost(a) > tile_cost(b); });
+  };
+  longest_first(tiles2, 0, n2n);
+  longest_first(tiles2, n2n, tiles2.size());
+  std::vector<tc::Tile> tiles2b = tiles2;
   balance(tiles1, 0, n1n, 2 * (size_t)sms);
   balance(tiles1, n1n, tiles1.size(), (size_t)sms);
+  balance(tiles2b, 0, n2n, 2 * (size_t)sms);
+  balance(tiles2b, n2n, tiles2b.size(), (size_t)sms);
 
   // --------------------------------------------------------------- device
   hh_tc_plan& t = p->tc;
@@ -386,6 +393,8 @@ int build_tc_plan(hh_plan* p) {
   for (auto& tl : tiles1) tl.out = untag(tl.out);
   for (auto& tk : op_tasks) tk.dst += base[0];
   for (auto& tk : x_tasks) tk.dst += base[1];
+  std::vector<int2> x_blocks;
+  t.n_x_blocks = tc_image_blocks(x_tasks.data(), (int)x_tasks.size(), x_blocks);
   auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
     if ((st = alloc(dptr, bytes))) return st;
     if (bytes) {
@@ -396,8 +405,10 @@ int build_tc_plan(hh_plan* p) {
   };
   if ((st = upload((void**)&t.d_op_tasks, op_tasks.data(), op_tasks.size() * sizeof(tc::ImgTask))) ||
       (st = upload((void**)&t.d_x_tasks, x_tasks.data(), x_tasks.size() * sizeof(tc::ImgTask))) ||
+      (st = upload((void**)&t.d_x_blocks, x_blocks.data(), x_blocks.size() * sizeof(int2))) ||
       (st = upload((void**)&t.d_tiles1, tiles1.data(), tiles1.size() * sizeof(tc::Tile))) ||
       (st = upload((void**)&t.d_tiles2, tiles2.data(), tiles2.size() * sizeof(tc::Tile))) ||
+      (st = upload((void**)&t.d_tiles2b, tiles2b.data(), tiles2b.size() * sizeof(tc::Tile))) ||
       (st = upload((void**)&t.d_segs, segs.data(), segs.size() * sizeof(tc::Seg))) ||
       (st = upload((void**)&t.d_csegs, csegs.data(), csegs.size() * sizeof(hh_seg))) ||
       (st = alloc((void**)&t.d_err, sizeof(int))) || (st = alloc((void**)&t.d_io, sizeof(tc::IoPtrs)))) {
@@ -417,9 +428,18 @@ int build_tc_plan(hh_plan* p) {
   t.bytes_t = (double)a_t.size;
   t.mma_flops1 = mma1;
   t.mma_flops2 = mma2;
-  // operator images are built once here
-  cudaError_t e = tc_build_images(t.d_op_tasks, t.n_op_tasks, nullptr, false, ctx->stream);
+  // operator images are built once here (block list freed after the build)
+  std::vector<int2> op_blocks;
+  const int n_op_blocks = tc_image_blocks(op_tasks.data(), (int)op_tasks.size(), op_blocks);
+  int2* d_op_blocks = nullptr;
+  if ((st = upload((void**)&d_op_blocks, op_blocks.data(), op_blocks.size() * sizeof(int2)))) {
+    release_tc_plan(p);
+    return st;
+  }
+  cudaError_t e = tc_build_images(t.d_op_tasks, t.n_op_tasks, nullptr, false, ctx->stream, nullptr, 3, d_op_blocks,
+                                  n_op_blocks);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  dev_free(ctx, d_op_blocks);
   if (e != cudaSuccess) {
     release_tc_plan(p);
     return cuda_check(ctx, e, "build operator images");
@@ -436,7 +456,7 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
   hh_tc_plan& t = p->tc;
   cudaStream_t s = p->ctx->stream;
   if (ev) cudaEventRecord(ev[0], s);
-  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io, split);
+  cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io, split, t.d_x_blocks, t.n_x_blocks);
   if (ev) cudaEventRecord(ev[1], s);
   if (e == cudaSuccess)
     e = tc_run_tiles(t.d_tiles1, t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s, io, 64, split);
@@ -445,10 +465,11 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
                      io, 128, split);
   if (ev) cudaEventRecord(ev[2], s);
   if (e == cudaSuccess) e = tc_zero_out(out, p->nelem, s, io);
+  const tc::Tile* tiles2 = t.persistent2 ? t.d_tiles2b : t.d_tiles2;
   if (e == cudaSuccess)
-    e = tc_run_tiles(t.d_tiles2, t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s, io, 64, split);
+    e = tc_run_tiles(tiles2, t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s, io, 64, split);
   if (e == cudaSuccess)
-    e = tc_run_tiles(t.d_tiles2 + t.n_narrow2, t.n_tiles2 - t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s,
+    e = tc_run_tiles(tiles2 + t.n_narrow2, t.n_tiles2 - t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s,
                      io, 128, split);
   if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, s, io);
   if (ev) cudaEventRecord(ev[3], s);
