@@ -197,6 +197,8 @@ struct hh_tc_plan {
   hh::tc::Tile* d_tiles2b = nullptr;  // the same tiles ordered for the persistent kernel
   int2* d_x_blocks = nullptr;         // wave-image block list (tc_image_blocks)
   int n_x_blocks = 0;
+  int2* d_c_blocks = nullptr;         // copy-term block list over d_tiles2 (tc_copy_blocks)
+  int n_c_blocks = 0;
   int n_tiles1 = 0, n_tiles2 = 0, n_cseg = 0;
   int n_narrow1 = 0, n_narrow2 = 0;  // leading tiles at most 64 wide (64-wide kernels)
   hh::tc::Seg* d_segs = nullptr;

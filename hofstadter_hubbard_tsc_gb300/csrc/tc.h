@@ -78,9 +78,13 @@ cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2
                             const int2* d_blocks = nullptr, int nblocks = 0);
 // block list of tc_build_images for host tasks: (task, first row group) per CTA
 int tc_image_blocks(const tc::ImgTask* tasks, int ntask, std::vector<int2>& out);
-// adds the FP64 copy terms of the stage-2 tiles to their output rectangles
-cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
-                          double2* base_out, cudaStream_t s, const tc::IoPtrs* io = nullptr);
+// adds the copy terms of the stage-2 tiles to their output rectangles, over
+// the block list of tc_copy_blocks (tile, first element) built on the same
+// tile array
+cudaError_t tc_copy_terms(const tc::Tile* d_tiles, const int2* d_blocks, int nblocks, const hh_seg* d_csegs,
+                          const double2* base_in, double2* base_out, cudaStream_t s,
+                          const tc::IoPtrs* io = nullptr);
+int tc_copy_blocks(const tc::Tile* tiles, int ntile, std::vector<int2>& out);
 // writes the vectors of the next graph replay (one thread; arguments by value)
 cudaError_t tc_set_io(tc::IoPtrs* d_io, const double2* in, double2* out, cudaStream_t s);
 // zeroes n complex elements of io->out (graph replays) or of out

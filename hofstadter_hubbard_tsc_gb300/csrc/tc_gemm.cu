@@ -741,10 +741,17 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
   }
 }
 
-// out[rect] += sum_c coef_c * in[region_c] for the FP64 copy terms of each
-// stage-2 tile (site-diagonal terms), element by element after the tiles:
-// coalesced along the column-major rows, bandwidth bound.
+// out[rect] += sum_c coef_c * in[region_c] for the copy terms (site-diagonal
+// terms) of the stage-2 tiles, element by element after the tiles; block b
+// handles elements [blocks[b].y, + kCopyElemsPerBlock) of tile blocks[b].x
+// (only tiles with copy terms are listed).  Coalesced along the
+// column-major rows.  The products are summed in FP32 (GB300 retires FP32
+// at 64 times its FP64 rate; 2^-24 relative on these terms, far below the
+// split products' error) and added to the FP64 output in FP64.
+constexpr int kCopyElemsPerBlock = 2048;
+
 __global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict__ tiles,
+                                                         const int2* __restrict__ blocks,
                                                          const hh_seg* __restrict__ csegs,
                                                          const double2* __restrict__ base_in,
                                                          double2* __restrict__ base_out,
@@ -753,20 +760,25 @@ __global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict_
     base_in = io->in;
     base_out = io->out;
   }
-  const Tile t = tiles[blockIdx.x];
-  if (t.mode != 0 || t.ncseg == 0) return;
+  const int2 bw = blocks[blockIdx.x];
+  const Tile t = tiles[bw.x];
   double2* O = base_out + t.out;
-  const int n = t.mrem * t.nrem;
-  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+  const int n = min(t.mrem * t.nrem, bw.y + kCopyElemsPerBlock);
+  for (int idx = bw.y + threadIdx.x; idx < n; idx += blockDim.x) {
     const int row = idx % t.mrem, col = idx / t.mrem;
-    double2 v = O[(long long)row + (long long)col * t.ldo];
+    float ar = 0.f, ai = 0.f;
     for (int ci = 0; ci < t.ncseg; ++ci) {
       const hh_seg cs = csegs[t.cseg0 + ci];
       const double2 x = base_in[cs.poff + (long long)(t.m0 + row) + (long long)(t.n0 + col) * cs.ldp];
-      v.x += cs.cre * x.x - cs.cim * x.y;
-      v.y += cs.cre * x.y + cs.cim * x.x;
+      const float xr = (float)x.x, xi = (float)x.y, cr = (float)cs.cre, cim = (float)cs.cim;
+      ar = fmaf(cr, xr, fmaf(-cim, xi, ar));
+      ai = fmaf(cr, xi, fmaf(cim, xr, ai));
     }
-    O[(long long)row + (long long)col * t.ldo] = v;
+    double2* o = O + (long long)row + (long long)col * t.ldo;
+    double2 v = *o;
+    v.x += (double)ar;
+    v.y += (double)ai;
+    *o = v;
   }
 }
 
@@ -818,11 +830,21 @@ int tc_image_blocks(const tc::ImgTask* tasks, int ntask, std::vector<int2>& out)
   return (int)out.size();
 }
 
-cudaError_t tc_copy_terms(const tc::Tile* d_tiles, int ntile, const hh_seg* d_csegs, const double2* base_in,
-                          double2* base_out, cudaStream_t s, const tc::IoPtrs* io) {
-  if (ntile <= 0) return cudaSuccess;
-  tc::copy_terms_kernel<<<ntile, 256, 0, s>>>(d_tiles, d_csegs, base_in, base_out, io);
+cudaError_t tc_copy_terms(const tc::Tile* d_tiles, const int2* d_blocks, int nblocks, const hh_seg* d_csegs,
+                          const double2* base_in, double2* base_out, cudaStream_t s, const tc::IoPtrs* io) {
+  if (nblocks <= 0) return cudaSuccess;
+  tc::copy_terms_kernel<<<nblocks, 256, 0, s>>>(d_tiles, d_blocks, d_csegs, base_in, base_out, io);
   return cudaGetLastError();
+}
+
+int tc_copy_blocks(const tc::Tile* tiles, int ntile, std::vector<int2>& out) {
+  out.clear();
+  for (int i = 0; i < ntile; ++i) {
+    if (tiles[i].mode != 0 || tiles[i].ncseg == 0) continue;
+    const int n = tiles[i].mrem * tiles[i].nrem;
+    for (int e = 0; e < n; e += tc::kCopyElemsPerBlock) out.push_back(make_int2(i, e));
+  }
+  return (int)out.size();
 }
 
 cudaError_t tc_set_io(tc::IoPtrs* d_io, const double2* in, double2* out, cudaStream_t s) {

@@ -108,7 +108,8 @@ void release_tc_plan(hh_plan* p) {
   hh_tc_plan& t = p->tc;
   destroy_graph(t);
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
-                  t.d_tiles2, t.d_tiles2b, t.d_segs, t.d_csegs, t.d_err, t.d_io, t.d_x_blocks};
+                  t.d_tiles2, t.d_tiles2b, t.d_segs, t.d_csegs, t.d_err, t.d_io, t.d_x_blocks,
+                  t.d_c_blocks};
   for (void* q : ptrs) dev_free(p->ctx, q);
   t = hh_tc_plan();
 }
@@ -393,8 +394,9 @@ int build_tc_plan(hh_plan* p) {
   for (auto& tl : tiles1) tl.out = untag(tl.out);
   for (auto& tk : op_tasks) tk.dst += base[0];
   for (auto& tk : x_tasks) tk.dst += base[1];
-  std::vector<int2> x_blocks;
+  std::vector<int2> x_blocks, c_blocks;
   t.n_x_blocks = tc_image_blocks(x_tasks.data(), (int)x_tasks.size(), x_blocks);
+  t.n_c_blocks = tc_copy_blocks(tiles2.data(), (int)tiles2.size(), c_blocks);
   auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
     if ((st = alloc(dptr, bytes))) return st;
     if (bytes) {
@@ -406,6 +408,7 @@ int build_tc_plan(hh_plan* p) {
   if ((st = upload((void**)&t.d_op_tasks, op_tasks.data(), op_tasks.size() * sizeof(tc::ImgTask))) ||
       (st = upload((void**)&t.d_x_tasks, x_tasks.data(), x_tasks.size() * sizeof(tc::ImgTask))) ||
       (st = upload((void**)&t.d_x_blocks, x_blocks.data(), x_blocks.size() * sizeof(int2))) ||
+      (st = upload((void**)&t.d_c_blocks, c_blocks.data(), c_blocks.size() * sizeof(int2))) ||
       (st = upload((void**)&t.d_tiles1, tiles1.data(), tiles1.size() * sizeof(tc::Tile))) ||
       (st = upload((void**)&t.d_tiles2, tiles2.data(), tiles2.size() * sizeof(tc::Tile))) ||
       (st = upload((void**)&t.d_tiles2b, tiles2b.data(), tiles2b.size() * sizeof(tc::Tile))) ||
@@ -471,7 +474,8 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
   if (e == cudaSuccess)
     e = tc_run_tiles(tiles2 + t.n_narrow2, t.n_tiles2 - t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s,
                      io, 128, split);
-  if (e == cudaSuccess && t.n_cseg > 0) e = tc_copy_terms(t.d_tiles2, t.n_tiles2, t.d_csegs, in, out, s, io);
+  if (e == cudaSuccess && t.n_c_blocks > 0)
+    e = tc_copy_terms(t.d_tiles2, t.d_c_blocks, t.n_c_blocks, t.d_csegs, in, out, s, io);
   if (ev) cudaEventRecord(ev[3], s);
   return e;
 }
