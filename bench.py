@@ -128,6 +128,20 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "_fallback": True}
 
 
+def captured_traffic(workload, precision):
+    """DRAM bytes per launch of the dominant (stage-2) kernel from the committed
+    ncu capture of the same workload and precision (dram__bytes_read.sum +
+    dram__bytes_write.sum), else None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "tc_stage2_traffic.json")) as f:
+            t = json.load(f)
+        if t.get("workload") == workload and t.get("precision") == precision:
+            return float(t["dram_bytes_per_launch"])
+    except Exception:
+        pass
+    return None
+
+
 def fp64_peak_tflops():
     """Dense FP64 rate of this GPU, measured with cuBLAS DGEMM (torch.matmul, best of 5)."""
     try:
@@ -412,7 +426,9 @@ def main():
         peak = peaks["bf16_tflops"] / nprod
         peak_note = (f"measured bf16 burst / {nprod} ({args.precision}: {nprod} bf16 products per real product)")
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if peak else None, "traffic": None,
+                "frac": (achieved / peak) if peak else None,
+                "traffic": (captured_traffic(wl.describe()["workload"], args.precision)
+                            if stage == 2 and prec != _lib.HH_PREC_FP64 else None),
                 "kernel": (f"seg_gemm_fp64 stage {stage}" if prec == _lib.HH_PREC_FP64
                            else f"tc_tile_kernel stage {stage}"),
                 "peak_note": peak_note,
