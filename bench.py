@@ -49,6 +49,10 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--precision", default="bf16x3", choices=["fp64", "bf16x6", "bf16x3"],
                    help="bf16x3: two BF16 parts, three products per real product; bf16x6: three parts, six")
+    p.add_argument("--config", default="c2", choices=["c2", "c3", "c4"],
+                   help="matvec workload: c2 Hubbard 4x32 phi=1/4 N_e=112 m=2000 (headline); c3 t-J 4x48 "
+                        "J=0.4 phi=1/6 N_e=176 m=4000; c4 Hubbard 6x24 phi=1/3 N_e=132 m=6000 (mid-chain "
+                        "superblocks, synthetic operators); --W/--L/--ne/--m override c2's sizes")
     p.add_argument("--m", type=int, default=2000)
     p.add_argument("--W", type=int, default=4)
     p.add_argument("--L", type=int, default=32)
@@ -164,6 +168,16 @@ def fp64_peak_tflops():
         return None
 
 
+def make_workload(args):
+    """The mid-chain superblock of the chosen configuration (synth.Workload)."""
+    from hofstadter_hubbard_tsc_gb300.synth import Workload
+    if args.config == "c3":
+        return Workload(W=4, L=48, n_elec=176, m=4000, model="tj", J=0.4, phi=1.0 / 6.0)
+    if args.config == "c4":
+        return Workload(W=6, L=24, n_elec=132, m=6000, U=8.0, phi=1.0 / 3.0)
+    return Workload(W=args.W, L=args.L, n_elec=args.ne, m=args.m)
+
+
 def to_oracle(wl):
     """The workload in the oracle's types (CPU baseline and parity check only)."""
     from oracle import blocks as OB
@@ -189,7 +203,7 @@ def to_oracle(wl):
             ob.sectors.append(sec)
         return ob
 
-    lat = Lattice(wl.W, wl.L, U=wl.U, phi=wl.phi)
+    lat = Lattice(wl.W, wl.L, model=wl.model, U=wl.U, J=wl.J, phi=wl.phi)
     sup = OB.Super(wl.sup.sys_len, wl.sup.env_len,
                    [OB.SSector(s.sys_num_up, s.sys_num_down, s.env_num_up, s.env_num_down, s.sys_dim, s.env_dim)
                     for s in wl.sup.subs])
@@ -203,7 +217,7 @@ def cpu_matvec_timer(wl, psi_flat, nrep):
     from oracle.sites import SiteOps
     sys_, env, sbs, ebs, geo, sup = to_oracle(wl)
     hmerge(sys_, env, geo)
-    st = SiteOps("hubbard")
+    st = SiteOps(wl.model)
     vin = allocate_wave(sup)
     vin.set_flat(psi_flat)
     vout = allocate_wave(sup)
@@ -273,10 +287,9 @@ def sweep_bench(dev, args):
 
 
 def run_reference(args, rank, ws, dist):
-    from hofstadter_hubbard_tsc_gb300.synth import Workload
     if rank != 0:
         return
-    wl = Workload(W=args.W, L=args.L, n_elec=args.ne, m=args.m)
+    wl = make_workload(args)
     rng = np.random.default_rng(1)
     psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
     steps = max(1, min(args.steps, 3))
@@ -314,11 +327,10 @@ def main():
     from hofstadter_hubbard_tsc_gb300 import _lib
     from hofstadter_hubbard_tsc_gb300.device import Device, DWave
     from hofstadter_hubbard_tsc_gb300.superblock import Superblock
-    from hofstadter_hubbard_tsc_gb300.synth import Workload
 
     prec = PREC[args.precision]
     t0 = time.perf_counter()
-    wl = Workload(W=args.W, L=args.L, n_elec=args.ne, m=args.m)
+    wl = make_workload(args)
     dev = Device(local)
     sb = Superblock(dev, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo, precision=prec)
     setup_s = time.perf_counter() - t0
@@ -466,7 +478,7 @@ def main():
         dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, prec))
         hmx = w_out.download()
         line["rel_err_vs_fp64_gpu"] = float(np.linalg.norm(hmx - h64) / np.linalg.norm(h64))
-    if rank == 0 and not args.no_sweep:
+    if rank == 0 and not args.no_sweep and args.config == "c2":
         line["sweep"] = sweep_bench(dev, args)
     if args.energy_check:
         rs = np.random.default_rng(7)

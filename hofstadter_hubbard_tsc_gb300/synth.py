@@ -1,6 +1,8 @@
 """Seeded synthetic superblocks with the sector structure of a real DMRG step.
 
-Used by bench.py when a workload is too large to grow with a full sweep: a
+Used by bench.py when a workload is too large to grow with a full sweep (the
+4x32 Hubbard cylinder at m = 2000, the 4x48 t-J cylinder at m = 4000, the 6x24
+Hubbard cylinder at m = 6000): a
 mid-chain superblock of a W x L cylinder keeps m multiplets per block, spread
 over (N, 2S) block sectors with a Gaussian profile in N around the filling and
 a profile (2S+1) exp(-S(S+1)/(2 s^2)) in S.  The profile was read off a real
@@ -11,7 +13,9 @@ largest 123 multiplets).  Operator entries are N(0,1) complex (re, im ~ N(0, 1/2
 Hamiltonians are Hermitian.  The term list and every quantum-number rule come
 from the real geometry (hmerge / model_wave), so the task structure and FLOP
 count of the matvec are those of the physical superblock; only the numbers in
-the blocks are random.
+the blocks are random.  t-J blocks have no doubly occupied sites (N <= sites)
+and carry, besides the hopping operators, the rank-1 spin operator spin_sd
+and the rank-0 density num_sn of their boundary sites.
 """
 import numpy as np
 
@@ -20,13 +24,14 @@ from .sites import SiteOperators
 from .lattice import SquareLattice
 
 
-def block_sectors(n_sites, n_fill, m, rng, sigma_n=2.5, s_scale=1.5, max_dim=None):
-    """(N, 2S, dim) of a block that keeps m multiplets."""
+def block_sectors(n_sites, n_fill, m, rng, sigma_n=2.5, s_scale=1.5, max_dim=None, tj=False):
+    """(N, 2S, dim) of a block that keeps m multiplets (tj: at most one
+    electron per site)."""
     lo = max(0, int(n_fill - 4 * sigma_n))
-    hi = min(2 * n_sites, int(n_fill + 4 * sigma_n) + 1)
+    hi = min(n_sites if tj else 2 * n_sites, int(n_fill + 4 * sigma_n) + 1)
     cands, w = [], []
     for N in range(lo, hi + 1):
-        smax = min(N, 2 * n_sites - N)
+        smax = N if tj else min(N, 2 * n_sites - N)
         for S2 in range(N % 2, smax + 1, 2):
             s = S2 / 2.0
             wt = np.exp(-((N - n_fill) ** 2) / (2 * sigma_n ** 2)) * (2 * s + 1) * np.exp(-s * (s + 1) / (2 * s_scale ** 2))
@@ -71,6 +76,19 @@ def synthetic_model(length, sectors, slots, rng, names=("elec_up", "elec_down"))
                     subs.append(SubBlock(N, S2, dd, _rand(rng, dims[tgt], d)))
         return TotalBlock(length, up_dif, 1, subs)
 
+    def spin():
+        # rank 1: 2S -> 2S + dd, dd in {-2, 0, 2}, no 0 -> 0
+        subs = []
+        for (N, S2, d) in sectors:
+            for dd in (-2, 0, 2):
+                tgt = (N, S2 + dd)
+                if tgt in dims and S2 + dd >= 0 and not (S2 == 0 and dd == 0):
+                    subs.append(SubBlock(N, S2, dd, _rand(rng, dims[tgt], d)))
+        return TotalBlock(length, 0, 2, subs)
+
+    def density():
+        return TotalBlock(length, 0, 0, [SubBlock(N, S2, 0, _herm(rng, d)) for (N, S2, d) in sectors])
+
     sub = {}
     for k in range(1, slots + 1):
         d = {}
@@ -78,6 +96,10 @@ def synthetic_model(length, sectors, slots, rng, names=("elec_up", "elec_down"))
             d["elec_up"] = ndia(+1)
         if "elec_down" in names:
             d["elec_down"] = ndia(-1)
+        if "spin_sd" in names:
+            d["spin_sd"] = spin()
+        if "num_sn" in names:
+            d["num_sn"] = density()
         sub[k] = d
     return TotalModel(length, ham, sub)
 
@@ -85,30 +107,40 @@ def synthetic_model(length, sectors, slots, rng, names=("elec_up", "elec_down"))
 class Workload:
     """A synthetic mid-chain superblock: models, bases, super basis, geometry."""
 
-    def __init__(self, W=4, L=32, n_elec=112, m=2000, U=8.0, phi=0.25, seed=20261203, sys_len=None):
+    def __init__(self, W=4, L=32, n_elec=112, m=2000, U=8.0, phi=0.25, seed=20261203, sys_len=None,
+                 model="hubbard", J=0.0):
         self.W, self.L, self.n_elec, self.m, self.U, self.phi, self.seed = W, L, n_elec, m, U, phi, seed
+        self.model, self.J = model, J
+        tj = model == "tj"
+        if tj:
+            self.U = U = 0.0
         rng = np.random.default_rng(seed)
-        self.lat = SquareLattice(W, L, U=U, phi=phi)
+        self.lat = SquareLattice(W, L, model=model, U=U, J=J, phi=phi)
         N = self.lat.N
         ls = N // 2 - 1 if sys_len is None else sys_len
         le = N - ls - 2
         fill = n_elec / N
-        self.sys_sectors = block_sectors(ls, fill * ls, m, rng)
-        self.env_sectors = block_sectors(le, fill * le, m, rng)
-        self.sys = synthetic_model(ls, self.sys_sectors, max(1, self.lat.nleg11[ls]), rng)
-        self.env = synthetic_model(le, self.env_sectors, max(1, self.lat.nleg11[le]), rng)
-        st = SiteOperators("hubbard")
+        names = ("elec_up", "elec_down", "spin_sd", "num_sn") if tj else ("elec_up", "elec_down")
+        self.sys_sectors = block_sectors(ls, fill * ls, m, rng, tj=tj)
+        self.env_sectors = block_sectors(le, fill * le, m, rng, tj=tj)
+        self.sys = synthetic_model(ls, self.sys_sectors, max(1, self.lat.nleg11[ls]), rng, names)
+        self.env = synthetic_model(le, self.env_sectors, max(1, self.lat.nleg11[le]), rng, names)
+        st = SiteOperators(model)
         self.sys_bs = get_basis(self.sys.ham, st.sz)
         self.env_bs = get_basis(self.env.ham, st.sz)
         self.sup = get_super_basis(self.sys_bs, self.env_bs, n_elec, 0)
         self.geo = self.lat.geometry(ls, le)
-        self.name = f"hubbard-cylinder-{W}x{L}-phi{phi:g}-U{U:g}-Ne{n_elec}-m{m}-midchain"
+        if tj:
+            self.name = f"tj-cylinder-{W}x{L}-phi{phi:.4g}-J{J:g}-Ne{n_elec}-m{m}-midchain"
+        else:
+            self.name = f"hubbard-cylinder-{W}x{L}-phi{phi:.4g}-U{U:g}-Ne{n_elec}-m{m}-midchain"
 
     def describe(self):
         return {
             "workload": self.name,
-            "lattice": f"{self.W}x{self.L} cylinder (periodic y, open x), Landau gauge",
-            "phi": self.phi, "U": self.U, "t": 1.0, "n_elec": self.n_elec, "kept_multiplets": self.m,
+            "lattice": f"{self.W}x{self.L} {'ladder' if self.W == 2 else 'cylinder (periodic y, open x)'}, "
+                       f"Landau gauge, {self.model}",
+            "phi": self.phi, "U": self.U, "J": self.J, "t": 1.0, "n_elec": self.n_elec, "kept_multiplets": self.m,
             "sys_len": self.sys.len, "env_len": self.env.len,
             "block_sectors": [len(self.sys_sectors), len(self.env_sectors)],
             "enlarged_dims": [self.sys_bs.dim, self.env_bs.dim],

@@ -1,0 +1,37 @@
+"""Synthetic mid-chain superblocks of the matvec configurations (Hubbard and
+t-J, the shapes of the m = 2000 / 4000 / 6000 workloads at small m): the GPU
+FP64 model_wave against the oracle's, and both split precisions against the
+FP64 path."""
+import numpy as np
+import pytest
+
+import bench
+from hofstadter_hubbard_tsc_gb300 import _lib
+from hofstadter_hubbard_tsc_gb300.superblock import Superblock
+from hofstadter_hubbard_tsc_gb300.synth import Workload
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "hubbard-4x6": dict(W=4, L=6, n_elec=20, m=60, phi=1.0 / 3.0),
+    "tj-2x12": dict(W=2, L=12, n_elec=20, m=160, model="tj", J=0.4, phi=1.0 / 6.0),
+    "tj-4x6": dict(W=4, L=6, n_elec=22, m=60, model="tj", J=0.4, phi=1.0 / 6.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_synthetic_matvec(device, name):
+    wl = Workload(**CASES[name])
+    sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
+    rng = np.random.default_rng(5)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    sb.w_in.upload(psi)
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
+    gpu = sb.w_out.download()
+    _, ref = bench.cpu_matvec_timer(wl, psi, 1)
+    assert np.linalg.norm(gpu - ref) / np.linalg.norm(ref) < 1e-12
+    for prec, tol in ((_lib.HH_PREC_BF16X6, 5e-6), (_lib.HH_PREC_BF16X3, 2e-5)):
+        device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, prec))
+        got = sb.w_out.download()
+        assert np.linalg.norm(got - gpu) / np.linalg.norm(gpu) < tol, (prec, name)
+    sb.free()
