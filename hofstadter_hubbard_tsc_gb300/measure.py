@@ -16,6 +16,15 @@ environment half (the cross part of Get_density_cor, code/correlation.f90:43):
 Re <phi_a|chi_b> with chi_b = (1 x O_b) psi, one dot product per pair on the
 device.  Sites are numbered like the reference's output: system block site i
 is site i, environment block site j is site N - j + 1.
+
+Cross-cut spin correlations <S_a . S_b> (the spin part of Get_spin_cor,
+code/correlation.f90): the rank-1 site operator sd is carried to its block
+with the ndia embeddings and truncation (update_site_ndia, update_block_ndia,
+update_trun_ndia, code/update.f90), and each pair is one matvec of a one-term
+plan of the kernel that carries the Hamiltonian's S.S bond in that geometry
+(block-block, block-site, site-block, site-site; the environment operator
+through block_transfer_trans); that term holds J S.S as jd = -sqrt(3) J
+times the unit-coefficient term, so <S_a . S_b> = -sqrt(3) <psi|T_ab psi>.
 """
 import ctypes as C
 
@@ -32,12 +41,18 @@ def _embed(dev, mode, op, dbasis, side):
     return DBlock.from_handle(dev, h)
 
 
-def _carry(dev, op, i, length, bases, truns, side):
-    """Operator of block site i in the truncated block of `length` sites."""
-    cur = op if i <= 1 else update_trun(dev, _embed(dev, 1, op, bases[i][1], side), truns[i], dia=True)
+def _carry(dev, op, i, length, bases, truns, side, rank1=False):
+    """Operator of block site i in the truncated block of `length` sites
+    (rank1: a boson operator of rank 1, through the ndia embeddings)."""
+    site_mode, block_mode = (3, 2) if rank1 else (1, 0)
+    dia = not rank1
+    cur = op if i <= 1 else update_trun(dev, _embed(dev, site_mode, op, bases[i][1], side), truns[i], dia=dia)
     for L in range(i + 1, length + 1):
-        cur = update_trun(dev, _embed(dev, 0, cur, bases[L][1], side), truns[L], dia=True)
+        cur = update_trun(dev, _embed(dev, block_mode, cur, bases[L][1], side), truns[L], dia=dia)
     return cur
+
+
+SPIN_NORM = -np.sqrt(3.0)  # <S_a . S_b> per unit-coefficient sd x sd term
 
 
 class Measurement:
@@ -53,11 +68,12 @@ class Measurement:
         self.env_bs = dmrg.env_bases[sup.env_len][1]
         self.Ls, self.Le = sup.sys_len - 1, sup.env_len - 1
 
-    def _apply(self, kind, op0, op1=None):
+    def _apply(self, kind, op0, op1=None, trans1=0):
         """(one term) psi as a new device wave."""
         dev, w = self.dev, self.wave
         t = (_lib.HHTerm * 1)()
-        t[0] = _lib.HHTerm(kind, ord("B"), ord("B"), 0, 0, op0.h, op1.h if op1 is not None else None, 1.0, 0.0)
+        t[0] = _lib.HHTerm(kind, ord("B"), ord("B"), 0, trans1, op0.h, op1.h if op1 is not None else None, 1.0,
+                           0.0)
         plan = C.c_void_p()
         dev.check(dev.lib.hh_plan_create(dev.h, self.sys_bs.h, self.env_bs.h, w.h, 1, t, C.byref(plan)))
         out = DWave(dev, w.layout, w.sys_len, w.env_len)
@@ -102,4 +118,30 @@ class Measurement:
         m = np.array([[va[a][1].dot(vb[b][1]) for b in sb] for a in sa])
         for v in {id(x[1]): x[1] for x in list(va.values()) + list(vb.values())}.values():
             v.free()
+        return sa, sb, m
+
+    def spin_correlations(self):
+        """<S_a . S_b>, a on the system half, b on the environment half:
+        (sites_a, sites_b, matrix)."""
+        d, dev, N = self.d, self.dev, self.N
+        sd = d.d_st["sd"]
+        a_ops = [(i, _carry(dev, sd, i, self.Ls, d.sys_bases, d.sys_truns, 0, rank1=True))
+                 for i in range(1, self.Ls + 1)] + [(self.Ls + 1, None)]
+        b_ops = [(N - self.Le, None)] + [(N - j + 1, _carry(dev, sd, j, self.Le, d.env_bases, d.env_truns, 1,
+                                                            rank1=True)) for j in range(1, self.Le + 1)]
+        sa = [a for a, _ in a_ops]
+        sb = sorted(b for b, _ in b_ops)
+        m = np.zeros((len(sa), len(sb)))
+        for ia, (a, oa) in enumerate(a_ops):
+            for b, ob in b_ops:
+                if oa is not None and ob is not None:
+                    phi = self._apply(_lib.BLOCK_VEC_BLOCK_NDIA, oa, ob, trans1=1)
+                elif oa is not None:
+                    phi = self._apply(_lib.BLOCK_VEC_SITE_NDIA, oa, sd)
+                elif ob is not None:
+                    phi = self._apply(_lib.SITE_VEC_BLOCK_NDIA, sd, ob, trans1=1)
+                else:
+                    phi = self._apply(_lib.SITE_VEC_SITE_NDIA, sd, sd)
+                m[ia, sb.index(b)] = SPIN_NORM * self.wave.dot(phi)
+                phi.free()
         return sa, sb, m

@@ -202,3 +202,62 @@ def hubbard_density_correlations(lat, n_up, n_dn):
     dens = p @ n
     corr = (n * p[:, None]).T @ n
     return float(e0), dens, corr
+
+
+def _pair_hop(confs, a, b):
+    """c+_a c_b (a != b) on one spin species' configurations, with the sign
+    of the occupied sites strictly between a and b."""
+    idx = {c: n for n, c in enumerate(confs)}
+    lo, hi = min(a, b), max(a, b)
+    mask = ((1 << hi) - 1) & ~((1 << (lo + 1)) - 1)
+    rows, cols, vals = [], [], []
+    for n, c in enumerate(confs):
+        if (c >> b) & 1 and not (c >> a) & 1:
+            c2 = c ^ (1 << a) ^ (1 << b)
+            rows.append(idx[c2]); cols.append(n)
+            vals.append(-1.0 if bin(c & mask).count("1") % 2 else 1.0)
+    m = len(confs)
+    return sp.csr_matrix((vals, (rows, cols)), shape=(m, m), dtype=np.complex128)
+
+
+def hubbard_spin_correlations(lat, n_up, n_dn):
+    """Lowest state of the (n_up, n_dn) sector: energy, <S_i.S_j> and
+    3 <S^z_i S^z_j> (equal for a singlet), sites in lattice order.
+    S_i.S_j = S^z_i S^z_j + (S^+_i S^-_j + S^-_i S^+_j) / 2 with
+    S^+_i S^-_j = c+_iu c_id c+_jd c_ju = -(c+_iu c_ju)(c+_jd c_id) for i != j
+    (the up bilinear acts on the up configurations, the down one on the down
+    configurations, same ordering as the Hamiltonian here); for i = j,
+    S_i.S_i = 3/4 (n_i,u - n_i,d)^2."""
+    N = lat.N
+    cu = _configs(N, n_up)
+    cd = _configs(N, n_dn)
+    hu = _spin_hop(lat, cu)
+    hd = _spin_hop(lat, cd)
+    H = sp.kron(hu, sp.identity(len(cd)), format="csr") + sp.kron(sp.identity(len(cu)), hd, format="csr")
+    au = np.array(cu, dtype=np.int64)
+    ad = np.array(cd, dtype=np.int64)
+    if lat.U != 0.0:
+        dbl = np.array([[bin(int(x & y)).count("1") for y in ad] for x in au], dtype=np.float64).ravel()
+        H = H + sp.diags(lat.U * dbl)
+    if H.shape[0] <= 2000:
+        w, v = np.linalg.eigh(H.toarray())
+        e0, psi = w[0], v[:, 0]
+    else:
+        w, v = spla.eigsh(H, k=1, which="SA", tol=1e-13)
+        e0, psi = w[0], v[:, 0]
+    p = np.abs(psi) ** 2
+    occ_u = np.array([[(c >> s) & 1 for s in range(N)] for c in au], dtype=np.float64)
+    occ_d = np.array([[(c >> s) & 1 for s in range(N)] for c in ad], dtype=np.float64)
+    sz = 0.5 * (occ_u[:, None, :] - occ_d[None, :, :]).reshape(-1, N)
+    szsz = (sz * p[:, None]).T @ sz
+    ss = np.array(szsz, dtype=np.float64)
+    for i in range(N):
+        ss[i, i] = 3.0 * szsz[i, i]
+        for j in range(N):
+            if i == j:
+                continue
+            # S+_i S-_j and its conjugate S-_i S+_j = -(c+_id c_jd)(c+_ju c_iu)
+            pm = -sp.kron(_pair_hop(cu, i, j), _pair_hop(cd, j, i), format="csr")
+            mp = -sp.kron(_pair_hop(cu, j, i), _pair_hop(cd, i, j), format="csr")
+            ss[i, j] += 0.5 * float(np.real(np.vdot(psi, (pm + mp) @ psi)))
+    return float(e0), ss, 3.0 * szsz

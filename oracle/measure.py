@@ -15,11 +15,22 @@ with phi_a = (O_a x 1) psi and chi_b = (1 x O_b) psi, <psi|O_a O_b|psi> =
 Re <phi_a|chi_b>, since the two operators act on different halves and are
 Hermitian.  Sites are numbered like the reference's output: system block site
 i is site i, environment block site j is site N - j + 1.
+
+Cross-cut spin correlations <S_a . S_b> (the spin part of Get_spin_cor,
+code/correlation.f90): the rank-1 operator sd of site a is carried to its
+block with update_site_ndia / update_block_ndia / update_trun_ndia, and the
+pair is applied by the kernel of the Hamiltonian's own S.S bond term of that
+geometry (block_vec_block_ndia, block_vec_site_ndia, site_vec_block_ndia,
+site_vec_site_ndia with the environment block through block_transfer_trans,
+code/mat_vec.f90:3509-3600), which carries J S.S as jd = -sqrt(3) J times
+the unit-coefficient term: <S_a . S_b> = -sqrt(3) <psi|T_ab psi>.
 """
 import numpy as np
 
-from .blocks import update_site_dia, update_block_dia, update_trun_dia, wave_product
-from .matvec import block_vec_dia, vec_block_dia, site_vec_site_dia
+from .blocks import (update_site_dia, update_block_dia, update_trun_dia, wave_product, update_site_ndia,
+                     update_block_ndia, update_trun_ndia, block_transfer_trans)
+from .matvec import (block_vec_dia, vec_block_dia, site_vec_site_dia, block_vec_block_ndia, block_vec_site_ndia,
+                     site_vec_block_ndia, site_vec_site_ndia)
 
 
 def _carry(op, i, length, bases, truns):
@@ -75,4 +86,48 @@ def cross_correlations(d, name_a="num_elec", name_b="num_elec"):
     sa = sorted(s for s, (side, _) in va.items() if side == 0)
     sb = sorted(s for s, (side, _) in vb.items() if side == 1)
     m = np.array([[wave_product(va[a][1], vb[b][1]) for b in sb] for a in sa])
+    return sa, sb, m
+
+
+def _carry_ndia(op, i, length, bases, truns, side):
+    """Rank-1 (boson) operator of block site i in the truncated block of
+    `length` sites (the ndia counterpart of _carry)."""
+    cur = op.copy() if i <= 1 else update_trun_ndia(update_site_ndia(op, bases[i], "B", side), truns[i])
+    for L in range(i + 1, length + 1):
+        cur = update_trun_ndia(update_block_ndia(cur, bases[L], "B", side), truns[L])
+    return cur
+
+
+SPIN_NORM = -np.sqrt(3.0)  # <S_a . S_b> per unit-coefficient sd x sd term
+
+
+def spin_correlations(d):
+    """<S_a . S_b> for a on the system half and b on the environment half of
+    the current superblock of an oracle DMRG ``d``: (sites_a, sites_b, matrix)."""
+    wave = d.wave
+    N = d.lat.N
+    sd = d.st.sd
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    # (site, block operator or None for the middle site)
+    a_ops = [(i, _carry_ndia(sd, i, Ls, d.sys_bases, d.sys_truns, "sys")) for i in range(1, Ls + 1)]
+    a_ops.append((Ls + 1, None))
+    b_ops = [(N - Le, None)]
+    b_ops += [(N - j + 1, block_transfer_trans(_carry_ndia(sd, j, Le, d.env_bases, d.env_truns, "env")))
+              for j in range(1, Le + 1)]
+    sa = [a for a, _ in a_ops]
+    sb = sorted(b for b, _ in b_ops)
+    m = np.zeros((len(sa), len(sb)))
+    for ia, (a, oa) in enumerate(a_ops):
+        for b, ob in b_ops:
+            phi = wave.zeros_like()
+            if oa is not None and ob is not None:
+                block_vec_block_ndia(oa, "B", ob, "B", sys_bs, env_bs, wave, phi, 1.0)
+            elif oa is not None:
+                block_vec_site_ndia(oa, "B", sd, "B", sys_bs, env_bs, wave, phi, 1.0)
+            elif ob is not None:
+                site_vec_block_ndia(sd, "B", ob, "B", sys_bs, env_bs, wave, phi, 1.0)
+            else:
+                site_vec_site_ndia(sd, "B", sd, "B", sys_bs, env_bs, wave, phi, 1.0)
+            m[ia, sb.index(b)] = SPIN_NORM * wave_product(wave, phi)
     return sa, sb, m

@@ -46,3 +46,17 @@ def test_profile_sum_rules_truncated(device):
     assert np.all(np.isfinite(c))
     # sum_b <n_a n_b> <= <n_a> * max particles on the environment side
     assert np.all(c.sum(axis=1) <= n[np.array(sa) - 1] * 2 * len(sb) + 1e-8)
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_spin_correlations_exact(device, precision):
+    """Cross-cut <S_a . S_b> on the GPU state (rank-1 operators carried with
+    the ndia embeddings, one-term S.S plans) against exact diagonalisation."""
+    W, L, ne, U, phi = 2, 4, 6, 8.0, 0.25
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    d.run(sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    _, ss, _ = ed.hubbard_spin_correlations(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
+    sa, sb, m = Measurement(d).spin_correlations()
+    np.testing.assert_allclose(m, ss[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)

@@ -56,3 +56,18 @@ def test_measurements_exact(W, L, ne, U, phi):
     np.testing.assert_allclose(prof, dens, atol=1e-6)
     sa, sb, m = om.cross_correlations(d)
     np.testing.assert_allclose(m, corr[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_spin_correlations_exact(W, L, ne, U, phi):
+    """Cross-cut <S_a . S_b> of the oracle (carried rank-1 operators, the S.S
+    bond kernels, -sqrt(3) normalisation) against the exact ground state; the
+    exact state is a singlet (<S.S> = 3 <Sz Sz>)."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    _, ss, szsz3 = ed.hubbard_spin_correlations(lat, ne // 2, ne // 2)
+    np.testing.assert_allclose(ss, szsz3, atol=1e-12)
+    _, d = _dmrg(lat, ne, sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    sa, sb, m = om.spin_correlations(d)
+    np.testing.assert_allclose(m, ss[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
