@@ -47,6 +47,12 @@ struct Arena {
   }
 };
 
+// Stage-1 tiles are at most 64 wide: all of stage 1 then runs on the 64-wide
+// kernel (256 TMEM columns, two CTAs per SM), where one CTA's T-image
+// epilogue overlaps the other's MMAs; 128-wide stage-1 tiles ran one CTA per
+// SM with the epilogue exposed (0.129 against 0.116 ms at m = 2000).
+constexpr int kStage1N = 64;
+
 // MMA cycles of one 16-k chunk of a tile, in units of a plain 128-wide
 // chunk: a K = 16 MMA costs about max(45, N/2) cycles whatever its M; plain
 // tiles issue four of width ntile per part pair, stacked tiles one of width
@@ -218,8 +224,8 @@ int build_tc_plan(hh_plan* p) {
     ImgRef ai = op_img(c.A, 0, c.M, c.Ka, 1.0, 0.0);
     ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.Kb, 1);
     for (int m0 = 0; m0 < c.M; m0 += 128)
-      for (int n0 = 0; n0 < c.Kb; n0 += 128) {
-        const int ntile = k16(std::min(128, c.Kb - n0));
+      for (int n0 = 0; n0 < c.Kb; n0 += kStage1N) {
+        const int ntile = k16(std::min(kStage1N, c.Kb - n0));
         tc::Tile tl{};
         tl.seg0 = (int)segs.size();
         tl.nseg = 1;
@@ -227,7 +233,7 @@ int build_tc_plan(hh_plan* p) {
         tl.mode = 1;
         tl.ntile = ntile;
         tl.mrem = std::min(128, c.M - m0);
-        tl.nrem = std::min(128, c.Kb - n0);
+        tl.nrem = std::min(kStage1N, c.Kb - n0);
         tl.out = tag(T.off, 2);
         tl.t_rpad = rpad(c.M);
         tl.m0 = m0;
@@ -322,9 +328,9 @@ int build_tc_plan(hh_plan* p) {
     }
 
   // ------------------------------------------------------- tile order
-  // Stage 1 (thousands of short tiles) is split into tiles at most 64 wide,
-  // which run on the 64-wide kernels (256 TMEM columns, two CTAs per SM),
-  // followed by the wider ones, both on the persistent kernel, where CTA c of
+  // Stage 1 (thousands of short tiles, at most kStage1N wide) runs on the
+  // 64-wide kernels (256 TMEM columns, two CTAs per SM; wider tiles, if any,
+  // follow on the 128-wide kernel), on the persistent kernel, where CTA c of
   // G resident CTAs takes tiles c, c + G, c + 2G, ...: within each part its
   // tiles go longest first (MMA chunks x N, plus a fixed epilogue share), in
   // a snake over the CTAs, so that every CTA receives a near-equal share.
