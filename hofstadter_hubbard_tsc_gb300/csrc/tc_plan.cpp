@@ -84,7 +84,7 @@ namespace tc {
 // (64-row halves when stacked).
 void finish_tile(Tile& t, const Seg* segs) {
   t.nchunk = 0;
-  bool stack = t.mode == 0 && t.mrem <= 64 && t.nseg > 0, pa = t.nseg > 0, pb = t.nseg > 0;
+  bool stack = t.mrem <= 64 && t.nseg > 0, pa = t.nseg > 0, pb = t.nseg > 0;
   const long long a_plane = t.nseg > 0 ? segs[t.seg0].a_plane : 0;
   for (int si = 0; si < t.nseg; ++si) {
     const Seg& sg = segs[t.seg0 + si];
