@@ -262,8 +262,8 @@ int build_tc_plan(hh_plan* p) {
     const int M = c0.M, N = c0.N;
     const hh_wsec& w = L->secs[c0.k_out];
     for (int m0 = 0; m0 < M; m0 += 128)
-      for (int n0 = 0; n0 < N; n0 += 128) {
-        const int ntile = k16(std::min(128, N - n0));
+      for (int n0 = 0; n0 < N; n0 += 64) {
+        const int ntile = k16(std::min(64, N - n0));
         tc::Tile tl{};
         tl.seg0 = (int)segs.size();
         tl.cseg0 = (int)csegs.size();
@@ -307,7 +307,7 @@ int build_tc_plan(hh_plan* p) {
         tl.mode = 0;
         tl.ntile = ntile;
         tl.mrem = std::min(128, M - m0);
-        tl.nrem = std::min(128, N - n0);
+        tl.nrem = std::min(64, N - n0);
         tl.out = w.off + (long long)(c0.ocol + n0) * w.sdim + c0.orow + m0;
         tl.ldo = w.sdim;
         tl.m0 = m0;
@@ -361,7 +361,7 @@ int build_tc_plan(hh_plan* p) {
     std::copy(out.begin(), out.end(), tl.begin() + lo);
   };
   const int n1n = split_narrow(tiles1);
-  const int n2n = 0;  // narrow stage-2 tiles on the two-CTA kernels: 0.29 against 0.24 ms (two tails)
+  const int n2n = split_narrow(tiles2);
   auto longest_first = [](std::vector<tc::Tile>& tl, size_t lo, size_t hi) {
     std::stable_sort(tl.begin() + lo, tl.begin() + hi,
                      [](const tc::Tile& a, const tc::Tile& b) { return tile_cost(a) > tile_cost(b); });
