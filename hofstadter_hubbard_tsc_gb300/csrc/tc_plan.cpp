@@ -47,11 +47,13 @@ struct Arena {
   }
 };
 
-// Stage-1 tiles are at most 64 wide: all of stage 1 then runs on the 64-wide
-// kernel (256 TMEM columns, two CTAs per SM), where one CTA's T-image
-// epilogue overlaps the other's MMAs; 128-wide stage-1 tiles ran one CTA per
-// SM with the epilogue exposed (0.129 against 0.116 ms at m = 2000).
-constexpr int kStage1N = 64;
+// Tiles are at most 64 wide (both stages): everything then runs on the
+// 64-wide kernels (256 TMEM columns, two CTAs per SM), where one CTA's
+// epilogue and pipeline fill overlap the other's MMAs.  A stacked tile costs
+// the same MMA cycles cut in two halves (two MMAs of width 128 = one of 256);
+// 128-wide tiles ran one CTA per SM with the epilogue exposed (m = 2000:
+// stage 1 0.129 -> 0.116 ms, stage 2 + copy terms 0.223 -> 0.205 ms).
+constexpr int kTileN = 64;
 
 // MMA cycles of one 16-k chunk of a tile, in units of a plain 128-wide
 // chunk: a K = 16 MMA costs about max(45, N/2) cycles whatever its M; plain
@@ -224,8 +226,8 @@ int build_tc_plan(hh_plan* p) {
     ImgRef ai = op_img(c.A, 0, c.M, c.Ka, 1.0, 0.0);
     ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.Kb, 1);
     for (int m0 = 0; m0 < c.M; m0 += 128)
-      for (int n0 = 0; n0 < c.Kb; n0 += kStage1N) {
-        const int ntile = k16(std::min(kStage1N, c.Kb - n0));
+      for (int n0 = 0; n0 < c.Kb; n0 += kTileN) {
+        const int ntile = k16(std::min(kTileN, c.Kb - n0));
         tc::Tile tl{};
         tl.seg0 = (int)segs.size();
         tl.nseg = 1;
@@ -233,7 +235,7 @@ int build_tc_plan(hh_plan* p) {
         tl.mode = 1;
         tl.ntile = ntile;
         tl.mrem = std::min(128, c.M - m0);
-        tl.nrem = std::min(kStage1N, c.Kb - n0);
+        tl.nrem = std::min(kTileN, c.Kb - n0);
         tl.out = tag(T.off, 2);
         tl.t_rpad = rpad(c.M);
         tl.m0 = m0;
@@ -262,8 +264,8 @@ int build_tc_plan(hh_plan* p) {
     const int M = c0.M, N = c0.N;
     const hh_wsec& w = L->secs[c0.k_out];
     for (int m0 = 0; m0 < M; m0 += 128)
-      for (int n0 = 0; n0 < N; n0 += 64) {
-        const int ntile = k16(std::min(64, N - n0));
+      for (int n0 = 0; n0 < N; n0 += kTileN) {
+        const int ntile = k16(std::min(kTileN, N - n0));
         tc::Tile tl{};
         tl.seg0 = (int)segs.size();
         tl.cseg0 = (int)csegs.size();
@@ -307,7 +309,7 @@ int build_tc_plan(hh_plan* p) {
         tl.mode = 0;
         tl.ntile = ntile;
         tl.mrem = std::min(128, M - m0);
-        tl.nrem = std::min(64, N - n0);
+        tl.nrem = std::min(kTileN, N - n0);
         tl.out = w.off + (long long)(c0.ocol + n0) * w.sdim + c0.orow + m0;
         tl.ldo = w.sdim;
         tl.m0 = m0;
@@ -328,17 +330,17 @@ int build_tc_plan(hh_plan* p) {
     }
 
   // ------------------------------------------------------- tile order
-  // Stage 1 (thousands of short tiles, at most kStage1N wide) runs on the
+  // Stage 1 (thousands of short tiles, at most kTileN wide) runs on the
   // 64-wide kernels (256 TMEM columns, two CTAs per SM; wider tiles, if any,
   // follow on the 128-wide kernel), on the persistent kernel, where CTA c of
   // G resident CTAs takes tiles c, c + G, c + 2G, ...: within each part its
   // tiles go longest first (MMA chunks x N, plus a fixed epilogue share), in
   // a snake over the CTAs, so that every CTA receives a near-equal share.
-  // Stage 2 (hundreds of long, uneven tiles) stays one list on the 128-wide
-  // kernels, in two orders: longest first for one CTA per tile (the hardware
-  // then hands the next tile to the first free SM: list scheduling; 0.28
-  // against 0.34 ms in plan order at m = 2000), and snake-balanced like
-  // stage 1 for the persistent kernel; the launch autotuner picks.
+  // Stage 2 (long, uneven tiles, at most kTileN wide) is kept in two orders:
+  // longest first for one CTA per tile (the hardware then hands the next
+  // tile to the first free SM: list scheduling; 0.28 against 0.34 ms in plan
+  // order at m = 2000), and snake-balanced like stage 1 for the persistent
+  // kernel; the launch autotuner picks.
   int sms = 148, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
