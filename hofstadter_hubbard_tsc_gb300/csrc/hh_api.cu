@@ -693,9 +693,11 @@ int hh_plan_stats(const hh_plan_t* p, double* c) {
   c[15] = p->tc.ready ? 1.0 : 0.0;
   // kernels of one matvec: FP64 (two segment GEMMs and their reductions of
   // split tiles) and split precision (graph replay: set_io, wave images,
-  // stage 1, zeroing, stage 2, copy terms)
+  // stage 1, zeroing when the stage-2 tiles do not cover the output, stage
+  // 2, copy terms)
   c[16] = 2.0 + (p->stage1.n_red > 0) + (p->stage2.n_red > 0);
-  c[17] = 3.0 + (p->tc.n_cseg > 0) + (p->tc.n_narrow1 > 0) + (p->tc.n_tiles1 > p->tc.n_narrow1) +
+  c[17] = 2.0 + (p->tc.zero_out ? 1.0 : 0.0) + (p->tc.n_cseg > 0) + (p->tc.n_narrow1 > 0) +
+          (p->tc.n_tiles1 > p->tc.n_narrow1) +
           (p->tc.n_narrow2 > 0) + (p->tc.n_tiles2 > p->tc.n_narrow2);
   c[18] = (double)(p->stage1.n_work + p->stage2.n_work);
   c[19] = p->tc.persistent1 ? 1.0 : 0.0;

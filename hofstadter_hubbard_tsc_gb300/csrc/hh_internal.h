@@ -199,6 +199,7 @@ struct hh_tc_plan {
   int n_x_blocks = 0;
   int2* d_c_blocks = nullptr;         // copy-term block list over d_tiles2 (tc_copy_blocks)
   int n_c_blocks = 0;
+  bool zero_out = true;               // stage-2 tiles do not cover the whole output
   int n_tiles1 = 0, n_tiles2 = 0, n_cseg = 0;
   int n_narrow1 = 0, n_narrow2 = 0;  // leading tiles at most 64 wide (64-wide kernels)
   hh::tc::Seg* d_segs = nullptr;
