@@ -91,6 +91,7 @@ SIGNATURES = {
     "hh_matvec_timed": (I, [P, P, P, I, C.POINTER(C.c_float)]),
     "hh_matvec_noalloc": (I, [P, P, P]),
     "hh_tc_selftest": (I, [P, I, I, I, DP, DP, DP, I]),
+    "hh_tc_selftest_hold": (I, [P, I]),
     "hh_density_truncate": (I, [P, P, I, I, I, D, PP, IP, DP, DP, DP]),
     "hh_enlarge_operator": (I, [P, I, P, P, I, I, PP]),
     "hh_ham_add_bond": (I, [P, P, P, P, I, P, DP, I, I]),

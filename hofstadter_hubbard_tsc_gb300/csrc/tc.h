@@ -48,7 +48,9 @@ struct Tile {
   int pack;              // bit 0: every segment's A copy is its whole image height (one copy
                          // of all planes per chunk); bit 1: the same for B with planes ntile rows
   int a_pair, a_im;      // shared memory of A plane q: (q / 2) * a_pair + (q % 2) * a_im bytes
-  int pad;
+  int hold;              // failure-detection test only (0 in every plan): the producer posts the first
+                         // chunk's bytes without issuing its copies, so the bounded waits run out
+                         // (each after 2^12 attempts instead of 2^20) and the CTA reports and unwinds
 };
 
 // Fills a finished tile's nchunk, stack, pack, a_pair and a_im from its

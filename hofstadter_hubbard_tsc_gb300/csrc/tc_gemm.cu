@@ -72,10 +72,18 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
-// bounded wait on an mbarrier phase; returns false when the limit ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Attempts per bounded mbarrier wait.  One try_wait attempt (it may suspend
+// the thread) plus the back-off costs about 5 us on GB300 (measured by the
+// held-tile check: 2^12 attempts in ~20 ms), so a wait gives up after about
+// 5 s: far beyond any legitimate wait here (a tile's MMAs take at most
+// milliseconds) and short enough to report instead of appearing hung.
+constexpr uint32_t kWaitLimit = 1u << 20;
+
+// bounded wait on an mbarrier phase (at most `limit` try_wait attempts);
+// returns false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
   const uint32_t addr = smem_u32(bar);
-  for (uint32_t i = 0; i < (1u << 26); ++i) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -505,6 +513,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
   __syncthreads();
   fence_after();
   const uint32_t tmem = *tslot;
+  const uint32_t lim = t.hold ? (1u << 12) : kWaitLimit;  // attempts per bounded wait
 
   if (warp == 0) {
     if (lane == 0) {
@@ -514,18 +523,21 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
         const Seg sg = segs[t.seg0 + si];
         for (int kc = 0; kc < sg.nkc; ++kc, ++it) {
           const int s = it % nst;
-          if (it >= nst && !mbar_wait(&empty[s], ((it / nst) + 1) & 1)) {
+          if (it >= nst && !mbar_wait(&empty[s], ((it / nst) + 1) & 1, lim)) {
             flag_error(err, 1);
             ok = false;
             break;
           }
-          load_chunk<SPLIT>(smem + s * stage_bytes, a_region, t, sg, kc, &full[s]);
+          if (t.hold && it == 0)  // failure-detection test: bytes announced, never sent
+            mbar_expect_tx(&full[s], 2u * SPLIT * (sg.a_bytes + sg.b_bytes));
+          else
+            load_chunk<SPLIT>(smem + s * stage_bytes, a_region, t, sg, kc, &full[s]);
         }
       }
       // copies still in flight land before the CTA leaves (already done
       // unless a wait gave up)
       for (int j = it > nst ? it - nst : 0; j < it; ++j)
-        if (!mbar_wait(&full[j % nst], (j / nst) & 1)) flag_error(err, 5);
+        if (!mbar_wait(&full[j % nst], (j / nst) & 1, lim)) flag_error(err, 5);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -536,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
         const Seg sg = segs[t.seg0 + si];
         for (int kc = 0; kc < sg.nkc; ++kc, ++it) {
           const int s = it % nst;
-          if (!mbar_wait(&full[s], (it / nst) & 1)) {
+          if (!mbar_wait(&full[s], (it / nst) & 1, lim)) {
             flag_error(err, 2);
             ok = false;
             break;
@@ -555,7 +567,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
     for (int si = 0; si < t.nseg; ++si) total += segs[t.seg0 + si].nkc;
     bool have = total > 0;
     if (have) {
-      if (!mbar_wait(accf, 0)) {
+      if (!mbar_wait(accf, 0, lim)) {
         flag_error(err, 3);
         have = false;
       }

@@ -601,8 +601,25 @@ int tune_tc_plan(hh_plan* p, int reps, double* ms, int split) {
 // ---------------------------------------------------------------------------
 // Self-test of the tensor-core tile path on one dense complex product
 // C = A B (column-major, interleaved complex), used by the unit tests.
+static int tc_selftest_impl(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C,
+                            int precision, bool hold);
+
 extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C,
                               int precision) {
+  return tc_selftest_impl(ctx, M, N, K, A, B, C, precision, false);
+}
+
+// Failure-detection check: a 16 x 16 x 16 product whose first chunk is
+// announced to the copy barrier but never sent, so the kernel's bounded
+// waits run out; the call must return HH_ERR_TIMEOUT with the context still
+// usable.
+extern "C" int hh_tc_selftest_hold(hh_ctx_t* ctx, int precision) {
+  std::vector<double> a(2 * 16 * 16, 0.0), c(2 * 16 * 16, 0.0);
+  return tc_selftest_impl(ctx, 16, 16, 16, a.data(), a.data(), c.data(), precision, true);
+}
+
+static int tc_selftest_impl(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C,
+                            int precision, bool hold) {
   using namespace hh;
   if (!ctx || M < 1 || N < 1 || K < 1 || !A || !B || !C || !split_of(precision)) return HH_ERR_INVALID;
   const long long ia = img_bytes(M, K), ib = img_bytes(N, K);
@@ -661,6 +678,7 @@ extern "C" int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* 
       tl.m0 = m0;
       tl.n0 = n0;
       tc::finish_tile(tl, segs.data());
+      tl.hold = hold ? 1 : 0;
       tiles.push_back(tl);
     }
   e = cudaMalloc(&dtask, sizeof(tk));

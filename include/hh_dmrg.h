@@ -285,6 +285,12 @@ int hh_wave_scale_sectors(hh_wave_t* w, const double* scale);
  * split precision (HH_PREC_BF16X6 or HH_PREC_BF16X3).                     */
 int hh_tc_selftest(hh_ctx_t* ctx, int M, int N, int K, const double* A, const double* B, double* C,
                    int precision);
+/* Failure-detection check of the tensor-core kernels: one tile whose first
+ * chunk is announced to its copy barrier but never sent, so the kernel's
+ * bounded waits run out (short limit) and it unwinds (TMEM freed, no copy in
+ * flight).  Returns HH_ERR_TIMEOUT (hh_last_error names the wait that gave
+ * up); the context stays usable.                                          */
+int hh_tc_selftest_hold(hh_ctx_t* ctx, int precision);
 
 #ifdef __cplusplus
 }

@@ -42,3 +42,19 @@ def test_tc_selftest_rejects_fp64(device):
     st = device.lib.hh_tc_selftest(device.h, 8, 8, 8, z.ctypes.data_as(dp), z.ctypes.data_as(dp),
                                    z.ctypes.data_as(dp), _lib.HH_PREC_FP64)
     assert st == -1
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_BF16X6, _lib.HH_PREC_BF16X3])
+def test_bounded_wait_reports_timeout(device, precision):
+    """A tile whose copy barrier is announced bytes that never arrive: the
+    kernel's bounded waits run out, it unwinds and reports HH_ERR_TIMEOUT,
+    and the context keeps working (the next product is correct)."""
+    import time
+    t0 = time.perf_counter()
+    st = device.lib.hh_tc_selftest_hold(device.h, precision)
+    dt = time.perf_counter() - t0
+    assert st == -5, st
+    assert "bounded" in device.lib.hh_last_error(device.h).decode()
+    assert dt < 30.0, dt
+    err = _run(device, 40, 24, 37, seed=1, precision=precision)
+    assert err < TOL[precision], err
