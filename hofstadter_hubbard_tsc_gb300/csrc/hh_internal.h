@@ -182,7 +182,7 @@ struct hh_contrib {
   double cre, cim;
 };
 
-namespace hh { namespace tc { struct ImgTask; struct Seg; struct Tile; struct IoPtrs; } }
+namespace hh { namespace tc { struct ImgTask; struct Seg; struct Tile; struct IoPtrs; struct TPiece; } }
 
 struct hh_tc_plan {
   bool ready = false;
@@ -195,6 +195,7 @@ struct hh_tc_plan {
   hh::tc::Tile* d_tiles1 = nullptr;
   hh::tc::Tile* d_tiles2 = nullptr;   // stage 2, longest first (one CTA per tile)
   hh::tc::Tile* d_tiles2b = nullptr;  // the same tiles ordered for the persistent kernel
+  hh::tc::TPiece* d_pieces = nullptr; // pieces of the row-packed stage-1 tiles
   int2* d_x_blocks = nullptr;         // wave-image block list (tc_image_blocks)
   int n_x_blocks = 0;
   int2* d_c_blocks = nullptr;         // copy-term block list over d_tiles2 (tc_copy_blocks)

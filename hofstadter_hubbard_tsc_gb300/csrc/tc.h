@@ -16,8 +16,10 @@ struct ImgTask {
   int sbase;
   int ld;
   int rows, kc;    // logical extent (complex)
-  int rpad, k16;   // padded extent (rows to a multiple of 16, k to 16)
+  int rpad, k16;   // padded extent of the image (rows to a multiple of 16, k to 16)
   int trans, conj;
+  int row0, prow;  // image rows [row0, row0 + prow) are this task's (several operators can
+                   // share one image, stacked in rows); one-operator images: 0, rpad
   double cre, cim;
   long long dst;   // absolute address of the image (256-byte aligned)
 };
@@ -51,6 +53,16 @@ struct Tile {
   int hold;              // failure-detection test only (0 in every plan): the producer posts the first
                          // chunk's bytes without issuing its copies, so the bounded waits run out
                          // (each after 2^12 attempts instead of 2^20) and the CTA reports and unwinds
+  int piece0, npiece;    // mode 1, row-packed tiles: rows of several products, routed by the pieces
+                         // [piece0, piece0 + npiece) to their own T images (npiece 0: one product)
+};
+
+// One product's rows inside a row-packed stage-1 tile: tile rows [row0, row0
+// + t_rpad) are rows [0, t_rpad) of the T image at `out` (rows >= `rows` are
+// its zero padding).
+struct TPiece {
+  long long out;
+  int row0, rows, t_rpad, pad;
 };
 
 // Fills a finished tile's nchunk, stack, pack, a_pair and a_im from its
@@ -95,8 +107,9 @@ cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoP
 // b, b + G, ...: the list must be ordered for balance) or one CTA per tile
 // nt: the list's widest tile (<= 64: the 64-wide kernels, two CTAs per SM);
 // split: BF16 parts per operand, 3 (six products) or 2 (three products)
+// d_pieces: the row-packed tiles' pieces (stage 1)
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
                          bool persistent, cudaStream_t s, const tc::IoPtrs* io = nullptr, int nt = 128,
-                         int split = 3);
+                         int split = 3, const tc::TPiece* d_pieces = nullptr);
 
 }  // namespace hh

@@ -208,13 +208,13 @@ __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __rest
   const ImgTask t = tasks[bw.x];
   const double2* src = t.sbase == HH_BASE_IN ? base_in + t.src : reinterpret_cast<const double2*>(t.src);
   uint8_t* dst = reinterpret_cast<uint8_t*>(t.dst);
-  const int rpad = t.rpad, k16 = t.k16;
+  const int rpad = t.rpad, k16 = t.k16, prow = t.prow;
   const size_t plane = (size_t)(rpad >> 3) * 256;
-  const int ngroups = rpad * (k16 >> 3);
+  const int ngroups = prow * (k16 >> 3);
   const int g_end = blocks ? min(ngroups, bw.y + kImgGroupsPerBlock) : ngroups;
   const float fre = (float)t.cre, fim = (float)t.cim;
   for (int idx = bw.y + threadIdx.x; idx < g_end; idx += blockDim.x) {
-    const int r = idx % rpad, k0 = (idx / rpad) * 8;
+    const int r = idx % prow, k0 = (idx / prow) * 8;  // r: row of this task's operator
     __nv_bfloat16 re[3][8], im[3][8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __rest
         im[0][j] = s[0]; im[1][j] = s[1]; im[2][j] = s[2];
       }
     }
-    const size_t o = img_off(rpad, r, k0);
+    const size_t o = img_off(rpad, t.row0 + r, k0);
 #pragma unroll
     for (int p = 0; p < SPLIT; ++p) {
       *reinterpret_cast<uint4*>(dst + o + (size_t)(2 * p) * plane) = pack8(re[p]);
@@ -352,7 +352,8 @@ __device__ __forceinline__ void mma_chunk(uint32_t sa, int a_region, const Tile&
 // reads).
 template <int SPLIT>
 __device__ __forceinline__ void epilogue16(const Tile& t, int row, int c0, const float* re, const float* im,
-                                           const float* cr, const float* cm, double2* base_out) {
+                                           const float* cr, const float* cm, double2* base_out,
+                                           const TPiece* __restrict__ pieces) {
   if (t.mode == 0) {
     if (row < t.mrem) {
       double2* O = base_out + t.out;
@@ -364,24 +365,36 @@ __device__ __forceinline__ void epilogue16(const Tile& t, int row, int c0, const
     }
     return;
   }
-  const int r = t.m0 + row;
-  if (r >= t.t_rpad) return;
+  int r = t.m0 + row;        // row of the T image
+  bool vrow = row < t.mrem;  // a row of the product (else zero padding)
   uint8_t* img = reinterpret_cast<uint8_t*>(t.out);
-  const size_t plane = (size_t)(t.t_rpad >> 3) * 256;
+  int trp = t.t_rpad;
+  if (t.npiece > 0) {  // row-packed tile: this row's product and its T image
+    int k = 0;
+    while (k < t.npiece && row >= pieces[t.piece0 + k].row0 + pieces[t.piece0 + k].t_rpad) ++k;
+    if (k == t.npiece) return;
+    const TPiece pc = pieces[t.piece0 + k];
+    r = row - pc.row0;
+    vrow = r < pc.rows;
+    img = reinterpret_cast<uint8_t*>(pc.out);
+    trp = pc.t_rpad;
+  }
+  if (r < 0 || r >= trp) return;
+  const size_t plane = (size_t)(trp >> 3) * 256;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     __nv_bfloat16 pr[3][8], pi[3][8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int cc = c0 + h * 8 + j;
-      const bool valid = row < t.mrem && cc < t.nrem;
+      const bool valid = vrow && cc < t.nrem;
       __nv_bfloat16 s3[3];
       split3f(valid ? re[h * 8 + j] + cr[h * 8 + j] : 0.f, s3);
       pr[0][j] = s3[0]; pr[1][j] = s3[1]; pr[2][j] = s3[2];
       split3f(valid ? im[h * 8 + j] + cm[h * 8 + j] : 0.f, s3);
       pi[0][j] = s3[0]; pi[1][j] = s3[1]; pi[2][j] = s3[2];
     }
-    const size_t o = img_off(t.t_rpad, r, t.n0 + c0 + h * 8);
+    const size_t o = img_off(trp, r, t.n0 + c0 + h * 8);
 #pragma unroll
     for (int p = 0; p < SPLIT; ++p) {
       *reinterpret_cast<uint4*>(img + o + (size_t)(2 * p) * plane) = pack8(pr[p]);
@@ -419,7 +432,7 @@ constexpr int kMaxStages = 16;           // barriers of the per-tile kernel's va
 // im = Ar Bi + Ai Br.
 template <int SPLIT, int NT>
 __device__ __forceinline__ void epilogue_tile(const Tile& t, int q, int lane, uint32_t lane_base, bool have,
-                                              double2* base_out, float* xbuf) {
+                                              double2* base_out, float* xbuf, const TPiece* __restrict__ pieces) {
   const int row = q * 32 + lane;
   const uint32_t o2 = t.stack ? (uint32_t)t.ntile : (uint32_t)NT;
   const int h = t.a_im >> 5;
@@ -438,7 +451,7 @@ __device__ __forceinline__ void epilogue_tile(const Tile& t, int q, int lane, ui
       for (int j = 0; j < 16; ++j) x1[j] = x2[j] = y1[j] = y2[j] = 0.f;
     }
     if (!t.stack) {
-      epilogue16<SPLIT>(t, row, c0, x1, x2, y1, y2, base_out);
+      epilogue16<SPLIT>(t, row, c0, x1, x2, y1, y2, base_out, pieces);
       continue;
     }
     float re[16], im[16];
@@ -463,7 +476,7 @@ __device__ __forceinline__ void epilogue_tile(const Tile& t, int q, int lane, ui
       }
       epi_sync();
     }
-    if (reader) epilogue16<SPLIT>(t, row, c0, re, im, zero, zero, base_out);
+    if (reader) epilogue16<SPLIT>(t, row, c0, re, im, zero, zero, base_out, pieces);
   }
 }
 
@@ -477,7 +490,8 @@ template <int STAGES, int NT, int SPLIT>
 __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kernel(const Tile* __restrict__ tiles,
                                                                   const Seg* __restrict__ segs,
                                                                   double2* __restrict__ base_out, int* err,
-                                                                  const IoPtrs* __restrict__ io) {
+                                                                  const IoPtrs* __restrict__ io,
+                                                                  const TPiece* __restrict__ pieces) {
   if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
   const Tile t = tiles[blockIdx.x];
@@ -575,7 +589,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_once_kerne
     }
     have = __all_sync(0xffffffffu, have);  // tcgen05.ld below is warp-collective
     const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
-    epilogue_tile<SPLIT, NT>(t, q, lane, lane_base, have, base_out, xbuf);
+    epilogue_tile<SPLIT, NT>(t, q, lane, lane_base, have, base_out, xbuf, pieces);
   }
   fence_before();
   __syncthreads();
@@ -608,7 +622,8 @@ template <int STAGES, int NT, int SPLIT>
 __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(const Tile* __restrict__ tiles, int ntile,
                                                              const Seg* __restrict__ segs,
                                                              double2* __restrict__ base_out, int* err,
-                                                             const IoPtrs* __restrict__ io) {
+                                                             const IoPtrs* __restrict__ io,
+                                                             const TPiece* __restrict__ pieces) {
   if (io) base_out = io->out;
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr int stage_bytes = stage_bytes_of(NT, SPLIT);
@@ -736,7 +751,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
         fence_after();
       }
       have = __all_sync(0xffffffffu, have);  // tcgen05.ld below is warp-collective
-      epilogue_tile<SPLIT, NT>(t, q, lane, lane_base, have, base_out, xbuf);
+      epilogue_tile<SPLIT, NT>(t, q, lane, lane_base, have, base_out, xbuf, pieces);
       // accumulators read: release them to the MMA warp
       if (mmas) {
         fence_before();
@@ -836,7 +851,7 @@ cudaError_t tc_build_images(const tc::ImgTask* d_tasks, int ntask, const double2
 int tc_image_blocks(const tc::ImgTask* tasks, int ntask, std::vector<int2>& out) {
   out.clear();
   for (int i = 0; i < ntask; ++i) {
-    const int ngroups = tasks[i].rpad * (tasks[i].k16 >> 3);
+    const int ngroups = tasks[i].prow * (tasks[i].k16 >> 3);
     for (int g = 0; g < ngroups; g += tc::kImgGroupsPerBlock) out.push_back(make_int2(i, g));
   }
   return (int)out.size();
@@ -874,7 +889,8 @@ cudaError_t tc_zero_out(double2* out, long long n, cudaStream_t s, const tc::IoP
 
 template <int NT, int SPLIT>
 static cudaError_t launch_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out,
-                                int* d_err, bool persistent, cudaStream_t s, const tc::IoPtrs* io) {
+                                int* d_err, bool persistent, cudaStream_t s, const tc::IoPtrs* io,
+                                const tc::TPiece* d_pieces) {
   constexpr int ST = tc::stages_of(NT, SPLIT);
   constexpr int per_sm = NT == 64 ? 2 : 1;  // shared memory and TMEM columns of one SM
   const size_t smem = tc::tile_smem_bytes(NT, SPLIT);
@@ -893,21 +909,23 @@ static cudaError_t launch_tiles(const tc::Tile* d_tiles, int ntile, const tc::Se
   const int resident = per_sm * sms;
   if (persistent && ntile > resident)
     tc::tc_tile_kernel<ST, NT, SPLIT>
-        <<<resident, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io);
+        <<<resident, tc::kThreads, smem, s>>>(d_tiles, ntile, d_segs, base_out, d_err, io, d_pieces);
   else
-    tc::tc_tile_once_kernel<ST, NT, SPLIT><<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io);
+    tc::tc_tile_once_kernel<ST, NT, SPLIT>
+        <<<ntile, tc::kThreads, smem, s>>>(d_tiles, d_segs, base_out, d_err, io, d_pieces);
   return cudaGetLastError();
 }
 
 cudaError_t tc_run_tiles(const tc::Tile* d_tiles, int ntile, const tc::Seg* d_segs, double2* base_out, int* d_err,
-                         bool persistent, cudaStream_t s, const tc::IoPtrs* io, int nt, int split) {
+                         bool persistent, cudaStream_t s, const tc::IoPtrs* io, int nt, int split,
+                         const tc::TPiece* d_pieces) {
   if (ntile <= 0) return cudaSuccess;
   if (split == 2) {
-    if (nt == 64) return launch_tiles<64, 2>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
-    return launch_tiles<128, 2>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+    if (nt == 64) return launch_tiles<64, 2>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io, d_pieces);
+    return launch_tiles<128, 2>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io, d_pieces);
   }
-  if (nt == 64) return launch_tiles<64, 3>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
-  return launch_tiles<128, 3>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io);
+  if (nt == 64) return launch_tiles<64, 3>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io, d_pieces);
+  return launch_tiles<128, 3>(d_tiles, ntile, d_segs, base_out, d_err, persistent, s, io, d_pieces);
 }
 
 }  // namespace hh

@@ -117,7 +117,7 @@ void release_tc_plan(hh_plan* p) {
   destroy_graph(t);
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
                   t.d_tiles2, t.d_tiles2b, t.d_segs, t.d_csegs, t.d_err, t.d_io, t.d_x_blocks,
-                  t.d_c_blocks};
+                  t.d_c_blocks, t.d_pieces};
   for (void* q : ptrs) dev_free(p->ctx, q);
   t = hh_tc_plan();
 }
@@ -147,6 +147,8 @@ int build_tc_plan(hh_plan* p) {
     t.kc = kc;
     t.rpad = rpad(rows);
     t.k16 = k16(kc);
+    t.row0 = 0;
+    t.prow = t.rpad;
     // A, op N: O[r + k ld]; A, op C: conj O[k + r ld]; B, op N: O[k + n ld]; B, op C: conj O[n + k ld]
     t.trans = (role == 0) ? (m.op == HH_OP_C) : (m.op == HH_OP_N);
     t.conj = (m.op == HH_OP_C);
@@ -175,6 +177,8 @@ int build_tc_plan(hh_plan* p) {
     t.kc = r.kc;
     t.rpad = rpad(r.rows);
     t.k16 = k16(r.kc);
+    t.row0 = 0;
+    t.prow = t.rpad;
     t.trans = role == 1 ? 1 : 0;
     t.conj = 0;
     t.cre = 1.0;
@@ -207,7 +211,23 @@ int build_tc_plan(hh_plan* p) {
     return s;
   };
 
+  // Unique two-operator products T = opA(A) X (deduplicated), grouped by their
+  // X operand.  Products of at most 64 rows that share an X are row-packed:
+  // first-fit, largest first, into bins of at most 64 rows; a bin's operators
+  // are stacked in one merged operator image (built once per plan) and the
+  // bin runs as ONE stacked tile per 64 columns whose pieces route each row
+  // to its product's T image.  The epilogue of a stage-1 tile costs about the
+  // same for 16 rows as for 64, and most products have few rows, so this cuts
+  // the number of epilogues and MMA chunks of stage 1.  Larger products and
+  // singletons keep their own tiles.
+  std::vector<tc::TPiece> pieces;
   std::vector<ImgRef> contrib_t(p->contribs.size());
+  struct Prod {
+    ImgRef T;
+    size_t ci;
+  };
+  std::vector<Prod> prods;
+  std::map<std::tuple<int, int, int, int, int>, std::vector<int>> by_x;
   for (size_t ci = 0; ci < p->contribs.size(); ++ci) {
     const hh_contrib& c = p->contribs[ci];
     if (!(c.hasA && c.hasB)) continue;
@@ -223,6 +243,11 @@ int build_tc_plan(hh_plan* p) {
     T.off = a_t.take(img_bytes(c.M, c.Kb));
     t_imgs.emplace(key, T);
     contrib_t[ci] = T;
+    by_x[std::make_tuple(c.i_in, c.irow, c.icol, c.Ka, c.Kb)].push_back((int)prods.size());
+    prods.push_back(Prod{T, ci});
+  }
+  auto single_tiles = [&](const Prod& pr) {
+    const hh_contrib& c = p->contribs[pr.ci];
     ImgRef ai = op_img(c.A, 0, c.M, c.Ka, 1.0, 0.0);
     ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.Kb, 1);
     for (int m0 = 0; m0 < c.M; m0 += 128)
@@ -236,12 +261,95 @@ int build_tc_plan(hh_plan* p) {
         tl.ntile = ntile;
         tl.mrem = std::min(128, c.M - m0);
         tl.nrem = std::min(kTileN, c.Kb - n0);
-        tl.out = tag(T.off, 2);
+        tl.out = tag(pr.T.off, 2);
         tl.t_rpad = rpad(c.M);
         tl.m0 = m0;
         tl.n0 = n0;
         tiles1.push_back(tl);
       }
+  };
+  for (const auto& kv : by_x) {
+    std::vector<int> small;
+    for (int i : kv.second) {
+      if (p->contribs[prods[i].ci].M <= 64)
+        small.push_back(i);
+      else
+        single_tiles(prods[i]);
+    }
+    std::stable_sort(small.begin(), small.end(), [&](int a, int b) {
+      return rpad(p->contribs[prods[a].ci].M) > rpad(p->contribs[prods[b].ci].M);
+    });
+    std::vector<std::vector<int>> bins;
+    std::vector<int> fill;
+    for (int i : small) {
+      const int r = rpad(p->contribs[prods[i].ci].M);
+      size_t b = 0;
+      while (b < bins.size() && fill[b] + r > 64) ++b;
+      if (b == bins.size()) {
+        bins.emplace_back();
+        fill.push_back(0);
+      }
+      bins[b].push_back(i);
+      fill[b] += r;
+    }
+    for (size_t b = 0; b < bins.size(); ++b) {
+      if (bins[b].size() == 1) {
+        single_tiles(prods[bins[b][0]]);
+        continue;
+      }
+      const hh_contrib& c0 = p->contribs[prods[bins[b][0]].ci];
+      const int R = fill[b], Ka = c0.Ka, Kb = c0.Kb;
+      ImgRef merged;
+      merged.rows = R;
+      merged.kc = Ka;
+      merged.off = a_op.take(img_bytes(R, Ka));
+      const int piece0 = (int)pieces.size();
+      int row0 = 0;
+      for (int i : bins[b]) {
+        const hh_contrib& c = p->contribs[prods[i].ci];
+        tc::ImgTask tk{};
+        tk.src = c.A.off;
+        tk.sbase = HH_BASE_ABS;
+        tk.ld = c.A.ld;
+        tk.rows = c.M;
+        tk.kc = Ka;
+        tk.rpad = R;
+        tk.k16 = k16(Ka);
+        tk.trans = c.A.op == HH_OP_C;  // role A
+        tk.conj = c.A.op == HH_OP_C;
+        tk.row0 = row0;
+        tk.prow = rpad(c.M);
+        tk.cre = 1.0;
+        tk.cim = 0.0;
+        tk.dst = merged.off;
+        op_tasks.push_back(tk);
+        tc::TPiece pc{};
+        pc.out = tag(prods[i].T.off, 2);
+        pc.row0 = row0;
+        pc.rows = c.M;
+        pc.t_rpad = rpad(c.M);
+        pieces.push_back(pc);
+        row0 += rpad(c.M);
+      }
+      ImgRef xi = x_img(c0.i_in, c0.irow, c0.icol, Ka, Kb, 1);
+      for (int n0 = 0; n0 < Kb; n0 += kTileN) {
+        const int ntile = k16(std::min(kTileN, Kb - n0));
+        tc::Tile tl{};
+        tl.seg0 = (int)segs.size();
+        tl.nseg = 1;
+        segs.push_back(make_seg(tag(merged.off, 0), merged, 0, tag(xi.off, 1), xi, n0, ntile));
+        tl.mode = 1;
+        tl.ntile = ntile;
+        tl.mrem = R;
+        tl.nrem = std::min(kTileN, Kb - n0);
+        tl.t_rpad = R;
+        tl.m0 = 0;
+        tl.n0 = n0;
+        tl.piece0 = piece0;
+        tl.npiece = (int)bins[b].size();
+        tiles1.push_back(tl);
+      }
+    }
   }
 
   // --------------------------------------------------------------- stage 2
@@ -399,7 +507,9 @@ int build_tc_plan(hh_plan* p) {
     s.a = untag(s.a);
     s.b = untag(s.b);
   }
-  for (auto& tl : tiles1) tl.out = untag(tl.out);
+  for (auto& tl : tiles1)
+    if (tl.npiece == 0) tl.out = untag(tl.out);
+  for (auto& pc : pieces) pc.out = untag(pc.out);
   for (auto& tk : op_tasks) tk.dst += base[0];
   for (auto& tk : x_tasks) tk.dst += base[1];
   std::vector<int2> x_blocks, c_blocks;
@@ -421,6 +531,7 @@ int build_tc_plan(hh_plan* p) {
   if ((st = upload((void**)&t.d_op_tasks, op_tasks.data(), op_tasks.size() * sizeof(tc::ImgTask))) ||
       (st = upload((void**)&t.d_x_tasks, x_tasks.data(), x_tasks.size() * sizeof(tc::ImgTask))) ||
       (st = upload((void**)&t.d_x_blocks, x_blocks.data(), x_blocks.size() * sizeof(int2))) ||
+      (st = upload((void**)&t.d_pieces, pieces.data(), pieces.size() * sizeof(tc::TPiece))) ||
       (st = upload((void**)&t.d_c_blocks, c_blocks.data(), c_blocks.size() * sizeof(int2))) ||
       (st = upload((void**)&t.d_tiles1, tiles1.data(), tiles1.size() * sizeof(tc::Tile))) ||
       (st = upload((void**)&t.d_tiles2, tiles2.data(), tiles2.size() * sizeof(tc::Tile))) ||
@@ -478,10 +589,10 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
   cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io, split, t.d_x_blocks, t.n_x_blocks);
   if (ev) cudaEventRecord(ev[1], s);
   if (e == cudaSuccess)
-    e = tc_run_tiles(t.d_tiles1, t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s, io, 64, split);
+    e = tc_run_tiles(t.d_tiles1, t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s, io, 64, split, t.d_pieces);
   if (e == cudaSuccess)
     e = tc_run_tiles(t.d_tiles1 + t.n_narrow1, t.n_tiles1 - t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s,
-                     io, 128, split);
+                     io, 128, split, t.d_pieces);
   if (ev) cudaEventRecord(ev[2], s);
   if (e == cudaSuccess && t.zero_out) e = tc_zero_out(out, p->nelem, s, io);
   const tc::Tile* tiles2 = t.persistent2 ? t.d_tiles2b : t.d_tiles2;
@@ -646,8 +757,10 @@ static int tc_selftest_impl(hh_ctx_t* ctx, int M, int N, int K, const double* A,
   tc::ImgTask tk[2] = {};
   tk[0].src = (long long)(uintptr_t)dA; tk[0].sbase = HH_BASE_ABS; tk[0].ld = M; tk[0].rows = M; tk[0].kc = K;
   tk[0].rpad = rpad(M); tk[0].k16 = k16(K); tk[0].trans = 0; tk[0].cre = 1.0; tk[0].dst = (long long)(uintptr_t)dimg;
+  tk[0].row0 = 0; tk[0].prow = tk[0].rpad;
   tk[1].src = (long long)(uintptr_t)dB; tk[1].sbase = HH_BASE_ABS; tk[1].ld = K; tk[1].rows = N; tk[1].kc = K;
   tk[1].rpad = rpad(N); tk[1].k16 = k16(K); tk[1].trans = 1; tk[1].cre = 1.0;
+  tk[1].row0 = 0; tk[1].prow = tk[1].rpad;
   tk[1].dst = (long long)(uintptr_t)dimg + ia;
   std::vector<tc::Seg> segs;
   std::vector<tc::Tile> tiles;
