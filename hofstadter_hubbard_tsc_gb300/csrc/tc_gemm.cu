@@ -196,7 +196,7 @@ __device__ __forceinline__ size_t img_off(int rpad, int r, int k) {
 // [blocks[b].y, blocks[b].y + kImgGroupsPerBlock) of task blocks[b].x, so
 // that large and small images spread evenly over the SMs; without one, block
 // b converts all of task b.
-constexpr int kImgGroupsPerBlock = 1024;
+constexpr int kImgGroupsPerBlock = 256;
 
 template <bool kFp32, int SPLIT>
 __global__ void __launch_bounds__(256) build_images_kernel(const ImgTask* __restrict__ tasks,
