@@ -775,7 +775,7 @@ __global__ void __launch_bounds__(kThreads, NT == 64 ? 2 : 1) tc_tile_kernel(con
 // column-major rows.  The products are summed in FP32 (GB300 retires FP32
 // at 64 times its FP64 rate; 2^-24 relative on these terms, far below the
 // split products' error) and added to the FP64 output in FP64.
-constexpr int kCopyElemsPerBlock = 2048;
+constexpr int kCopyElemsPerBlock = 512;
 
 __global__ void __launch_bounds__(256) copy_terms_kernel(const Tile* __restrict__ tiles,
                                                          const int2* __restrict__ blocks,
