@@ -17,6 +17,14 @@ Re <phi_a|chi_b> with chi_b = (1 x O_b) psi, one dot product per pair on the
 device.  Sites are numbered like the reference's output: system block site i
 is site i, environment block site j is site N - j + 1.
 
+Same-side density correlations <n_a n_b> (a < b on one half): n_a carried to
+the block of length b - 1 and embedded in the enlarged basis of length b, n_b
+embedded as the new site, their product formed there the way
+Get_hamiltonian_dia forms the n.n bond (code/get_ham.f90:852-941), then
+truncated and carried to the current block and measured with block_vec_dia /
+vec_block_dia; a block site with its half's middle site is one
+block_site_vec_dia / vec_block_site_dia term; <n_i n_i> = <n_i> + 2 <d_i>.
+
 Cross-cut spin correlations <S_a . S_b> (the spin part of Get_spin_cor,
 code/correlation.f90): the rank-1 site operator sd is carried to its block
 with the ndia embeddings and truncation (update_site_ndia, update_block_ndia,
@@ -33,6 +41,7 @@ import numpy as np
 from . import _lib
 from .device import DBlock, DWave
 from .step import update_trun
+from .types import SubBlock, TotalBlock
 
 
 def _embed(dev, mode, op, dbasis, side):
@@ -53,6 +62,22 @@ def _carry(dev, op, i, length, bases, truns, side, rank1=False):
 
 
 SPIN_NORM = -np.sqrt(3.0)  # <S_a . S_b> per unit-coefficient sd x sd term
+
+
+def _pair_operator(dev, op, a, b, length, bases, truns, side):
+    """n_a n_b (block sites a < b <= length) in the truncated block of
+    `length` sites."""
+    basis, dbasis = bases[b]
+    A = _embed(dev, 0, _carry(dev, op, a, b - 1, bases, truns, side), dbasis, side)
+    B = _embed(dev, 1, op, dbasis, side)
+    P = DBlock.upload(dev, TotalBlock(b, 0, 0, [SubBlock(sec.new_num_up, sec.new_num_down, 0,
+                                                         np.zeros((sec.dim, sec.dim))) for sec in basis.sectors]))
+    one = np.array([1.0, 0.0])
+    dev.check(dev.lib.hh_ham_add_product(dev.h, P.h, A.h, B.h, one.ctypes.data_as(C.POINTER(C.c_double))))
+    cur = update_trun(dev, P, truns[b], dia=True)
+    for L in range(b + 1, length + 1):
+        cur = update_trun(dev, _embed(dev, 0, cur, bases[L][1], side), truns[L], dia=True)
+    return cur
 
 
 class Measurement:
@@ -145,3 +170,43 @@ class Measurement:
                 m[ia, sb.index(b)] = SPIN_NORM * self.wave.dot(phi)
                 phi.free()
         return sa, sb, m
+
+    def density_correlations(self, name="num_elec"):
+        """<n_i n_j> for all sites i, j (N x N): cross-cut pairs, same-side
+        pairs from carried products, the diagonal from <n_i> + 2 <d_i>."""
+        d, dev, N, w = self.d, self.dev, self.N, self.wave
+        op, st_op = d.d_st[name], d.d_st[name]
+        Ls, Le = self.Ls, self.Le
+        m = np.zeros((N, N))
+        sa, sb, cross = self.cross_correlations(name, name)
+        for ia, a in enumerate(sa):
+            for ib, b in enumerate(sb):
+                m[a - 1, b - 1] = m[b - 1, a - 1] = cross[ia, ib]
+
+        def measure(kind, o0, o1=None):
+            phi = self._apply(kind, o0, o1)
+            v = w.dot(phi)
+            phi.free()
+            return v
+
+        for b in range(2, Ls + 1):
+            for a in range(1, b):
+                v = measure(_lib.BLOCK_VEC_DIA, _pair_operator(dev, op, a, b, Ls, d.sys_bases, d.sys_truns, 0))
+                m[a - 1, b - 1] = m[b - 1, a - 1] = v
+        for a in range(1, Ls + 1):
+            v = measure(_lib.BLOCK_SITE_VEC_DIA, _carry(dev, op, a, Ls, d.sys_bases, d.sys_truns, 0), st_op)
+            m[a - 1, Ls] = m[Ls, a - 1] = v
+        for jb in range(2, Le + 1):
+            for ja in range(1, jb):
+                v = measure(_lib.VEC_BLOCK_DIA, _pair_operator(dev, op, ja, jb, Le, d.env_bases, d.env_truns, 1))
+                i, j = N - ja, N - jb
+                m[i, j] = m[j, i] = v
+        for ja in range(1, Le + 1):
+            v = measure(_lib.VEC_BLOCK_SITE_DIA, _carry(dev, op, ja, Le, d.env_bases, d.env_truns, 1), st_op)
+            i, j = N - ja, N - Le - 1
+            m[i, j] = m[j, i] = v
+        n = self.site_profile(name)
+        dbl = self.site_profile("double")
+        for i in range(N):
+            m[i, i] = n[i] + 2.0 * dbl[i]
+        return m

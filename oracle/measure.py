@@ -16,6 +16,16 @@ Re <phi_a|chi_b>, since the two operators act on different halves and are
 Hermitian.  Sites are numbered like the reference's output: system block site
 i is site i, environment block site j is site N - j + 1.
 
+Same-side density correlations <n_a n_b> (a < b on one half, the rest of
+Get_density_cor): n_a is carried to the block of length b - 1 and embedded in
+the enlarged basis of length b (update_block_dia), n_b embedded as the new
+site (update_site_dia), and their product formed in that basis the way
+Get_hamiltonian_dia forms the n.n bond (code/get_ham.f90:852-941:
+coef/sqrt(2S+1) O1 O2 per sector); the product is truncated and carried to
+the current block like a site operator and measured with block_vec_dia /
+vec_block_dia.  A block site with the middle site of its half is the
+block_site_vec_dia / vec_block_site_dia term; <n_i n_i> = <n_i> + 2 <d_i>.
+
 Cross-cut spin correlations <S_a . S_b> (the spin part of Get_spin_cor,
 code/correlation.f90): the rank-1 operator sd of site a is carried to its
 block with update_site_ndia / update_block_ndia / update_trun_ndia, and the
@@ -27,10 +37,11 @@ the unit-coefficient term: <S_a . S_b> = -sqrt(3) <psi|T_ab psi>.
 """
 import numpy as np
 
-from .blocks import (update_site_dia, update_block_dia, update_trun_dia, wave_product, update_site_ndia,
-                     update_block_ndia, update_trun_ndia, block_transfer_trans)
+from .blocks import (Block, Sub, update_site_dia, update_block_dia, update_trun_dia, wave_product,
+                     update_site_ndia, update_block_ndia, update_trun_ndia, block_transfer_trans)
+from .enlarge import get_hamiltonian_dia
 from .matvec import (block_vec_dia, vec_block_dia, site_vec_site_dia, block_vec_block_ndia, block_vec_site_ndia,
-                     site_vec_block_ndia, site_vec_site_ndia)
+                     site_vec_block_ndia, site_vec_site_ndia, block_site_vec_dia, vec_block_site_dia)
 
 
 def _carry(op, i, length, bases, truns):
@@ -131,3 +142,64 @@ def spin_correlations(d):
                 site_vec_site_ndia(sd, "B", sd, "B", sys_bs, env_bs, wave, phi, 1.0)
             m[ia, sb.index(b)] = SPIN_NORM * wave_product(wave, phi)
     return sa, sb, m
+
+
+def _pair_operator(op, a, b, length, bases, truns):
+    """n_a n_b (block sites a < b <= length) in the truncated block of
+    `length` sites."""
+    basis = bases[b]
+    A = update_block_dia(_carry(op, a, b - 1, bases, truns), basis)
+    B = update_site_dia(op, basis)
+    P = Block(b, 0, 0, [Sub(sec.new_num_up, sec.new_num_down, 0, sec.dim, sec.dim) for sec in basis.sectors])
+    get_hamiltonian_dia(A, B, 1.0, P)
+    cur = update_trun_dia(P, truns[b])
+    for L in range(b + 1, length + 1):
+        cur = update_trun_dia(update_block_dia(cur, bases[L]), truns[L])
+    return cur
+
+
+def density_correlations(d, name="num_elec"):
+    """<n_i n_j> for all sites i, j (N x N, sites numbered as in the
+    reference's output) on the current superblock of an oracle DMRG ``d``:
+    cross-cut pairs from cross_correlations, same-side pairs from carried
+    products, the diagonal from the site profiles of n and of the double
+    occupancy (Hubbard)."""
+    wave = d.wave
+    N = d.lat.N
+    op = getattr(d.st, name)
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    m = np.zeros((N, N))
+    sa, sb, cross = cross_correlations(d, name, name)
+    for ia, a in enumerate(sa):
+        for ib, b in enumerate(sb):
+            m[a - 1, b - 1] = m[b - 1, a - 1] = cross[ia, ib]
+
+    def measure(fn, *args):
+        phi = wave.zeros_like()
+        fn(*args, wave, phi, 1.0)
+        return wave_product(wave, phi)
+
+    # system half: block sites 1..Ls and the middle site Ls + 1
+    for b in range(2, Ls + 1):
+        for a in range(1, b):
+            v = measure(block_vec_dia, _pair_operator(op, a, b, Ls, d.sys_bases, d.sys_truns), sys_bs)
+            m[a - 1, b - 1] = m[b - 1, a - 1] = v
+    for a in range(1, Ls + 1):
+        v = measure(block_site_vec_dia, _carry(op, a, Ls, d.sys_bases, d.sys_truns), op, sys_bs)
+        m[a - 1, Ls] = m[Ls, a - 1] = v
+    # environment half: block sites j = 1..Le (site N - j + 1) and the middle site N - Le
+    for jb in range(2, Le + 1):
+        for ja in range(1, jb):
+            v = measure(vec_block_dia, _pair_operator(op, ja, jb, Le, d.env_bases, d.env_truns), env_bs)
+            i, j = N - ja, N - jb
+            m[i, j] = m[j, i] = v
+    for ja in range(1, Le + 1):
+        v = measure(vec_block_site_dia, _carry(op, ja, Le, d.env_bases, d.env_truns), op, env_bs)
+        i, j = N - ja, N - Le - 1
+        m[i, j] = m[j, i] = v
+    n = site_profile(d, name)
+    dbl = site_profile(d, "double") if hasattr(d.st, "double") else np.zeros(N)
+    for i in range(N):
+        m[i, i] = n[i] + 2.0 * dbl[i]
+    return m

@@ -71,3 +71,15 @@ def test_spin_correlations_exact(W, L, ne, U, phi):
     d.left_to_right(1, lat.N // 2 - 1)
     sa, sb, m = om.spin_correlations(d)
     np.testing.assert_allclose(m, ss[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_density_correlations_all_pairs(W, L, ne, U, phi):
+    """<n_i n_j> for every pair (same-side products, cross-cut and diagonal)
+    of the oracle against the exact ground state."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    _, _, corr = ed.hubbard_density_correlations(lat, ne // 2, ne // 2)
+    _, d = _dmrg(lat, ne, sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    np.testing.assert_allclose(om.density_correlations(d), corr, atol=1e-6)
