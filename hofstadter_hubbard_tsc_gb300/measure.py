@@ -25,6 +25,12 @@ truncated and carried to the current block and measured with block_vec_dia /
 vec_block_dia; a block site with its half's middle site is one
 block_site_vec_dia / vec_block_site_dia term; <n_i n_i> = <n_i> + 2 <d_i>.
 
+Same-side spin pairs: S_a carried (rank 1) to the block of length b - 1 and
+the scalar product with the new site's S added in the enlarged basis as the
+S.S bond of Get_hamiltonian_ndia (code/get_ham.f90:954-1152), then carried
+like a scalar; a block site with its half's middle site is the
+block_site_vec_ndia / vec_block_site_ndia S.S term.
+
 Cross-cut spin correlations <S_a . S_b> (the spin part of Get_spin_cor,
 code/correlation.f90): the rank-1 site operator sd is carried to its block
 with the ndia embeddings and truncation (update_site_ndia, update_block_ndia,
@@ -62,6 +68,25 @@ def _carry(dev, op, i, length, bases, truns, side, rank1=False):
 
 
 SPIN_NORM = -np.sqrt(3.0)  # <S_a . S_b> per unit-coefficient sd x sd term
+
+
+def _spin_pair_operator(dev, sd, a, b, length, bases, truns, side):
+    """S_a . S_b (block sites a < b <= length) in the truncated block of
+    `length` sites: S_a carried (rank 1) to the block of length b - 1, the
+    scalar product with the new site's sd added in the enlarged basis as the
+    S.S bond of Get_hamiltonian_ndia (coefficient -sqrt(3)), then truncated
+    and carried."""
+    basis, dbasis = bases[b]
+    Sa = _carry(dev, sd, a, b - 1, bases, truns, side, rank1=True)
+    P = DBlock.upload(dev, TotalBlock(b, 0, 0, [SubBlock(sec.new_num_up, sec.new_num_down, 0,
+                                                         np.zeros((sec.dim, sec.dim))) for sec in basis.sectors]))
+    c = np.array([SPIN_NORM, 0.0])
+    dev.check(dev.lib.hh_ham_add_bond(dev.h, P.h, Sa.h, sd.h, 0, dbasis.h, c.ctypes.data_as(C.POINTER(C.c_double)),
+                                      ord("B"), ord("S") if side == 0 else ord("E")))
+    cur = update_trun(dev, P, truns[b], dia=True)
+    for L in range(b + 1, length + 1):
+        cur = update_trun(dev, _embed(dev, 0, cur, bases[L][1], side), truns[L], dia=True)
+    return cur
 
 
 def _pair_operator(dev, op, a, b, length, bases, truns, side):
@@ -209,4 +234,45 @@ class Measurement:
         dbl = self.site_profile("double")
         for i in range(N):
             m[i, i] = n[i] + 2.0 * dbl[i]
+        return m
+
+    def spin_correlations_all(self):
+        """<S_i . S_j> for all sites i, j (N x N): cross-cut pairs, same-side
+        pairs from carried bond products, block-middle-site terms, diagonal
+        3/4 (<n_i> - 2 <d_i>)."""
+        d, dev, N, w = self.d, self.dev, self.N, self.wave
+        sd = d.d_st["sd"]
+        Ls, Le = self.Ls, self.Le
+        m = np.zeros((N, N))
+        sa, sb, cross = self.spin_correlations()
+        for ia, a in enumerate(sa):
+            for ib, b in enumerate(sb):
+                m[a - 1, b - 1] = m[b - 1, a - 1] = cross[ia, ib]
+
+        def measure(kind, o0, o1=None):
+            phi = self._apply(kind, o0, o1)
+            v = w.dot(phi)
+            phi.free()
+            return v
+
+        for b in range(2, Ls + 1):
+            for a in range(1, b):
+                P = _spin_pair_operator(dev, sd, a, b, Ls, d.sys_bases, d.sys_truns, 0)
+                m[a - 1, b - 1] = m[b - 1, a - 1] = measure(_lib.BLOCK_VEC_DIA, P)
+        for a in range(1, Ls + 1):
+            Sa = _carry(dev, sd, a, Ls, d.sys_bases, d.sys_truns, 0, rank1=True)
+            m[a - 1, Ls] = m[Ls, a - 1] = SPIN_NORM * measure(_lib.BLOCK_SITE_VEC_NDIA, Sa, sd)
+        for jb in range(2, Le + 1):
+            for ja in range(1, jb):
+                P = _spin_pair_operator(dev, sd, ja, jb, Le, d.env_bases, d.env_truns, 1)
+                i, j = N - ja, N - jb
+                m[i, j] = m[j, i] = measure(_lib.VEC_BLOCK_DIA, P)
+        for ja in range(1, Le + 1):
+            Sj = _carry(dev, sd, ja, Le, d.env_bases, d.env_truns, 1, rank1=True)
+            i, j = N - ja, N - Le - 1
+            m[i, j] = m[j, i] = SPIN_NORM * measure(_lib.VEC_BLOCK_SITE_NDIA, Sj, sd)
+        n = self.site_profile("num_elec")
+        dbl = self.site_profile("double")
+        for i in range(N):
+            m[i, i] = 0.75 * (n[i] - 2.0 * dbl[i])
         return m

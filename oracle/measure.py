@@ -39,9 +39,10 @@ import numpy as np
 
 from .blocks import (Block, Sub, update_site_dia, update_block_dia, update_trun_dia, wave_product,
                      update_site_ndia, update_block_ndia, update_trun_ndia, block_transfer_trans)
-from .enlarge import get_hamiltonian_dia
+from .enlarge import get_hamiltonian_dia, get_hamiltonian_ndia
 from .matvec import (block_vec_dia, vec_block_dia, site_vec_site_dia, block_vec_block_ndia, block_vec_site_ndia,
-                     site_vec_block_ndia, site_vec_site_ndia, block_site_vec_dia, vec_block_site_dia)
+                     site_vec_block_ndia, site_vec_site_ndia, block_site_vec_dia, vec_block_site_dia,
+                     block_site_vec_ndia, vec_block_site_ndia)
 
 
 def _carry(op, i, length, bases, truns):
@@ -202,4 +203,66 @@ def density_correlations(d, name="num_elec"):
     dbl = site_profile(d, "double") if hasattr(d.st, "double") else np.zeros(N)
     for i in range(N):
         m[i, i] = n[i] + 2.0 * dbl[i]
+    return m
+
+
+def _spin_pair_operator(sd, a, b, length, bases, truns, side):
+    """S_a . S_b (block sites a < b <= length) in the truncated block of
+    `length` sites: S_a carried (rank 1) to the block of length b - 1, the
+    scalar product with the new site's sd added in the enlarged basis of
+    length b as the S.S bond of Get_hamiltonian_ndia (with -sqrt(3), the
+    inverse of jd / J), then truncated and carried."""
+    basis = bases[b]
+    Sa = _carry_ndia(sd, a, b - 1, bases, truns, side)
+    P = Block(b, 0, 0, [Sub(sec.new_num_up, sec.new_num_down, 0, sec.dim, sec.dim) for sec in basis.sectors])
+    get_hamiltonian_ndia(Sa, sd, basis, SPIN_NORM, P, "B", "S" if side == "sys" else "E")
+    cur = update_trun_dia(P, truns[b])
+    for L in range(b + 1, length + 1):
+        cur = update_trun_dia(update_block_dia(cur, bases[L]), truns[L])
+    return cur
+
+
+def spin_correlations_all(d):
+    """<S_i . S_j> for all sites i, j (N x N): cross-cut pairs from
+    spin_correlations, same-side pairs from carried bond products, a block
+    site with its half's middle site as the block-site S.S term, and
+    <S_i . S_i> = 3/4 (<n_i> - 2 <d_i>) (Hubbard)."""
+    wave = d.wave
+    N = d.lat.N
+    sd = d.st.sd
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    m = np.zeros((N, N))
+    sa, sb, cross = spin_correlations(d)
+    for ia, a in enumerate(sa):
+        for ib, b in enumerate(sb):
+            m[a - 1, b - 1] = m[b - 1, a - 1] = cross[ia, ib]
+
+    def measure(fn, *args, coef=1.0):
+        phi = wave.zeros_like()
+        fn(*args, wave, phi, coef)
+        return wave_product(wave, phi)
+
+    for b in range(2, Ls + 1):
+        for a in range(1, b):
+            v = measure(block_vec_dia, _spin_pair_operator(sd, a, b, Ls, d.sys_bases, d.sys_truns, "sys"), sys_bs)
+            m[a - 1, b - 1] = m[b - 1, a - 1] = v
+    for a in range(1, Ls + 1):
+        v = SPIN_NORM * measure(block_site_vec_ndia, _carry_ndia(sd, a, Ls, d.sys_bases, d.sys_truns, "sys"), "B",
+                                sd, "B", sys_bs)
+        m[a - 1, Ls] = m[Ls, a - 1] = v
+    for jb in range(2, Le + 1):
+        for ja in range(1, jb):
+            v = measure(vec_block_dia, _spin_pair_operator(sd, ja, jb, Le, d.env_bases, d.env_truns, "env"), env_bs)
+            i, j = N - ja, N - jb
+            m[i, j] = m[j, i] = v
+    for ja in range(1, Le + 1):
+        v = SPIN_NORM * measure(vec_block_site_ndia, _carry_ndia(sd, ja, Le, d.env_bases, d.env_truns, "env"), "B",
+                                sd, "B", env_bs)
+        i, j = N - ja, N - Le - 1
+        m[i, j] = m[j, i] = v
+    n = site_profile(d, "num_elec")
+    dbl = site_profile(d, "double")
+    for i in range(N):
+        m[i, i] = 0.75 * (n[i] - 2.0 * dbl[i])
     return m

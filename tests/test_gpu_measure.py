@@ -73,3 +73,16 @@ def test_density_correlations_all_pairs(device, precision):
     d.left_to_right(1, lat.N // 2 - 1)
     _, _, corr = ed.hubbard_density_correlations(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
     np.testing.assert_allclose(Measurement(d).density_correlations(), corr, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_spin_correlations_all_pairs(device, precision):
+    """<S_i . S_j> for every pair on the GPU state against exact
+    diagonalisation."""
+    W, L, ne, U, phi = 2, 4, 6, 8.0, 0.25
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    d.run(sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    _, ss, _ = ed.hubbard_spin_correlations(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
+    np.testing.assert_allclose(Measurement(d).spin_correlations_all(), ss, atol=1e-6)

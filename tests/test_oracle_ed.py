@@ -83,3 +83,15 @@ def test_density_correlations_all_pairs(W, L, ne, U, phi):
     _, d = _dmrg(lat, ne, sweeps=1)
     d.left_to_right(1, lat.N // 2 - 1)
     np.testing.assert_allclose(om.density_correlations(d), corr, atol=1e-6)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_spin_correlations_all_pairs(W, L, ne, U, phi):
+    """<S_i . S_j> for every pair (same-side bond products, block-site terms,
+    cross-cut, diagonal) of the oracle against the exact ground state."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    _, ss, _ = ed.hubbard_spin_correlations(lat, ne // 2, ne // 2)
+    _, d = _dmrg(lat, ne, sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    np.testing.assert_allclose(om.spin_correlations_all(d), ss, atol=1e-6)
