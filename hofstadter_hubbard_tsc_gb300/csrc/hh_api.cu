@@ -743,14 +743,27 @@ int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision) {
   if (!p->d_host_in) e = dev_alloc(ctx, (void**)&p->d_host_in, bytes);
   if (e == cudaSuccess && !p->d_host_out) e = dev_alloc(ctx, (void**)&p->d_host_out, bytes);
   if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(matvec_host)");
+  int st = ensure_hred(ctx, 16);
+  if (st != HH_OK) return st;
+  // one synchronisation: the tensor-core error flag comes back with the output
   e = cudaMemcpyAsync(p->d_host_in, in, bytes, cudaMemcpyHostToDevice, ctx->stream);
-  int st = HH_OK;
-  if (e == cudaSuccess) st = matvec_dev(p, p->d_host_in, p->d_host_out, precision);
+  if (e == cudaSuccess) st = matvec_dev(p, p->d_host_in, p->d_host_out, precision, false);
+  int* h_err = reinterpret_cast<int*>(ctx->h_red + 8);
+  *h_err = 0;
+  const bool tc = precision != HH_PREC_FP64 && p->tc.ready;
   if (e == cudaSuccess && st == HH_OK)
     e = cudaMemcpyAsync(out, p->d_host_out, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess && st == HH_OK && tc)
+    e = cudaMemcpyAsync(h_err, p->tc.d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (st != HH_OK) return st;
-  return cuda_check(ctx, e, "matvec_host");
+  if (e != cudaSuccess) return cuda_check(ctx, e, "matvec_host");
+  if (*h_err) {
+    cudaMemsetAsync(p->tc.d_err, 0, sizeof(int), ctx->stream);
+    return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
+                                         std::to_string(*h_err) + ")");
+  }
+  return HH_OK;
 }
 
 int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision, float* ms) {
