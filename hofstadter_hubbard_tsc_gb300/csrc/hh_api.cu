@@ -728,11 +728,24 @@ static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision
   return cuda_check(ctx, e, "matvec");
 }
 
+// The vectors of a batch (waves of one layout holding nbatch vectors) are
+// multiplied one after another on the same plan (the tensor-core path as one
+// graph replay each); in and out must hold the same number of vectors.
+static int matvec_batch(hh_plan* p, const hh_wave* in, hh_wave* out, int precision, bool check) {
+  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out || in->nbatch != out->nbatch)
+    return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
+  for (int b = 0; b < in->nbatch; ++b) {
+    const bool last = b + 1 == in->nbatch;
+    const int st = matvec_dev(p, in->d + (size_t)b * p->nelem, out->d + (size_t)b * p->nelem, precision,
+                              check && last);
+    if (st != HH_OK) return st;
+  }
+  return HH_OK;
+}
+
 int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision) {
   if (!p || !in || !out) return HH_ERR_INVALID;
-  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out)
-    return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
-  return matvec_dev(p, in->d, out->d, precision);
+  return matvec_batch(p, in, out, precision, true);
 }
 
 int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision) {
@@ -795,9 +808,7 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
 
 int hh_matvec_async(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision) {
   if (!p || !in || !out) return HH_ERR_INVALID;
-  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out)
-    return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
-  return matvec_dev(p, in->d, out->d, precision, false);
+  return matvec_batch(p, in, out, precision, false);
 }
 
 int hh_plan_check(hh_plan_t* p) {

@@ -155,7 +155,9 @@ int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* en
 int hh_plan_stats(const hh_plan_t* p, double* counts);
 int hh_plan_free(hh_plan_t* p);
 
-/* model_wave (code/mat_vec.f90:3476): out = H in, device-resident waves.   */
+/* model_wave (code/mat_vec.f90:3476): out = H in, device-resident waves;
+ * waves holding nbatch vectors (hh_wave_create) are multiplied vector by
+ * vector on the same plan (in and out must hold the same number).         */
 int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision);
 /* model_wave with host buffers: copies in, multiplies, copies out (device
  * buffers of the plan are reused between calls).                          */

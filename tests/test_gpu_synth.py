@@ -35,3 +35,31 @@ def test_synthetic_matvec(device, name):
         got = sb.w_out.download()
         assert np.linalg.norm(got - gpu) / np.linalg.norm(gpu) < tol, (prec, name)
     sb.free()
+
+
+def test_batched_matvec(device):
+    """A wave of several vectors (the batched psi of the synthetic
+    configuration): every vector equals its own single-vector product, in
+    FP64 and split precision; mismatched batches are rejected."""
+    from hofstadter_hubbard_tsc_gb300.device import DWave
+    wl = Workload(**CASES["tj-2x12"])
+    sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
+    nb = 3
+    rng = np.random.default_rng(8)
+    psi = rng.normal(size=(nb, wl.sup.dim)) + 1j * rng.normal(size=(nb, wl.sup.dim))
+    lay = sb.w_in.layout
+    win = DWave(device, lay, sb.w_in.sys_len, sb.w_in.env_len, nbatch=nb)
+    wout = DWave(device, lay, sb.w_in.sys_len, sb.w_in.env_len, nbatch=nb)
+    win.upload(psi)
+    for prec in (_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3):
+        device.check(device.lib.hh_matvec(sb.plan, win.h, wout.h, prec))
+        got = wout.download().reshape(nb, -1)
+        for b in range(nb):
+            sb.w_in.upload(psi[b])
+            device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, prec))
+            ref = sb.w_out.download()
+            assert np.linalg.norm(got[b] - ref) / np.linalg.norm(ref) < 1e-13, (prec, b)
+    assert device.lib.hh_matvec(sb.plan, win.h, sb.w_out.h, _lib.HH_PREC_FP64) == -1
+    win.free()
+    wout.free()
+    sb.free()
