@@ -53,7 +53,9 @@ def parse():
                    help="matvec workload: c2 Hubbard 4x32 phi=1/4 N_e=112 m=2000 (headline); c3 t-J 4x48 "
                         "J=0.4 phi=1/6 N_e=176 m=4000; c4 Hubbard 6x24 phi=1/3 N_e=132 m=6000 (mid-chain "
                         "superblocks, synthetic operators); --W/--L/--ne/--m override c2's sizes")
-    p.add_argument("--m", type=int, default=2000)
+    p.add_argument("--m", "--kept", dest="m", type=int, default=2000,
+                   help="kept multiplets of the c2 workload (--kept under torchrun, whose own options "
+                        "shadow --m)")
     p.add_argument("--W", type=int, default=4)
     p.add_argument("--L", type=int, default=32)
     p.add_argument("--ne", type=int, default=112)
@@ -69,6 +71,23 @@ def parse():
                    help="also run Lanczos (100 vectors) in FP64 and in split precision from one start "
                         "vector and report |dE/E| (outside the timed region)")
     return p.parse_args()
+
+
+def max_over_ranks(x, dist, device):
+    """The largest value of x over the ranks (x itself without a process
+    group): the job's time is its slowest replica's."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world_size, steps, t_max):
+    """Whole-job throughput of independent replicas: every rank did `steps`
+    matvecs in at most t_max seconds."""
+    return world_size * steps / t_max
 
 
 def dist_setup(args):
@@ -394,12 +413,8 @@ def main():
         s1 += b
         s2 += c
         s0 += d
-    t_steps = tot / 1e3  # seconds, device time of the K matvecs
-    if dist:
-        t = torch.tensor([t_steps], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_steps = float(t.item())
-    value = ws * args.steps / t_steps
+    t_steps = max_over_ranks(tot / 1e3, dist, "cuda")  # seconds, device time of the K matvecs
+    value = replica_rate(ws, args.steps, t_steps)
 
     # end to end through the C-ABI call with pinned host buffers
     nbytes = wl.sup.dim * 16
