@@ -39,6 +39,14 @@ plan of the kernel that carries the Hamiltonian's S.S bond in that geometry
 (block-block, block-site, site-block, site-site; the environment operator
 through block_transfer_trans); that term holds J S.S as jd = -sqrt(3) J
 times the unit-coefficient term, so <S_a . S_b> = -sqrt(3) <psi|T_ab psi>.
+
+Cross-cut electron correlations G_ab = sum_s <c+_as c_bs> (the 'F' call of
+Get_density_cor, code/quantum.f90:531): elec_up of site a and elec_down of
+site b carried with the fermion ('F') ndia embeddings, each pair the hopping
+kernel of its geometry (the Hamiltonian's own t term, code/mat_vec.f90:
+3502-3615) with coefficient 1 and with i.  That term holds X + X^+ with
+X = sum_s c+_as c_bs / sqrt(2), so Re G = <T_1> / sqrt(2) and
+Im G = -<T_i> / sqrt(2).
 """
 import ctypes as C
 
@@ -50,20 +58,21 @@ from .step import update_trun
 from .types import SubBlock, TotalBlock
 
 
-def _embed(dev, mode, op, dbasis, side):
+def _embed(dev, mode, op, dbasis, side, flag="B"):
     h = C.c_void_p()
-    dev.check(dev.lib.hh_enlarge_operator(dev.h, mode, op.h, dbasis.h, ord("B"), side, C.byref(h)))
+    dev.check(dev.lib.hh_enlarge_operator(dev.h, mode, op.h, dbasis.h, ord(flag), side, C.byref(h)))
     return DBlock.from_handle(dev, h)
 
 
-def _carry(dev, op, i, length, bases, truns, side, rank1=False):
+def _carry(dev, op, i, length, bases, truns, side, rank1=False, flag="B"):
     """Operator of block site i in the truncated block of `length` sites
-    (rank1: a boson operator of rank 1, through the ndia embeddings)."""
+    (rank1: an operator of nonzero rank through the ndia embeddings, flag
+    'B' boson or 'F' fermion)."""
     site_mode, block_mode = (3, 2) if rank1 else (1, 0)
     dia = not rank1
-    cur = op if i <= 1 else update_trun(dev, _embed(dev, site_mode, op, bases[i][1], side), truns[i], dia=dia)
+    cur = op if i <= 1 else update_trun(dev, _embed(dev, site_mode, op, bases[i][1], side, flag), truns[i], dia=dia)
     for L in range(i + 1, length + 1):
-        cur = update_trun(dev, _embed(dev, block_mode, cur, bases[L][1], side), truns[L], dia=dia)
+        cur = update_trun(dev, _embed(dev, block_mode, cur, bases[L][1], side, flag), truns[L], dia=dia)
     return cur
 
 
@@ -118,12 +127,13 @@ class Measurement:
         self.env_bs = dmrg.env_bases[sup.env_len][1]
         self.Ls, self.Le = sup.sys_len - 1, sup.env_len - 1
 
-    def _apply(self, kind, op0, op1=None, trans1=0):
+    def _apply(self, kind, op0, op1=None, trans1=0, flag="B", coef=1.0):
         """(one term) psi as a new device wave."""
         dev, w = self.dev, self.wave
         t = (_lib.HHTerm * 1)()
-        t[0] = _lib.HHTerm(kind, ord("B"), ord("B"), 0, trans1, op0.h, op1.h if op1 is not None else None, 1.0,
-                           0.0)
+        c = complex(coef)
+        t[0] = _lib.HHTerm(kind, ord(flag), ord(flag), 0, trans1, op0.h, op1.h if op1 is not None else None, c.real,
+                           c.imag)
         plan = C.c_void_p()
         dev.check(dev.lib.hh_plan_create(dev.h, self.sys_bs.h, self.env_bs.h, w.h, 1, t, C.byref(plan)))
         out = DWave(dev, w.layout, w.sys_len, w.env_len)
@@ -194,6 +204,35 @@ class Measurement:
                     phi = self._apply(_lib.SITE_VEC_SITE_NDIA, sd, sd)
                 m[ia, sb.index(b)] = SPIN_NORM * self.wave.dot(phi)
                 phi.free()
+        return sa, sb, m
+
+    def electron_correlations(self):
+        """G_ab = sum_s <c+_as c_bs>, a on the system half, b on the
+        environment half: (sites_a, sites_b, complex matrix)."""
+        d, dev, N = self.d, self.dev, self.N
+        up, dn = d.d_st["elec_up"], d.d_st["elec_down"]
+        a_ops = [(i, _carry(dev, up, i, self.Ls, d.sys_bases, d.sys_truns, 0, rank1=True, flag="F"))
+                 for i in range(1, self.Ls + 1)] + [(self.Ls + 1, None)]
+        b_ops = [(N - self.Le, None)] + [(N - j + 1, _carry(dev, dn, j, self.Le, d.env_bases, d.env_truns, 1,
+                                                            rank1=True, flag="F")) for j in range(1, self.Le + 1)]
+        sa = [a for a, _ in a_ops]
+        sb = sorted(b for b, _ in b_ops)
+        m = np.zeros((len(sa), len(sb)), dtype=np.complex128)
+        for ia, (a, oa) in enumerate(a_ops):
+            for b, ob in b_ops:
+                t = []
+                for coef in (1.0, 1j):
+                    if oa is not None and ob is not None:
+                        phi = self._apply(_lib.BLOCK_VEC_BLOCK_NDIA, oa, ob, 1, "F", coef)
+                    elif oa is not None:
+                        phi = self._apply(_lib.BLOCK_VEC_SITE_NDIA, oa, dn, 1, "F", coef)
+                    elif ob is not None:
+                        phi = self._apply(_lib.SITE_VEC_BLOCK_NDIA, up, ob, 1, "F", coef)
+                    else:
+                        phi = self._apply(_lib.SITE_VEC_SITE_NDIA, up, dn, 1, "F", coef)
+                    t.append(self.wave.dot(phi))
+                    phi.free()
+                m[ia, sb.index(b)] = (t[0] - 1j * t[1]) / np.sqrt(2.0)
         return sa, sb, m
 
     def density_correlations(self, name="num_elec"):

@@ -261,3 +261,38 @@ def hubbard_spin_correlations(lat, n_up, n_dn):
             mp = -sp.kron(_pair_hop(cu, j, i), _pair_hop(cd, i, j), format="csr")
             ss[i, j] += 0.5 * float(np.real(np.vdot(psi, (pm + mp) @ psi)))
     return float(e0), ss, 3.0 * szsz
+
+
+def hubbard_green(lat, n_up, n_dn):
+    """Lowest state of the (n_up, n_dn) sector: energy and
+    G_ij = sum_s <c+_is c_js> (complex, sites in lattice order)."""
+    N = lat.N
+    cu = _configs(N, n_up)
+    cd = _configs(N, n_dn)
+    hu = _spin_hop(lat, cu)
+    hd = _spin_hop(lat, cd)
+    H = sp.kron(hu, sp.identity(len(cd)), format="csr") + sp.kron(sp.identity(len(cu)), hd, format="csr")
+    au = np.array(cu, dtype=np.int64)
+    ad = np.array(cd, dtype=np.int64)
+    if lat.U != 0.0:
+        dbl = np.array([[bin(int(x & y)).count("1") for y in ad] for x in au], dtype=np.float64).ravel()
+        H = H + sp.diags(lat.U * dbl)
+    if H.shape[0] <= 2000:
+        w, v = np.linalg.eigh(H.toarray())
+        e0, psi = w[0], v[:, 0]
+    else:
+        w, v = spla.eigsh(H, k=1, which="SA", tol=1e-13)
+        e0, psi = w[0], v[:, 0]
+    G = np.zeros((N, N), dtype=np.complex128)
+    Iu, Id = sp.identity(len(cu), format="csr"), sp.identity(len(cd), format="csr")
+    occ_u = np.array([[(c >> s) & 1 for s in range(N)] for c in au], dtype=np.float64)
+    occ_d = np.array([[(c >> s) & 1 for s in range(N)] for c in ad], dtype=np.float64)
+    n = (occ_u[:, None, :] + occ_d[None, :, :]).reshape(-1, N)
+    p = np.abs(psi) ** 2
+    for i in range(N):
+        G[i, i] = p @ n[:, i]
+        for j in range(N):
+            if i != j:
+                op = sp.kron(_pair_hop(cu, i, j), Id, format="csr") + sp.kron(Iu, _pair_hop(cd, i, j), format="csr")
+                G[i, j] = np.vdot(psi, op @ psi)
+    return float(e0), G

@@ -266,3 +266,52 @@ def spin_correlations_all(d):
     for i in range(N):
         m[i, i] = 0.75 * (n[i] - 2.0 * dbl[i])
     return m
+
+
+def _carry_fermion(op, i, length, bases, truns, side):
+    """Rank-1/2 (fermion) operator of block site i in the truncated block of
+    `length` sites."""
+    cur = op.copy() if i <= 1 else update_trun_ndia(update_site_ndia(op, bases[i], "F", side), truns[i])
+    for L in range(i + 1, length + 1):
+        cur = update_trun_ndia(update_block_ndia(cur, bases[L], "F", side), truns[L])
+    return cur
+
+
+def electron_correlations(d):
+    """G_ab = sum_s <c+_as c_bs> for a on the system half and b on the
+    environment half (the electron part of Get_density_cor, flag 'F'):
+    (sites_a, sites_b, complex matrix).  Each pair is the hopping kernel of
+    that geometry (the environment operator through block_transfer_trans),
+    which holds X + X^+ with X = sum_s c+_as c_bs / sqrt(2); with the
+    coefficients 1 and i it gives Re G = <T_1> / sqrt(2), Im G = -<T_i> /
+    sqrt(2)."""
+    wave = d.wave
+    N = d.lat.N
+    up, dn = d.st.elec_up, d.st.elec_down
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    a_ops = [(i, _carry_fermion(up, i, Ls, d.sys_bases, d.sys_truns, "sys")) for i in range(1, Ls + 1)]
+    a_ops.append((Ls + 1, None))
+    b_ops = [(N - Le, None)]
+    b_ops += [(N - j + 1, block_transfer_trans(_carry_fermion(dn, j, Le, d.env_bases, d.env_truns, "env")))
+              for j in range(1, Le + 1)]
+    dn_t = block_transfer_trans(dn)
+    sa = [a for a, _ in a_ops]
+    sb = sorted(b for b, _ in b_ops)
+    m = np.zeros((len(sa), len(sb)), dtype=np.complex128)
+    for ia, (a, oa) in enumerate(a_ops):
+        for b, ob in b_ops:
+            t = []
+            for coef in (1.0, 1j):
+                phi = wave.zeros_like()
+                if oa is not None and ob is not None:
+                    block_vec_block_ndia(oa, "F", ob, "F", sys_bs, env_bs, wave, phi, coef)
+                elif oa is not None:
+                    block_vec_site_ndia(oa, "F", dn_t, "F", sys_bs, env_bs, wave, phi, coef)
+                elif ob is not None:
+                    site_vec_block_ndia(up, "F", ob, "F", sys_bs, env_bs, wave, phi, coef)
+                else:
+                    site_vec_site_ndia(up, "F", dn_t, "F", sys_bs, env_bs, wave, phi, coef)
+                t.append(wave_product(wave, phi))
+            m[ia, sb.index(b)] = (t[0] - 1j * t[1]) / np.sqrt(2.0)
+    return sa, sb, m

@@ -95,3 +95,22 @@ def test_spin_correlations_all_pairs(W, L, ne, U, phi):
     _, d = _dmrg(lat, ne, sweeps=1)
     d.left_to_right(1, lat.N // 2 - 1)
     np.testing.assert_allclose(om.spin_correlations_all(d), ss, atol=1e-6)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_electron_correlations_exact(W, L, ne, U, phi):
+    """Cross-cut G_ab = sum_s <c+_as c_bs> of the oracle (fermion operators
+    carried with the 'F' ndia embeddings, the hopping kernels with
+    coefficients 1 and i) against the exact ground state; the exact G is
+    Hermitian with trace N_e and carries the flux phases (complex)."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    e0, G = ed.hubbard_green(lat, ne // 2, ne // 2)
+    np.testing.assert_allclose(G, G.conj().T, atol=1e-12)
+    assert np.trace(G).real == pytest.approx(ne, abs=1e-10)
+    assert np.abs(G.imag).max() > 1e-3
+    e, d = _dmrg(lat, ne, sweeps=1)
+    assert e == pytest.approx(e0, rel=1e-10)
+    d.left_to_right(1, lat.N // 2 - 1)
+    sa, sb, m = om.electron_correlations(d)
+    np.testing.assert_allclose(m, G[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
