@@ -114,6 +114,29 @@ def _pair_operator(dev, op, a, b, length, bases, truns, side):
     return cur
 
 
+def _hop_pair_operators(dev, op, site, a, b, length, bases, truns, side):
+    """The hopping bond of Get_hamiltonian_ndia between block site a (op
+    carried with the fermion ndia embeddings to the block of length b - 1)
+    and the new site b (site operator through block_transfer_trans), formed
+    with coefficients 1 and i in the enlarged basis of length b, each
+    truncated and carried as a scalar to the block of `length` sites."""
+    basis, dbasis = bases[b]
+    out = []
+    for coef in (1.0, 1j):
+        Ca = _carry(dev, op, a, b - 1, bases, truns, side, rank1=True, flag="F")
+        P = DBlock.upload(dev, TotalBlock(b, 0, 0, [SubBlock(sec.new_num_up, sec.new_num_down, 0,
+                                                             np.zeros((sec.dim, sec.dim))) for sec in basis.sectors]))
+        c = np.array([complex(coef).real, complex(coef).imag])
+        dev.check(dev.lib.hh_ham_add_bond(dev.h, P.h, Ca.h, site.h, 1, dbasis.h,
+                                          c.ctypes.data_as(C.POINTER(C.c_double)), ord("F"),
+                                          ord("S") if side == 0 else ord("E")))
+        cur = update_trun(dev, P, truns[b], dia=True)
+        for L in range(b + 1, length + 1):
+            cur = update_trun(dev, _embed(dev, 0, cur, bases[L][1], side), truns[L], dia=True)
+        out.append(cur)
+    return out
+
+
 class Measurement:
     """Measurements on the current superblock of a ``GPUDMRG`` (its last
     Lanczos state and the bases and truncations it keeps on the device)."""
@@ -315,3 +338,58 @@ class Measurement:
         for i in range(N):
             m[i, i] = 0.75 * (n[i] - 2.0 * dbl[i])
         return m
+
+    def electron_correlations_all(self):
+        """G_ij = sum_s <c+_is c_js> for all sites i, j (N x N, complex,
+        Hermitian): cross-cut pairs, same-side pairs from the hopping bond
+        formed in the enlarged basis (system side: block elec_up with the new
+        site's elec_down; environment side: block elec_down with the new
+        site's elec_up), block-middle-site hopping terms, diagonal <n_i>."""
+        d, dev, N, w = self.d, self.dev, self.N, self.wave
+        up, dn = d.d_st["elec_up"], d.d_st["elec_down"]
+        Ls, Le = self.Ls, self.Le
+        G = np.zeros((N, N), dtype=np.complex128)
+
+        def put(i, j, v):
+            G[i, j] = v
+            G[j, i] = np.conj(v)
+
+        sa, sb, cross = self.electron_correlations()
+        for ia, a in enumerate(sa):
+            for ib, b in enumerate(sb):
+                put(a - 1, b - 1, cross[ia, ib])
+
+        def scalar(kind, ops):
+            t = []
+            for o in ops:
+                phi = self._apply(kind, o)
+                t.append(w.dot(phi))
+                phi.free()
+            return (t[0] - 1j * t[1]) / np.sqrt(2.0)
+
+        def term(kind, o0, o1):
+            t = []
+            for coef in (1.0, 1j):
+                phi = self._apply(kind, o0, o1, 1, "F", coef)
+                t.append(w.dot(phi))
+                phi.free()
+            return (t[0] - 1j * t[1]) / np.sqrt(2.0)
+
+        for b in range(2, Ls + 1):
+            for a in range(1, b):
+                ops = _hop_pair_operators(dev, up, dn, a, b, Ls, d.sys_bases, d.sys_truns, 0)
+                put(a - 1, b - 1, scalar(_lib.BLOCK_VEC_DIA, ops))
+        for a in range(1, Ls + 1):
+            oa = _carry(dev, up, a, Ls, d.sys_bases, d.sys_truns, 0, rank1=True, flag="F")
+            put(a - 1, Ls, term(_lib.BLOCK_SITE_VEC_NDIA, oa, dn))
+        for jb in range(2, Le + 1):
+            for ja in range(1, jb):
+                ops = _hop_pair_operators(dev, dn, up, ja, jb, Le, d.env_bases, d.env_truns, 1)
+                put(N - ja, N - jb, scalar(_lib.VEC_BLOCK_DIA, ops))
+        for ja in range(1, Le + 1):
+            oa = _carry(dev, up, ja, Le, d.env_bases, d.env_truns, 1, rank1=True, flag="F")
+            put(N - ja, N - Le - 1, term(_lib.VEC_BLOCK_SITE_NDIA, oa, dn))
+        n = self.site_profile("num_elec")
+        for i in range(N):
+            G[i, i] = n[i]
+        return G

@@ -315,3 +315,85 @@ def electron_correlations(d):
                 t.append(wave_product(wave, phi))
             m[ia, sb.index(b)] = (t[0] - 1j * t[1]) / np.sqrt(2.0)
     return sa, sb, m
+
+
+def _hop_pair_operators(op, site, a, b, length, bases, truns, side):
+    """The hopping bond of Get_hamiltonian_ndia between block site a (op:
+    elec_up on the system side, elec_down on the environment side, carried
+    to the block of length b - 1) and the new site b (site operator through
+    block_transfer_trans), formed with coefficients 1 and i in the enlarged
+    basis of length b and carried as scalars to the block of `length`
+    sites."""
+    basis = bases[b]
+    out = []
+    for coef in (1.0, 1j):
+        Ca = _carry_fermion(op, a, b - 1, bases, truns, side)
+        P = Block(b, 0, 0, [Sub(sec.new_num_up, sec.new_num_down, 0, sec.dim, sec.dim) for sec in basis.sectors])
+        get_hamiltonian_ndia(Ca, block_transfer_trans(site), basis, coef, P, "F", "S" if side == "sys" else "E")
+        cur = update_trun_dia(P, truns[b])
+        for L in range(b + 1, length + 1):
+            cur = update_trun_dia(update_block_dia(cur, bases[L]), truns[L])
+        out.append(cur)
+    return out
+
+
+def electron_correlations_all(d):
+    """G_ij = sum_s <c+_is c_js> for all sites i, j (N x N, complex,
+    Hermitian): cross-cut pairs from electron_correlations; same-side pairs
+    from the hopping bond formed in the enlarged basis (system side: block
+    elec_up with the new site's elec_down, giving G_ab, a < b; environment
+    side: block elec_down with the new site's elec_up, giving G for the
+    outer site first); a block site with its half's middle site from the
+    block-site hopping kernels; the diagonal <n_i>.  Every term holds
+    X + X^+ with X = G / sqrt(2): G = (<T_1> - i <T_i>) / sqrt(2)."""
+    wave = d.wave
+    N = d.lat.N
+    up, dn = d.st.elec_up, d.st.elec_down
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    G = np.zeros((N, N), dtype=np.complex128)
+
+    def put(i, j, v):
+        G[i, j] = v
+        G[j, i] = np.conj(v)
+
+    sa, sb, cross = electron_correlations(d)
+    for ia, a in enumerate(sa):
+        for ib, b in enumerate(sb):
+            put(a - 1, b - 1, cross[ia, ib])
+
+    def scalar(ops, fn, bs):
+        t = []
+        for cur in ops:
+            phi = wave.zeros_like()
+            fn(cur, bs, wave, phi, 1.0)
+            t.append(wave_product(wave, phi))
+        return (t[0] - 1j * t[1]) / np.sqrt(2.0)
+
+    def term(fn, *args):
+        t = []
+        for coef in (1.0, 1j):
+            phi = wave.zeros_like()
+            fn(*args, wave, phi, coef)
+            t.append(wave_product(wave, phi))
+        return (t[0] - 1j * t[1]) / np.sqrt(2.0)
+
+    dn_t = block_transfer_trans(dn)
+    for b in range(2, Ls + 1):
+        for a in range(1, b):
+            ops = _hop_pair_operators(up, dn, a, b, Ls, d.sys_bases, d.sys_truns, "sys")
+            put(a - 1, b - 1, scalar(ops, block_vec_dia, sys_bs))
+    for a in range(1, Ls + 1):
+        oa = _carry_fermion(up, a, Ls, d.sys_bases, d.sys_truns, "sys")
+        put(a - 1, Ls, term(block_site_vec_ndia, oa, "F", dn_t, "F", sys_bs))
+    for jb in range(2, Le + 1):
+        for ja in range(1, jb):
+            ops = _hop_pair_operators(dn, up, ja, jb, Le, d.env_bases, d.env_truns, "env")
+            put(N - ja, N - jb, scalar(ops, vec_block_dia, env_bs))
+    for ja in range(1, Le + 1):
+        oa = _carry_fermion(up, ja, Le, d.env_bases, d.env_truns, "env")
+        put(N - ja, N - Le - 1, term(vec_block_site_ndia, oa, "F", dn_t, "F", env_bs))
+    n = site_profile(d, "num_elec")
+    for i in range(N):
+        G[i, i] = n[i]
+    return G

@@ -6,8 +6,8 @@ are known answers of this project's own independent code paths:
 
 * ed_known_answers.json: Fock-basis exact diagonalisation (oracle/ed.py,
   which shares nothing with the SU(2) code) of a Hubbard flux ladder and a
-  t-J ladder: singlet ground energies, and for the Hubbard ladder the density
-  and spin correlation matrices;
+  t-J ladder: singlet ground energies, and for the Hubbard ladder the density,
+  spin and electron (sum_s <c+_i c_j>, complex) correlation matrices;
 * matvec_tj_2x6.npz and matvec_hubbard_4x4.npz: a seeded input vector and the
   oracle's model_wave of it on small synthetic mid-chain superblocks
   (hofstadter_hubbard_tsc_gb300/synth.py).
@@ -37,11 +37,12 @@ def ed_fixtures():
     e_h, _ = ed.singlet_ground_energy(hub, 6)
     _, dens, corr = ed.hubbard_density_correlations(hub, 3, 3)
     _, ss, _ = ed.hubbard_spin_correlations(hub, 3, 3)
+    _, G = ed.hubbard_green(hub, 3, 3)
     tj = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
     e_t = ed.tj_singlet_ground_energy(tj, 6)
     return {
         "hubbard_2x4_U8_phi0.25_Ne6": {"energy": float(e_h), "density": dens.tolist(), "nn": corr.tolist(),
-                                       "ss": ss.tolist()},
+                                       "ss": ss.tolist(), "green_re": G.real.tolist(), "green_im": G.imag.tolist()},
         "tj_2x4_J0.4_phi1/6_Ne6": {"energy": float(e_t)},
     }
 

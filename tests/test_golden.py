@@ -22,6 +22,10 @@ def _ed():
         return json.load(f)
 
 
+def _green(g):
+    return np.array(g["green_re"]) + 1j * np.array(g["green_im"])
+
+
 def _matvec(name):
     z = np.load(os.path.join(HERE, name + ".npz"))
     return z["psi"], z["hpsi"]
@@ -34,6 +38,8 @@ def test_ed_reproduces_fixture():
     assert e == pytest.approx(g["energy"], abs=1e-12)
     _, ss, _ = ed.hubbard_spin_correlations(hub, 3, 3)
     np.testing.assert_allclose(ss, np.array(g["ss"]), atol=1e-12)
+    _, G = ed.hubbard_green(hub, 3, 3)
+    np.testing.assert_allclose(G, _green(g), atol=1e-12)
 
 
 def test_oracle_dmrg_reproduces_fixture():
@@ -44,6 +50,7 @@ def test_oracle_dmrg_reproduces_fixture():
     assert d.run(sweeps=1) == pytest.approx(g["hubbard_2x4_U8_phi0.25_Ne6"]["energy"], abs=1e-9)
     d.left_to_right(1, 3)
     np.testing.assert_allclose(om.density_correlations(d), np.array(g["hubbard_2x4_U8_phi0.25_Ne6"]["nn"]), atol=1e-6)
+    np.testing.assert_allclose(om.electron_correlations_all(d), _green(g["hubbard_2x4_U8_phi0.25_Ne6"]), atol=1e-6)
     t = DMRG(Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0), 6, kept_min=300, kept_max=300, trun_err=1e-14,
              lanzero=1e-11, seed=3)
     assert t.run(sweeps=1) == pytest.approx(g["tj_2x4_J0.4_phi1/6_Ne6"]["energy"], abs=1e-9)
@@ -86,3 +93,4 @@ def test_gpu_dmrg_golden(device):
     m = Measurement(d)
     np.testing.assert_allclose(m.density_correlations(), np.array(g["nn"]), atol=1e-6)
     np.testing.assert_allclose(m.spin_correlations_all(), np.array(g["ss"]), atol=1e-6)
+    np.testing.assert_allclose(m.electron_correlations_all(), _green(g), atol=1e-6)

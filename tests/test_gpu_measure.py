@@ -101,3 +101,16 @@ def test_electron_correlations_exact(device, precision):
     _, G = ed.hubbard_green(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
     sa, sb, m = Measurement(d).electron_correlations()
     np.testing.assert_allclose(m, G[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_electron_correlations_all_pairs(device, precision):
+    """G_ij = sum_s <c+_is c_js> for every pair on the GPU state against exact
+    diagonalisation."""
+    W, L, ne, U, phi = 2, 4, 6, 8.0, 0.25
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    d.run(sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    _, G = ed.hubbard_green(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
+    np.testing.assert_allclose(Measurement(d).electron_correlations_all(), G, atol=1e-6)

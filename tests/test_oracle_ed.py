@@ -114,3 +114,18 @@ def test_electron_correlations_exact(W, L, ne, U, phi):
     d.left_to_right(1, lat.N // 2 - 1)
     sa, sb, m = om.electron_correlations(d)
     np.testing.assert_allclose(m, G[np.ix_(np.array(sa) - 1, np.array(sb) - 1)], atol=1e-6)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 3, 4, 4.0, 0.3)])
+def test_electron_correlations_all_pairs(W, L, ne, U, phi):
+    """G_ij = sum_s <c+_is c_js> for every pair (same-side hopping bonds
+    formed in the enlarged basis, block-middle-site hopping terms, cross-cut,
+    diagonal) of the oracle against the exact ground state."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    _, G = ed.hubbard_green(lat, ne // 2, ne // 2)
+    _, d = _dmrg(lat, ne, sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    m = om.electron_correlations_all(d)
+    np.testing.assert_allclose(m, m.conj().T, atol=1e-12)
+    np.testing.assert_allclose(m, G, atol=1e-6)
