@@ -95,6 +95,7 @@ SIGNATURES = {
     "hh_density_truncate": (I, [P, P, I, I, I, D, PP, IP, DP, DP, DP]),
     "hh_enlarge_operator": (I, [P, I, P, P, I, I, PP]),
     "hh_ham_add_bond": (I, [P, P, P, P, I, P, DP, I, I]),
+    "hh_block_product": (I, [P, P, P, I, P, DP, PP]),
     "hh_ham_add_product": (I, [P, P, P, P, DP]),
     "hh_block_copy": (I, [P, P, PP]),
     "hh_wave_random": (I, [P, C.c_ulonglong]),

@@ -360,6 +360,97 @@ extern "C" int hh_ham_add_product(hh_ctx_t* ctx, hh_block_t* ham, const hh_block
   return cuda_check(ctx, e, "ham_add_product");
 }
 
+// block_mul_block_ndia with flags 'N', 'N' (code/space_info.f90:373-631):
+// *out = coef (o1 o2)^K in the basis B, K = down_dif / 2.  Sub-blocks follow
+// the basis: for each sector (N, 2S) and each 2S' within down_dif of 2S whose
+// sector (N + up_dif, 2S') exists.  The reduced product is the regular matrix
+// element at the stretched projections (M' = S', M = S) by the
+// Wigner-Eckart theorem, summed over the intermediate projection with the
+// Clebsch-Gordan coefficient of the coupling, divided by the product's own
+// 3j at those projections; one FP64 segment GEMM per intermediate spin.
+extern "C" int hh_block_product(hh_ctx_t* ctx, const hh_block_t* o1, const hh_block_t* o2, int down_dif,
+                                const hh_basis_t* B, const double* coef, hh_block_t** out) {
+  if (!ctx || !o1 || !o2 || !B || !coef || !out || down_dif < 0) return HH_ERR_INVALID;
+  *out = nullptr;
+  const int up_dif = o1->up_dif + o2->up_dif, k1 = o1->down_dif, k2 = o2->down_dif, K = down_dif;
+  std::vector<int> qn;
+  for (const auto& sec : B->secs)
+    for (int nnd = std::abs(sec.down - K); nnd <= sec.down + K; nnd += SU) {
+      int l = B->find(sec.up + up_dif, nnd);
+      if (l >= 0) qn.insert(qn.end(), {sec.up, sec.down, nnd - sec.down, B->secs[l].dim, sec.dim});
+    }
+  hh_block* nb = nullptr;
+  int st = new_block(ctx, B->len, up_dif, K, qn, &nb);
+  if (st) return st;
+  hh_gemm_list L;
+  for (size_t i = 0; i < nb->subs.size(); ++i) {
+    const auto& s = nb->subs[i];
+    const int nd = s.down, nnd = s.down + s.dd, q = s.dd;
+    const double norm = w3j(nnd, K, nd, -nnd, q, nd);
+    const int seg0 = (int)L.segs.size();
+    for (int md = std::abs(nd - k2); md <= nd + k2; md += SU) {
+      const int ib = o2->find3(s.up, nd, md - nd), ia = o1->find3(s.up + o2->up_dif, md, nnd - md);
+      if (ia < 0 || ib < 0) continue;
+      if (o1->subs[ia].row != s.row || o2->subs[ib].sdim != s.sdim || o1->subs[ia].sdim != o2->subs[ib].row) {
+        hh_block_free(nb);
+        return fail(ctx, HH_ERR_INVALID, "block product: factor dimensions do not match the basis");
+      }
+      double c = 0.0;
+      for (int mm = -md; mm <= md; mm += SU) {
+        const int q1 = nnd - mm, q2 = mm - nd;
+        double ea = w3j(nnd, k1, md, -nnd, q1, mm);
+        double eb = w3j(md, k2, nd, -mm, q2, nd);
+        if (((md - mm) / 2) & 1) eb = -eb;
+        double cgk = w3j(k1, k2, K, q1, q2, -q) * std::sqrt(K + 1.0);
+        if (((-k1 + k2 + q) / 2) & 1) cgk = -cgk;
+        c += ea * eb * cgk;
+      }
+      if (c == 0.0 || o1->subs[ia].sdim == 0) continue;
+      c /= norm;
+      hh_seg g{};
+      g.poff = addr_of(o1, ia);
+      g.pbase = HH_BASE_ABS;
+      g.ldp = o1->subs[ia].row;
+      g.opP = HH_OP_N;
+      g.qoff = addr_of(o2, ib);
+      g.qbase = HH_BASE_ABS;
+      g.ldq = o2->subs[ib].row;
+      g.opQ = HH_OP_N;
+      g.K = o1->subs[ia].sdim;
+      g.kind = HH_SEG_GEMM;
+      g.cre = coef[0] * c;
+      g.cim = coef[1] * c;
+      L.segs.push_back(g);
+    }
+    const int nseg = (int)L.segs.size() - seg0;
+    if (nseg == 0 || s.row == 0 || s.sdim == 0) continue;
+    for (int m0 = 0; m0 < s.row; m0 += 64)
+      for (int n0 = 0; n0 < s.sdim; n0 += 64) {
+        hh_tile t{};
+        t.ooff = s.off;
+        t.obase = HH_BASE_OUT;
+        t.ldo = s.row;
+        t.M = s.row;
+        t.N = s.sdim;
+        t.m0 = m0;
+        t.n0 = n0;
+        t.seg0 = seg0;
+        t.nseg = nseg;
+        t.accumulate = 1;
+        L.tiles.push_back(t);
+      }
+  }
+  L.upload(ctx);
+  cudaError_t e = launch_segment_gemm_fp64(L, nullptr, nullptr, nb->d, ctx->stream);
+  L.release();
+  if (e != cudaSuccess) {
+    hh_block_free(nb);
+    return cuda_check(ctx, e, "block product");
+  }
+  *out = nb;
+  return HH_OK;
+}
+
 // block_transfer (code/space_info.f90:100-129): a device copy of a block.
 extern "C" int hh_block_copy(hh_ctx_t* ctx, const hh_block_t* src, hh_block_t** out) {
   if (!ctx || !src || !out) return HH_ERR_INVALID;

@@ -282,6 +282,7 @@ inline int split_of(int precision) {
   return precision == HH_PREC_BF16X6 ? 3 : precision == HH_PREC_BF16X3 ? 2 : 0;
 }
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
+double w3j(int j1, int j2, int j3, int m1, int m2, int m3);
 int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, double* z);
 // Eigenvalues (ascending, into *d_w: sector k's at the sum of the earlier
 // dims) and eigenvectors (in place) of the Hermitian sectors A + offs[k] of

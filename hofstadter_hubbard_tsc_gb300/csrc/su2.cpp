@@ -52,6 +52,32 @@ static double w6j_eval(int j1, int j2, int j3, int l1, int l2, int l3) {
   return s * std::sqrt(delta(j1, j2, j3) * delta(j1, l2, l3) * delta(l1, j2, l3) * delta(l1, l2, j3));
 }
 
+// Wigner 3j symbol (j1 j2 j3; m1 m2 m3), doubled arguments, by Racah's
+// single-sum formula.  Every half-sum below is exact: the triangle and
+// projection parities make each numerator even.
+double w3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  std::call_once(g_fact_once, init_fact);
+  if (m1 + m2 + m3 != 0 || j1 < 0 || j2 < 0 || j3 < 0 || !tri_ok(j1, j2, j3)) return 0.0;
+  if (std::abs(m1) > j1 || std::abs(m2) > j2 || std::abs(m3) > j3) return 0.0;
+  if (((j1 - m1) & 1) || ((j2 - m2) & 1) || ((j3 - m3) & 1)) return 0.0;
+  if ((j1 + j2 + j3) / 2 + 1 > 301) return std::nan("");
+  int kmin = 0;
+  if ((j2 - j3 - m1) / 2 > kmin) kmin = (j2 - j3 - m1) / 2;
+  if ((j1 - j3 + m2) / 2 > kmin) kmin = (j1 - j3 + m2) / 2;
+  int kmax = (j1 + j2 - j3) / 2;
+  if ((j1 - m1) / 2 < kmax) kmax = (j1 - m1) / 2;
+  if ((j2 + m2) / 2 < kmax) kmax = (j2 + m2) / 2;
+  double s = 0.0;
+  for (int k = kmin; k <= kmax; ++k) {
+    double den = g_fact[k] * g_fact[(j1 + j2 - j3) / 2 - k] * g_fact[(j1 - m1) / 2 - k] *
+                 g_fact[(j2 + m2) / 2 - k] * g_fact[(j3 - j2 + m1) / 2 + k] * g_fact[(j3 - j1 - m2) / 2 + k];
+    s += (k & 1 ? -1.0 : 1.0) / den;
+  }
+  double pre = std::sqrt(delta(j1, j2, j3) * g_fact[(j1 + m1) / 2] * g_fact[(j1 - m1) / 2] * g_fact[(j2 + m2) / 2] *
+                         g_fact[(j2 - m2) / 2] * g_fact[(j3 + m3) / 2] * g_fact[(j3 - m3) / 2]);
+  return (((j1 - j2 - m3) / 2) & 1 ? -1.0 : 1.0) * pre * s;
+}
+
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3) {
   std::call_once(g_fact_once, init_fact);
   static thread_local std::unordered_map<uint64_t, double> memo;

@@ -47,6 +47,15 @@ kernel of its geometry (the Hamiltonian's own t term, code/mat_vec.f90:
 3502-3615) with coefficient 1 and with i.  That term holds X + X^+ with
 X = sum_s c+_as c_bs / sqrt(2), so Re G = <T_1> / sqrt(2) and
 Im G = -<T_i> / sqrt(2).
+
+Cross-cut singlet-pair correlations <D+_x D_y> (Get_mSCOP_Operator_cor0,
+code/correlation.f90:198-327): the pair creator of a bond inside a block is
+the product of the two sites' elec_up operators in the basis of the later
+site, coupled to rank 0 (block_mul_block_ndia, hh_block_product), truncated
+and carried as a boson operator.  sys_block_env_block_cor_ndia
+(code/correlation.f90:1666-1929) has the coefficients of the block-block
+term with the environment creator untransposed; that term also holds its
+h.c., so with coefficients 1 and i, <D+_x D_y> = (<T_1> - i <T_i>) / 2.
 """
 import ctypes as C
 
@@ -135,6 +144,34 @@ def _hop_pair_operators(dev, op, site, a, b, length, bases, truns, side):
             cur = update_trun(dev, _embed(dev, 0, cur, bases[L][1], side), truns[L], dia=True)
         out.append(cur)
     return out
+
+
+def _fermion_in_basis(dev, op, a, b, bases, truns, side):
+    """Get_sys_oper_ndia / Get_env_oper_ndia with Truns = .false.
+    (code/get_ham.f90:1631-1695): the fermion operator of site a in the
+    enlarged, untruncated basis of length b >= a."""
+    if a == b:
+        return op if b <= 1 else _embed(dev, 3, op, bases[b][1], side, "F")
+    cur = _carry(dev, op, a, b - 1, bases, truns, side, rank1=True, flag="F")
+    return _embed(dev, 2, cur, bases[b][1], side, "F")
+
+
+def _pair_creator(dev, up, a, b, length, bases, truns, side):
+    """Singlet pair creator [c+_a c+_b]^0 of block sites a < b
+    (Get_SCOP_Operator_Sys / _Env with 'S0', code/correlation.f90:2659-2772):
+    the product of the two elec_up operators in the basis of length b
+    (hh_block_product, rank 0), truncated, then carried as a boson operator
+    to the block of `length` sites."""
+    A = _fermion_in_basis(dev, up, a, b, bases, truns, side)
+    Bo = _fermion_in_basis(dev, up, b, b, bases, truns, side)
+    h = C.c_void_p()
+    one = np.array([1.0, 0.0])
+    dev.check(dev.lib.hh_block_product(dev.h, A.h, Bo.h, 0, bases[b][1].h, one.ctypes.data_as(C.POINTER(C.c_double)),
+                                       C.byref(h)))
+    cur = update_trun(dev, DBlock.from_handle(dev, h), truns[b], dia=False)
+    for L in range(b + 1, length + 1):
+        cur = update_trun(dev, _embed(dev, 2, cur, bases[L][1], side, "B"), truns[L], dia=False)
+    return cur
 
 
 class Measurement:
@@ -257,6 +294,34 @@ class Measurement:
                     phi.free()
                 m[ia, sb.index(b)] = (t[0] - 1j * t[1]) / np.sqrt(2.0)
         return sa, sb, m
+
+    def pairing_correlations(self, sys_bonds, env_bonds):
+        """Cross-cut singlet-pair correlations <D+_x D_y> of
+        Get_mSCOP_Operator_cor0 (code/correlation.f90:198-327) for bonds x
+        inside the system block and y inside the environment block (sites in
+        the output numbering): (len(sys_bonds), len(env_bonds)) complex."""
+        d, dev, N, w = self.d, self.dev, self.N, self.wave
+        up = d.d_st["elec_up"]
+        for a, b in sys_bonds:
+            if not (1 <= min(a, b) < max(a, b) <= self.Ls):
+                raise ValueError(f"bond ({a}, {b}) is not inside the system block (sites 1..{self.Ls})")
+        for a, b in env_bonds:
+            if not (N - self.Le + 1 <= min(a, b) < max(a, b) <= N):
+                raise ValueError(f"bond ({a}, {b}) is not inside the environment block "
+                                 f"(sites {N - self.Le + 1}..{N})")
+        A = [_pair_creator(dev, up, min(a, b), max(a, b), self.Ls, d.sys_bases, d.sys_truns, 0) for a, b in sys_bonds]
+        B = [_pair_creator(dev, up, min(N - a + 1, N - b + 1), max(N - a + 1, N - b + 1), self.Le, d.env_bases,
+                           d.env_truns, 1) for a, b in env_bonds]
+        m = np.zeros((len(A), len(B)), dtype=np.complex128)
+        for i, x in enumerate(A):
+            for j, y in enumerate(B):
+                t = []
+                for coef in (1.0, 1j):
+                    phi = self._apply(_lib.BLOCK_VEC_BLOCK_NDIA, x, y, 0, "B", coef)
+                    t.append(w.dot(phi))
+                    phi.free()
+                m[i, j] = (t[0] - 1j * t[1]) / 2.0
+        return m
 
     def density_correlations(self, name="num_elec"):
         """<n_i n_j> for all sites i, j (N x N): cross-cut pairs, same-side

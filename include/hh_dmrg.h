@@ -249,6 +249,11 @@ int hh_ham_add_bond(hh_ctx_t* ctx, hh_block_t* ham, const hh_block_t* block, con
 /* Get_hamiltonian_dia (code/get_ham.f90:852-941): ham += coef/sqrt(2S+1) O1 O2 */
 int hh_ham_add_product(hh_ctx_t* ctx, hh_block_t* ham, const hh_block_t* o1, const hh_block_t* o2,
                        const double* coef);
+/* block_mul_block_ndia, flags 'N' 'N' (code/space_info.f90:373-631):
+ * *out = coef (o1 o2)^K, the product of two operators of one block coupled
+ * to rank K = down_dif / 2, laid out over the sectors of the basis B.      */
+int hh_block_product(hh_ctx_t* ctx, const hh_block_t* o1, const hh_block_t* o2, int down_dif,
+                     const hh_basis_t* B, const double* coef, hh_block_t** out);
 /* block_transfer (code/space_info.f90:100-129): device copy of a block     */
 int hh_block_copy(hh_ctx_t* ctx, const hh_block_t* src, hh_block_t** out);
 

@@ -12,7 +12,7 @@ reference produces, a dictionary of the first matching index is equivalent.
 """
 import numpy as np
 
-from .su2 import w6j, parity_sign
+from .su2 import w3j, w6j, parity_sign
 
 SU = 2  # code/pubdata.f90:11 (su=2: spin steps in doubled units)
 
@@ -122,6 +122,53 @@ def block_add_block_two(block1, coef1, new_block):
 # ---------------------------------------------------------------------------
 # Bases
 # ---------------------------------------------------------------------------
+def _odd(n):
+    return -1.0 if n % 2 else 1.0
+
+
+def block_mul_block_ndia(op1, op2, down_dif, basis, coef=1.0):
+    """(op1 op2)^K, K = down_dif / 2: the product of two operators of one
+    block coupled to rank K (block_mul_block_ndia with flags 'N', 'N',
+    code/space_info.f90:373-631).  For each sector (N, 2S) of the basis and
+    each 2S' = |2S - down_dif| .. 2S + down_dif whose sector (N + up_dif,
+    2S') exists, the reduced matrix of the product is the regular matrix
+    element at the stretched projections M' = S', M = S, built by the
+    Wigner-Eckart theorem (<S' M'|T^k_q|S M> = (-1)^(S'-M') (S' k S; -M' q M)
+    <S'||T^k||S>) from the two factors summed over the intermediate
+    projection with the Clebsch-Gordan coefficient of the coupling
+    (-1)^(-k1+k2+q) sqrt(2K+1) (k1 k2 K; q1 q2 -q), divided by the 3j of the
+    product at the same projections.  Intermediate spins run over
+    |2S - k2| .. 2S + k2; a product term needs both factor sub-blocks."""
+    up_dif = op1.up_dif + op2.up_dif
+    k1, k2, K = op1.down_dif, op2.down_dif, down_dif
+    subs = []
+    for sec in basis.sectors:
+        nu, nd = sec.new_num_up, sec.new_num_down
+        for nnd in range(abs(nd - K), nd + K + 1, SU):
+            tgt = basis.find(nu + up_dif, nnd)
+            if tgt is None:
+                continue
+            sub = Sub(nu, nd, nnd - nd, tgt.dim, sec.dim)
+            subs.append(sub)
+            q = nnd - nd
+            norm = w3j(nnd, K, nd, -nnd, q, nd)
+            for md in range(abs(nd - k2), nd + k2 + 1, SU):
+                ib = op2.find(nu, nd, md - nd)
+                ia = op1.find(nu + op2.up_dif, md, nnd - md)
+                if ia is None or ib is None:
+                    continue
+                c = 0.0
+                for mm in range(-md, md + 1, SU):
+                    q1, q2 = nnd - mm, mm - nd
+                    ea = w3j(nnd, k1, md, -nnd, q1, mm)
+                    eb = w3j(md, k2, nd, -mm, q2, nd) * _odd((md - mm) // 2)
+                    cgk = w3j(k1, k2, K, q1, q2, -q) * _odd((-k1 + k2 + q) // 2) * np.sqrt(K + 1.0)
+                    c += ea * eb * cgk
+                if c != 0.0:
+                    sub.mat += (coef * c / norm) * (op1.subs[ia].mat @ op2.subs[ib].mat)
+    return Block(basis.len, up_dif, K, subs)
+
+
 class BSub:
     __slots__ = ("spos", "sdim", "bl_num_up", "bl_num_down", "st_num_up", "st_num_down")
 

@@ -263,9 +263,9 @@ def hubbard_spin_correlations(lat, n_up, n_dn):
     return float(e0), ss, 3.0 * szsz
 
 
-def hubbard_green(lat, n_up, n_dn):
-    """Lowest state of the (n_up, n_dn) sector: energy and
-    G_ij = sum_s <c+_is c_js> (complex, sites in lattice order)."""
+def _hubbard_ground(lat, n_up, n_dn):
+    """Lowest state of the (n_up, n_dn) sector of the Hubbard model: energy,
+    state (up configuration major), up and down configurations."""
     N = lat.N
     cu = _configs(N, n_up)
     cd = _configs(N, n_dn)
@@ -283,6 +283,16 @@ def hubbard_green(lat, n_up, n_dn):
     else:
         w, v = spla.eigsh(H, k=1, which="SA", tol=1e-13)
         e0, psi = w[0], v[:, 0]
+    return float(e0), psi, cu, cd
+
+
+def hubbard_green(lat, n_up, n_dn):
+    """Lowest state of the (n_up, n_dn) sector: energy and
+    G_ij = sum_s <c+_is c_js> (complex, sites in lattice order)."""
+    N = lat.N
+    e0, psi, cu, cd = _hubbard_ground(lat, n_up, n_dn)
+    au = np.array(cu, dtype=np.int64)
+    ad = np.array(cd, dtype=np.int64)
     G = np.zeros((N, N), dtype=np.complex128)
     Iu, Id = sp.identity(len(cu), format="csr"), sp.identity(len(cd), format="csr")
     occ_u = np.array([[(c >> s) & 1 for s in range(N)] for c in au], dtype=np.float64)
@@ -296,3 +306,40 @@ def hubbard_green(lat, n_up, n_dn):
                 op = sp.kron(_pair_hop(cu, i, j), Id, format="csr") + sp.kron(Iu, _pair_hop(cd, i, j), format="csr")
                 G[i, j] = np.vdot(psi, op @ psi)
     return float(e0), G
+
+
+def _annihilate(src, dst, site):
+    """c_site from configurations src to dst of one spin species, with the
+    sign of the occupied sites below site."""
+    idx = {c: n for n, c in enumerate(dst)}
+    low = (1 << site) - 1
+    rows, cols, vals = [], [], []
+    for n, c in enumerate(src):
+        if (c >> site) & 1:
+            rows.append(idx[c ^ (1 << site)]); cols.append(n)
+            vals.append(-1.0 if bin(c & low).count("1") % 2 else 1.0)
+    return sp.csr_matrix((vals, (rows, cols)), shape=(len(dst), len(src)), dtype=np.complex128)
+
+
+def hubbard_pair_correlations(lat, n_up, n_dn, bonds):
+    """Lowest state of the (n_up, n_dn) sector: energy and the singlet-pair
+    correlations P[x, y] = <D+_x D_y> for the given bonds (i, j) (sites in
+    lattice order, 1-based), D+_ij = (c+_i,up c+_j,dn - c+_i,dn c+_j,up) /
+    sqrt(2).  Up operators are ordered before down operators."""
+    N = lat.N
+    e0, psi, cu, cd = _hubbard_ground(lat, n_up, n_dn)
+    cu1, cd1 = _configs(N, n_up - 1), _configs(N, n_dn - 1)
+    Psi = psi.reshape(len(cu), len(cd))
+    up = [_annihilate(cu, cu1, s) for s in range(N)]
+    dn = [_annihilate(cd, cd1, s) for s in range(N)]
+    su0 = -1.0 if n_up % 2 else 1.0           # down operator passing the n_up up electrons
+    su1 = -1.0 if (n_up - 1) % 2 else 1.0     # ... after one up electron was removed
+    vecs = []
+    for (i, j) in bonds:
+        a, b = i - 1, j - 1
+        # D_ij = (c_j,dn c_i,up - c_j,up c_i,dn) / sqrt(2)
+        t1 = su1 * (up[a] @ Psi) @ dn[b].T
+        t2 = up[b] @ (su0 * Psi @ dn[a].T)
+        vecs.append(np.asarray(t1 - t2).ravel() / np.sqrt(2.0))
+    P = np.array([[np.vdot(vx, vy) for vy in vecs] for vx in vecs])
+    return e0, P

@@ -38,7 +38,9 @@ the unit-coefficient term: <S_a . S_b> = -sqrt(3) <psi|T_ab psi>.
 import numpy as np
 
 from .blocks import (Block, Sub, update_site_dia, update_block_dia, update_trun_dia, wave_product,
-                     update_site_ndia, update_block_ndia, update_trun_ndia, block_transfer_trans)
+                     update_site_ndia, update_block_ndia, update_trun_ndia, block_transfer_trans,
+                     block_mul_block_ndia, SU)
+from .su2 import w6j
 from .enlarge import get_hamiltonian_dia, get_hamiltonian_ndia
 from .matvec import (block_vec_dia, vec_block_dia, site_vec_site_dia, block_vec_block_ndia, block_vec_site_ndia,
                      site_vec_block_ndia, site_vec_site_ndia, block_site_vec_dia, vec_block_site_dia,
@@ -397,3 +399,109 @@ def electron_correlations_all(d):
     for i in range(N):
         G[i, i] = n[i]
     return G
+
+
+def _fermion_in_basis(op, a, b, bases, truns, side):
+    """Get_sys_oper_ndia / Get_env_oper_ndia with Truns = .false.
+    (code/get_ham.f90:1631-1695): the operator of site a in the enlarged,
+    untruncated basis of length b >= a."""
+    if a == b:
+        return op.copy() if b <= 1 else update_site_ndia(op, bases[b], "F", side)
+    cur = _carry_fermion(op, a, b - 1, bases, truns, side)
+    return update_block_ndia(cur, bases[b], "F", side)
+
+
+def pair_creator(d, a, b, side):
+    """Singlet pair creator [c+_a c+_b]^0 of block sites a < b (Get_SCOP_Operator_Sys /
+    Get_SCOP_Operator_Env with 'S0', code/correlation.f90:2659-2772):
+    elec_up of both sites in the enlarged basis of length b, their product
+    coupled to rank 0 (block_mul_block_ndia), truncated, then carried as a
+    boson operator to the block of the current superblock (Change_sys_oper_ndia,
+    code/get_ham.f90:1767-1818)."""
+    if side == "sys":
+        bases, truns, length = d.sys_bases, d.sys_truns, d.wave.sys_len - 1
+    else:
+        bases, truns, length = d.env_bases, d.env_truns, d.wave.env_len - 1
+    up = d.st.elec_up
+    P = block_mul_block_ndia(_fermion_in_basis(up, a, b, bases, truns, side),
+                             _fermion_in_basis(up, b, b, bases, truns, side), 0, bases[b])
+    cur = update_trun_ndia(P, truns[b])
+    for L in range(b + 1, length + 1):
+        cur = update_trun_ndia(update_block_ndia(cur, bases[L], "B", side), truns[L])
+    return cur
+
+
+def sys_block_env_block_cor_ndia(sys_bl, env_bl, sys_bs, env_bs, wave):
+    """<(A x 1) psi | (1 x B) psi> for a system block operator A and an
+    environment block operator B of the same rank k and the same up_dif,
+    boson sign (sys_block_env_block_cor_ndia with 'B',
+    code/correlation.f90:1666-1929): each operator re-coupled into its
+    enlarged basis with the 6j of its block and site, times
+    sqrt((2S'+1)(2S+1)/(k+1)) and the phase of the two recouplings."""
+    up_dif, k = sys_bl.up_dif, sys_bl.down_dif
+    value = 0.0 + 0.0j
+    for w in wave.subs:
+        ss = sys_bs.find(w.sys_num_up, w.sys_num_down)
+        es = env_bs.find(w.env_num_up, w.env_num_down)
+        if ss is None or es is None:
+            continue
+        for m in ss.subs:
+            for n in es.subs:
+                for dd in range(-k, k + 1, SU):
+                    sid = sys_bl.find(m.bl_num_up, m.bl_num_down, dd)
+                    nsbu, nsbd = m.bl_num_up + up_dif, m.bl_num_down + dd
+                    for edd in range(-k, k + 1, SU):
+                        nebu, nebd = n.bl_num_up - up_dif, n.bl_num_down - edd
+                        eid = env_bl.find(nebu, nebd, edd)
+                        if sid is None or eid is None:
+                            continue
+                        for nsd in range(abs(w.sys_num_down - k), w.sys_num_down + k + 1, SU):
+                            nsu, neu, ned = w.sys_num_up + up_dif, w.env_num_up - up_dif, nsd
+                            ts, te = sys_bs.find(nsu, nsd), env_bs.find(neu, ned)
+                            ms = ts.find_full(nsbu, nsbd, m.st_num_up, m.st_num_down) if ts else None
+                            me = te.find_full(nebu, nebd, n.st_num_up, n.st_num_down) if te else None
+                            kk = wave.find(nsu, nsd, neu, ned)
+                            if ms is None or me is None or kk is None:
+                                continue
+                            c1 = w6j(nsd, k, w.sys_num_down, m.bl_num_down, m.st_num_down, nsbd)
+                            if c1 == 0.0:
+                                continue
+                            c1 *= w6j(ned, k, w.env_num_down, n.bl_num_down, n.st_num_down, nebd)
+                            if c1 == 0.0:
+                                continue
+                            c1 *= np.sqrt((1.0 + ned) * (1.0 + w.env_num_down) / (1.0 + k))
+                            if ((nsbd + m.st_num_down + w.sys_num_down + k) // 2
+                                    + (nebd + n.st_num_down + w.env_num_down + k) // 2) % 2 == 1:
+                                c1 = -c1
+                            x = w.vec[m.spos:m.spos + m.sdim, n.spos:n.spos + n.sdim]
+                            y = wave.subs[kk].vec[ms.spos:ms.spos + ms.sdim, me.spos:me.spos + me.sdim]
+                            m1 = sys_bl.subs[sid].mat @ x
+                            m2 = c1 * (y @ env_bl.subs[eid].mat.conj().T)
+                            value += np.vdot(m1, m2)
+    return value
+
+
+def pairing_correlations(d, sys_bonds, env_bonds):
+    """Cross-cut singlet-pair correlations of Get_mSCOP_Operator_cor0
+    (code/correlation.f90:198-327): for a bond (a, a') inside the system
+    block and a bond (b, b') inside the environment block (sites in the
+    output numbering), the conjugate of sys_block_env_block_cor_ndia of the
+    two pair creators, <D+_(a,a') D_(b,b')> in the reference's reduced
+    normalisation.  Returns the (len(sys_bonds), len(env_bonds)) complex
+    matrix."""
+    wave = d.wave
+    N = d.lat.N
+    Ls, Le = wave.sys_len - 1, wave.env_len - 1
+    for a, b in sys_bonds:
+        if not (1 <= min(a, b) < max(a, b) <= Ls):
+            raise ValueError(f"bond ({a}, {b}) is not inside the system block")
+    for a, b in env_bonds:
+        if not (N - Le + 1 <= min(a, b) < max(a, b) <= N):
+            raise ValueError(f"bond ({a}, {b}) is not inside the environment block")
+    sys_bs, env_bs = d.sys_bases[wave.sys_len], d.env_bases[wave.env_len]
+    A = [pair_creator(d, min(a, b), max(a, b), "sys") for a, b in sys_bonds]
+    B = []
+    for a, b in env_bonds:
+        ea, eb = N - a + 1, N - b + 1
+        B.append(pair_creator(d, min(ea, eb), max(ea, eb), "env"))
+    return np.array([[np.conj(sys_block_env_block_cor_ndia(x, y, sys_bs, env_bs, wave)) for y in B] for x in A])

@@ -59,7 +59,7 @@ def w6j(j1, j2, j3, l1, l2, l3):
 
 
 def w3j(j1, j2, j3, m1, m2, m3):
-    """Wigner 3j symbol, doubled arguments (Racah formula; used by tests only)."""
+    """Wigner 3j symbol, doubled arguments (Racah formula)."""
     if m1 + m2 + m3 != 0 or not _tri_ok(j1, j2, j3):
         return 0.0
     if abs(m1) > j1 or abs(m2) > j2 or abs(m3) > j3:

@@ -7,7 +7,8 @@ are known answers of this project's own independent code paths:
 * ed_known_answers.json: Fock-basis exact diagonalisation (oracle/ed.py,
   which shares nothing with the SU(2) code) of a Hubbard flux ladder and a
   t-J ladder: singlet ground energies, and for the Hubbard ladder the density,
-  spin and electron (sum_s <c+_i c_j>, complex) correlation matrices;
+  spin and electron (sum_s <c+_i c_j>, complex) correlation matrices and
+  singlet-pair correlations <D+_x D_y> of bonds on either side of the middle;
 * matvec_tj_2x6.npz and matvec_hubbard_4x4.npz: a seeded input vector and the
   oracle's model_wave of it on small synthetic mid-chain superblocks
   (hofstadter_hubbard_tsc_gb300/synth.py).
@@ -26,6 +27,8 @@ from oracle.lattice import Lattice  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
+PAIR_BONDS = [[1, 2], [8, 7], [7, 6], [6, 5], [8, 6], [7, 5], [8, 5]]
+
 MATVEC_CASES = {
     "matvec_tj_2x6": dict(W=2, L=6, n_elec=10, m=24, model="tj", J=0.4, phi=1.0 / 6.0),
     "matvec_hubbard_4x4": dict(W=4, L=4, n_elec=14, m=30, phi=0.25),
@@ -38,11 +41,14 @@ def ed_fixtures():
     _, dens, corr = ed.hubbard_density_correlations(hub, 3, 3)
     _, ss, _ = ed.hubbard_spin_correlations(hub, 3, 3)
     _, G = ed.hubbard_green(hub, 3, 3)
+    _, P = ed.hubbard_pair_correlations(hub, 3, 3, PAIR_BONDS)
     tj = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
     e_t = ed.tj_singlet_ground_energy(tj, 6)
     return {
         "hubbard_2x4_U8_phi0.25_Ne6": {"energy": float(e_h), "density": dens.tolist(), "nn": corr.tolist(),
-                                       "ss": ss.tolist(), "green_re": G.real.tolist(), "green_im": G.imag.tolist()},
+                                       "ss": ss.tolist(), "green_re": G.real.tolist(), "green_im": G.imag.tolist(),
+                                       "pair_bonds": PAIR_BONDS, "pair_re": P.real.tolist(),
+                                       "pair_im": P.imag.tolist()},
         "tj_2x4_J0.4_phi1/6_Ne6": {"energy": float(e_t)},
     }
 

@@ -26,6 +26,10 @@ def _green(g):
     return np.array(g["green_re"]) + 1j * np.array(g["green_im"])
 
 
+def _pair(g):
+    return np.array(g["pair_re"]) + 1j * np.array(g["pair_im"])
+
+
 def _matvec(name):
     z = np.load(os.path.join(HERE, name + ".npz"))
     return z["psi"], z["hpsi"]
@@ -40,6 +44,8 @@ def test_ed_reproduces_fixture():
     np.testing.assert_allclose(ss, np.array(g["ss"]), atol=1e-12)
     _, G = ed.hubbard_green(hub, 3, 3)
     np.testing.assert_allclose(G, _green(g), atol=1e-12)
+    _, P = ed.hubbard_pair_correlations(hub, 3, 3, [tuple(b) for b in g["pair_bonds"]])
+    np.testing.assert_allclose(P, _pair(g), atol=1e-12)
 
 
 def test_oracle_dmrg_reproduces_fixture():
@@ -51,6 +57,9 @@ def test_oracle_dmrg_reproduces_fixture():
     d.left_to_right(1, 3)
     np.testing.assert_allclose(om.density_correlations(d), np.array(g["hubbard_2x4_U8_phi0.25_Ne6"]["nn"]), atol=1e-6)
     np.testing.assert_allclose(om.electron_correlations_all(d), _green(g["hubbard_2x4_U8_phi0.25_Ne6"]), atol=1e-6)
+    h = g["hubbard_2x4_U8_phi0.25_Ne6"]
+    bonds = [tuple(b) for b in h["pair_bonds"]]
+    np.testing.assert_allclose(om.pairing_correlations(d, bonds[:1], bonds[1:]), _pair(h)[:1, 1:], atol=1e-6)
     t = DMRG(Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0), 6, kept_min=300, kept_max=300, trun_err=1e-14,
              lanzero=1e-11, seed=3)
     assert t.run(sweeps=1) == pytest.approx(g["tj_2x4_J0.4_phi1/6_Ne6"]["energy"], abs=1e-9)
@@ -94,3 +103,5 @@ def test_gpu_dmrg_golden(device):
     np.testing.assert_allclose(m.density_correlations(), np.array(g["nn"]), atol=1e-6)
     np.testing.assert_allclose(m.spin_correlations_all(), np.array(g["ss"]), atol=1e-6)
     np.testing.assert_allclose(m.electron_correlations_all(), _green(g), atol=1e-6)
+    bonds = [tuple(b) for b in g["pair_bonds"]]
+    np.testing.assert_allclose(m.pairing_correlations(bonds[:1], bonds[1:]), _pair(g)[:1, 1:], atol=1e-6)

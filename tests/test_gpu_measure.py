@@ -114,3 +114,22 @@ def test_electron_correlations_all_pairs(device, precision):
     d.left_to_right(1, lat.N // 2 - 1)
     _, G = ed.hubbard_green(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2)
     np.testing.assert_allclose(Measurement(d).electron_correlations_all(), G, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_pairing_correlations_exact(device, precision):
+    """Cross-cut singlet-pair correlations on the GPU state (pair creators
+    from hh_block_product, one-term block-block plans with coefficients 1 and
+    i) against exact diagonalisation."""
+    W, L, ne, U, phi = 2, 4, 6, 8.0, 0.25
+    sys_bonds = [(1, 2)]
+    env_bonds = [(8, 7), (7, 6), (6, 5), (8, 6), (7, 5), (8, 5)]
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    d.run(sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    _, P = ed.hubbard_pair_correlations(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2, sys_bonds + env_bonds)
+    m = Measurement(d)
+    np.testing.assert_allclose(m.pairing_correlations(sys_bonds, env_bonds), P[:1, 1:], atol=1e-6)
+    with pytest.raises(ValueError):
+        m.pairing_correlations([(2, 3)], env_bonds)

@@ -129,3 +129,41 @@ def test_electron_correlations_all_pairs(W, L, ne, U, phi):
     m = om.electron_correlations_all(d)
     np.testing.assert_allclose(m, m.conj().T, atol=1e-12)
     np.testing.assert_allclose(m, G, atol=1e-6)
+
+
+PAIR_SYS = [(1, 2)]
+PAIR_ENV = [(8, 7), (7, 6), (6, 5), (8, 6), (7, 5), (8, 5)]
+
+
+@pytest.mark.parametrize("W,L,nu,phi", [(2, 3, 2, 0.0), (2, 4, 3, 0.25)])
+def test_exact_pair_correlations_wick(W, L, nu, phi):
+    """At U = 0 (a single Slater determinant per spin) the exact singlet-pair
+    correlation is <D+_ab D_cd> = g_ac g_bd + g_ad g_bc with the per-spin
+    one-body matrix g = G / 2."""
+    lat = Lattice(W, L, U=0.0, phi=phi)
+    bonds = [(1, 2), (1, 3), (2, 4), (3, 5), (4, 6), (5, 6)]
+    _, P = ed.hubbard_pair_correlations(lat, nu, nu, bonds)
+    _, G = ed.hubbard_green(lat, nu, nu)
+    g = G / 2
+    wick = np.array([[g[a - 1, c - 1] * g[b - 1, d - 1] + g[a - 1, d - 1] * g[b - 1, c - 1] for (c, d) in bonds]
+                     for (a, b) in bonds])
+    np.testing.assert_allclose(P, wick, atol=1e-12)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 4, 4, 4.0, 0.3), (2, 4, 8, 4.0, 0.0)])
+def test_pairing_correlations_exact(W, L, ne, U, phi):
+    """Cross-cut singlet-pair correlations of the oracle (pair creators as
+    rank-0 products of two elec_up operators, block_mul_block_ndia; the
+    measurement of sys_block_env_block_cor_ndia) against the exact ground
+    state: the reference's reduced normalisation is <D+_x D_y> with
+    D+_ij = (c+_i,up c+_j,dn - c+_i,dn c+_j,up) / sqrt(2)."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    e0, P = ed.hubbard_pair_correlations(lat, ne // 2, ne // 2, PAIR_SYS + PAIR_ENV)
+    e, d = _dmrg(lat, ne, sweeps=1)
+    assert e == pytest.approx(e0, rel=1e-10)
+    d.left_to_right(1, lat.N // 2 - 1)
+    m = om.pairing_correlations(d, PAIR_SYS, PAIR_ENV)
+    np.testing.assert_allclose(m, P[:len(PAIR_SYS), len(PAIR_SYS):], atol=1e-6)
+    with pytest.raises(ValueError):
+        om.pairing_correlations(d, [(2, 3)], PAIR_ENV)
