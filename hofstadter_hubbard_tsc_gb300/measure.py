@@ -56,6 +56,9 @@ and carried as a boson operator.  sys_block_env_block_cor_ndia
 (code/correlation.f90:1666-1929) has the coefficients of the block-block
 term with the environment creator untransposed; that term also holds its
 h.c., so with coefficients 1 and i, <D+_x D_y> = (<T_1> - i <T_i>) / 2.
+Same-side pairs (x before y inside the system block) multiply the creator
+of x by the two elec_down operators of y in turn (ranks 1/2, then 0) and
+measure the scalar with block_vec_dia (no h.c.): <T_1> - i <T_i>.
 """
 import ctypes as C
 
@@ -172,6 +175,48 @@ def _pair_creator(dev, up, a, b, length, bases, truns, side):
     for L in range(b + 1, length + 1):
         cur = update_trun(dev, _embed(dev, 2, cur, bases[L][1], side, "B"), truns[L], dia=False)
     return cur
+
+
+def _product(dev, o1, o2, down_dif, dbasis):
+    """hh_block_product: (o1 o2) coupled to rank down_dif / 2 in dbasis."""
+    h = C.c_void_p()
+    one = np.array([1.0, 0.0])
+    dev.check(dev.lib.hh_block_product(dev.h, o1.h, o2.h, down_dif, dbasis.h, one.ctypes.data_as(C.POINTER(C.c_double)),
+                                       C.byref(h)))
+    return DBlock.from_handle(dev, h)
+
+
+def _carry_untruncated(dev, op, a, b, bases, truns, side, flag):
+    """Change_sys_oper_ndia with Truns = .false. (code/get_ham.f90:1767-1818):
+    a block operator of the truncated block of length a embedded in the
+    enlarged, untruncated basis of length b > a."""
+    cur = op
+    for L in range(a + 1, b):
+        cur = update_trun(dev, _embed(dev, 2, cur, bases[L][1], side, flag), truns[L], dia=False)
+    return _embed(dev, 2, cur, bases[b][1], side, flag)
+
+
+def _pair_pair_operator(dev, up, dn, bond_x, bond_y, length, bases, truns):
+    """The scalar D+_x D_y of two bonds inside the system block, x before y
+    (Get_sys_two / Get_sys_two1, code/correlation.f90:331-428): the pair
+    creator of x truncated at its later site, embedded up to the first site
+    of y and multiplied by that site's elec_down (rank 1/2), truncated,
+    embedded (fermion) up to the second site of y and multiplied by its
+    elec_down to rank 0, then truncated and carried as a scalar."""
+    a1, a2 = sorted(bond_x)
+    a3, a4 = sorted(bond_y)
+    P = _product(dev, _fermion_in_basis(dev, up, a1, a2, bases, truns, 0),
+                 _fermion_in_basis(dev, up, a2, a2, bases, truns, 0), 0, bases[a2][1])
+    P = update_trun(dev, P, truns[a2], dia=False)
+    X = _product(dev, _carry_untruncated(dev, P, a2, a3, bases, truns, 0, "B"),
+                 _fermion_in_basis(dev, dn, a3, a3, bases, truns, 0), 1, bases[a3][1])
+    X = update_trun(dev, X, truns[a3], dia=False)
+    X = _product(dev, _carry_untruncated(dev, X, a3, a4, bases, truns, 0, "F"),
+                 _fermion_in_basis(dev, dn, a4, a4, bases, truns, 0), 0, bases[a4][1])
+    X = update_trun(dev, X, truns[a4], dia=True)
+    for L in range(a4 + 1, length + 1):
+        X = update_trun(dev, _embed(dev, 0, X, bases[L][1], 0), truns[L], dia=True)
+    return X
 
 
 class Measurement:
@@ -321,6 +366,31 @@ class Measurement:
                     t.append(w.dot(phi))
                     phi.free()
                 m[i, j] = (t[0] - 1j * t[1]) / 2.0
+        return m
+
+    def pairing_correlations_sys(self, bonds_x, bonds_y):
+        """Same-side singlet-pair correlations <D+_x D_y> of
+        Get_mSCOP_Operator_cor0 (code/correlation.f90:226-262) for bonds x
+        and y inside the system block, every site of x before every site of
+        y: measure_sys_block of the scalar D+_x D_y, as
+        <T_1> - i <T_i> of one-term block_vec_dia plans with coefficients 1
+        and i.  Returns the (len(bonds_x), len(bonds_y)) complex matrix."""
+        d, dev, w = self.d, self.dev, self.wave
+        for x in bonds_x:
+            for y in bonds_y:
+                if not (1 <= min(x) and max(x) < min(y) and max(y) <= self.Ls):
+                    raise ValueError(f"bonds {x}, {y} are not ordered inside the system block (sites 1..{self.Ls})")
+        up, dn = d.d_st["elec_up"], d.d_st["elec_down"]
+        m = np.zeros((len(bonds_x), len(bonds_y)), dtype=np.complex128)
+        for i, x in enumerate(bonds_x):
+            for j, y in enumerate(bonds_y):
+                O = _pair_pair_operator(dev, up, dn, x, y, self.Ls, d.sys_bases, d.sys_truns)
+                t = []
+                for coef in (1.0, 1j):
+                    phi = self._apply(_lib.BLOCK_VEC_DIA, O, coef=coef)
+                    t.append(w.dot(phi))
+                    phi.free()
+                m[i, j] = t[0] - 1j * t[1]
         return m
 
     def density_correlations(self, name="num_elec"):

@@ -505,3 +505,62 @@ def pairing_correlations(d, sys_bonds, env_bonds):
         ea, eb = N - a + 1, N - b + 1
         B.append(pair_creator(d, min(ea, eb), max(ea, eb), "env"))
     return np.array([[np.conj(sys_block_env_block_cor_ndia(x, y, sys_bs, env_bs, wave)) for y in B] for x in A])
+
+
+def _carry_untruncated(op, a, b, bases, truns, side, flag):
+    """Change_sys_oper_ndia with Truns = .false. (code/get_ham.f90:1767-1818):
+    a block operator of the truncated block of length a embedded in the
+    enlarged, untruncated basis of length b > a (truncated at the lengths in
+    between)."""
+    cur = op
+    for L in range(a + 1, b):
+        cur = update_trun_ndia(update_block_ndia(cur, bases[L], flag, side), truns[L])
+    return update_block_ndia(cur, bases[b], flag, side)
+
+
+def pair_pair_operator(d, bond_x, bond_y):
+    """The scalar D+_x D_y of two bonds inside the system block, bond x before
+    bond y (Get_sys_two and Get_sys_two1, code/correlation.f90:331-428): the
+    pair creator of x truncated at its later site, embedded up to the first
+    site of y, multiplied by that site's elec_down (rank 1/2) and truncated,
+    embedded (fermion) up to the second site of y and multiplied by its
+    elec_down to rank 0, then truncated and carried as a scalar to the
+    block of the superblock (Change_sys_oper_dia)."""
+    a1, a2 = sorted(bond_x)
+    a3, a4 = sorted(bond_y)
+    bases, truns, length = d.sys_bases, d.sys_truns, d.wave.sys_len - 1
+    up, dn = d.st.elec_up, d.st.elec_down
+    P = block_mul_block_ndia(_fermion_in_basis(up, a1, a2, bases, truns, "sys"),
+                             _fermion_in_basis(up, a2, a2, bases, truns, "sys"), 0, bases[a2])
+    P = update_trun_ndia(P, truns[a2])
+    X = block_mul_block_ndia(_carry_untruncated(P, a2, a3, bases, truns, "sys", "B"),
+                             _fermion_in_basis(dn, a3, a3, bases, truns, "sys"), 1, bases[a3])
+    X = update_trun_ndia(X, truns[a3])
+    X = block_mul_block_ndia(_carry_untruncated(X, a3, a4, bases, truns, "sys", "F"),
+                             _fermion_in_basis(dn, a4, a4, bases, truns, "sys"), 0, bases[a4])
+    X = update_trun_dia(X, truns[a4])
+    for L in range(a4 + 1, length + 1):
+        X = update_trun_dia(update_block_dia(X, bases[L]), truns[L])
+    return X
+
+
+def measure_sys_block(op, sys_bs, wave):
+    """<psi|(O x 1)|psi>, complex (measure_sys_block, code/measure.f90:611-673)."""
+    phi = wave.zeros_like()
+    block_vec_dia(op, sys_bs, wave, phi, 1.0)
+    return sum(np.vdot(w.vec, p.vec) for w, p in zip(wave.subs, phi.subs))
+
+
+def pairing_correlations_sys(d, bonds_x, bonds_y):
+    """Same-side singlet-pair correlations of Get_mSCOP_Operator_cor0
+    (code/correlation.f90:226-262): measure_sys_block of pair_pair_operator
+    for bonds x and y inside the system block, every site of x before every
+    site of y.  Returns the (len(bonds_x), len(bonds_y)) complex matrix."""
+    Ls = d.wave.sys_len - 1
+    for x in bonds_x:
+        for y in bonds_y:
+            if not (1 <= min(x) and max(x) < min(y) and max(y) <= Ls):
+                raise ValueError(f"bonds {x}, {y} are not ordered inside the system block")
+    sys_bs = d.sys_bases[d.wave.sys_len]
+    return np.array([[measure_sys_block(pair_pair_operator(d, x, y), sys_bs, d.wave) for y in bonds_y]
+                     for x in bonds_x])

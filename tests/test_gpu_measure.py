@@ -133,3 +133,21 @@ def test_pairing_correlations_exact(device, precision):
     np.testing.assert_allclose(m.pairing_correlations(sys_bonds, env_bonds), P[:1, 1:], atol=1e-6)
     with pytest.raises(ValueError):
         m.pairing_correlations([(2, 3)], env_bonds)
+
+
+@pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
+def test_pairing_correlations_same_side_exact(device, precision):
+    """Same-side singlet-pair correlations on the GPU state (products of the
+    pair creator with two elec_down operators by hh_block_product, the scalar
+    measured by block_vec_dia plans) against exact diagonalisation."""
+    W, L, ne, U, phi = 2, 4, 6, 8.0, 0.25
+    lat = SquareLattice(W, L, U=U, phi=phi)
+    d = GPUDMRG(device, lat, ne, kept_min=256, kept_max=256, trun_err=1e-14, lanzero=1e-11, precision=precision)
+    d.run(sweeps=1)
+    d.left_to_right(1, 5)
+    _, P = ed.hubbard_pair_correlations(Lattice(W, L, U=U, phi=phi), ne // 2, ne // 2, [(1, 2), (3, 4)])
+    m = Measurement(d)
+    assert m.Ls == 4
+    np.testing.assert_allclose(m.pairing_correlations_sys([(1, 2)], [(3, 4)]), P[:1, 1:], atol=1e-6)
+    with pytest.raises(ValueError):
+        m.pairing_correlations_sys([(1, 3)], [(2, 4)])

@@ -167,3 +167,21 @@ def test_pairing_correlations_exact(W, L, ne, U, phi):
     np.testing.assert_allclose(m, P[:len(PAIR_SYS), len(PAIR_SYS):], atol=1e-6)
     with pytest.raises(ValueError):
         om.pairing_correlations(d, [(2, 3)], PAIR_ENV)
+
+
+@pytest.mark.parametrize("W,L,ne,U,phi", [(2, 4, 6, 8.0, 0.25), (2, 4, 8, 4.0, 0.0)])
+def test_pairing_correlations_same_side_exact(W, L, ne, U, phi):
+    """Same-side singlet-pair correlations of the oracle (the pair creator of
+    the first bond multiplied by the second bond's two elec_down operators,
+    ranks 1/2 then 0, measured with measure_sys_block) against the exact
+    ground state, on a superblock with four system block sites."""
+    from oracle import measure as om
+    lat = Lattice(W, L, U=U, phi=phi)
+    _, P = ed.hubbard_pair_correlations(lat, ne // 2, ne // 2, [(1, 2), (3, 4)])
+    _, d = _dmrg(lat, ne, sweeps=1)
+    d.left_to_right(1, 5)
+    assert d.wave.sys_len == 5
+    m = om.pairing_correlations_sys(d, [(1, 2)], [(3, 4)])
+    np.testing.assert_allclose(m, P[:1, 1:], atol=1e-6)
+    with pytest.raises(ValueError):
+        om.pairing_correlations_sys(d, [(1, 3)], [(2, 4)])
