@@ -118,6 +118,18 @@ def tj_ground_energies(lat, n_up, n_dn, k=1):
     """Lowest k levels of H = -t sum P(c+_is c_js + h.c.)P + J sum_<ij> (S_i.S_j - n_i n_j / 4)
     in the (n_up, n_dn) sector, no double occupancy, same bonds and Peierls
     factors as the Hubbard case."""
+    H, _ = _tj_hamiltonian(lat, n_up, n_dn)
+    m = H.shape[0]
+    if m <= 400:
+        return np.linalg.eigvalsh(H.toarray())[:k]
+    w = spla.eigsh(H, k=k, which="SA", return_eigenvectors=False, tol=1e-12)
+    return np.sort(w)
+
+
+def _tj_hamiltonian(lat, n_up, n_dn):
+    """The t-J Hamiltonian of tj_ground_energies on the (n_up, n_dn) sector
+    and its configurations (bit s: up electron on site s + 1; bit N + s:
+    down electron)."""
     N = lat.N
     confs = []
     for ups in combinations(range(N), n_up):
@@ -154,11 +166,7 @@ def tj_ground_energies(lat, n_up, n_dn, k=1):
             add(c, [(a, 1), (a + N, 0), (b + N, 1), (b, 0)], 0.5 * lat.J)
             add(c, [(a + N, 1), (a, 0), (b, 1), (b + N, 0)], 0.5 * lat.J)
     m = len(confs)
-    H = sp.csr_matrix((vals, (rows, cols)), shape=(m, m), dtype=np.complex128)
-    if m <= 400:
-        return np.linalg.eigvalsh(H.toarray())[:k]
-    w = spla.eigsh(H, k=k, which="SA", return_eigenvectors=False, tol=1e-12)
-    return np.sort(w)
+    return sp.csr_matrix((vals, (rows, cols)), shape=(m, m), dtype=np.complex128), confs
 
 
 def tj_singlet_ground_energy(lat, n_elec, k=10, tol=1e-7):
@@ -343,3 +351,52 @@ def hubbard_pair_correlations(lat, n_up, n_dn, bonds):
         vecs.append(np.asarray(t1 - t2).ravel() / np.sqrt(2.0))
     P = np.array([[np.vdot(vx, vy) for vy in vecs] for vx in vecs])
     return e0, P
+
+
+def tj_singlet_correlations(lat, n_elec, bonds, k=10):
+    """The t-J singlet ground state (tj_singlet_ground_energy picked out of the
+    lowest levels of the S_z = 0 sector): energy, G_ij = sum_s <c+_is c_js>
+    with projected operators, and the singlet-pair correlations
+    <D+_x D_y> of the given bonds, D+_ij = (c+_i,up c+_j,dn - c+_i,dn c+_j,up)
+    / sqrt(2).  On a state without double occupancy the plain annihilators
+    equal the projected ones; a creation that makes a double occupancy
+    gives zero."""
+    N = lat.N
+    e_s = tj_singlet_ground_energy(lat, n_elec)
+    H, confs = _tj_hamiltonian(lat, n_elec // 2, n_elec // 2)
+    w, v = np.linalg.eigh(H.toarray()) if H.shape[0] <= 3000 else spla.eigsh(H, k=k, which="SA", tol=1e-13)
+    order = np.argsort(w)
+    w, v = w[order], v[:, order]
+    i0 = int(np.argmin(np.abs(w - e_s)))
+    if abs(w[i0] - e_s) > 1e-8 or (i0 + 1 < len(w) and abs(w[i0 + 1] - w[i0]) < 1e-8) or \
+            (i0 > 0 and abs(w[i0] - w[i0 - 1]) < 1e-8):
+        raise RuntimeError("singlet ground state not isolated in the S_z = 0 sector")
+    psi = v[:, i0]
+    amp = dict(zip(confs, psi))
+
+    def apply(ops):
+        out = {}
+        for c, a in amp.items():
+            sgn, c2 = _tj_apply(c, ops, N)
+            if c2 is None or (c2 & ((1 << N) - 1)) & (c2 >> N):
+                continue
+            out[c2] = out.get(c2, 0.0) + sgn * a
+        return out
+
+    G = np.zeros((N, N), dtype=np.complex128)
+    for i in range(N):
+        for j in range(N):
+            for sh in (0, N):
+                phi = apply([(i + sh, 1), (j + sh, 0)])
+                G[i, j] += sum(np.conj(amp.get(c, 0.0)) * a for c, a in phi.items())
+    vecs = []
+    for (i, j) in bonds:
+        a, b = i - 1, j - 1
+        t1 = apply([(b + N, 0), (a, 0)])
+        t2 = apply([(b, 0), (a + N, 0)])
+        vec = dict(t1)
+        for c, x in t2.items():
+            vec[c] = vec.get(c, 0.0) - x
+        vecs.append({c: x / np.sqrt(2.0) for c, x in vec.items()})
+    P = np.array([[sum(np.conj(vx.get(c, 0.0)) * y for c, y in vy.items()) for vy in vecs] for vx in vecs])
+    return float(w[i0]), G, P

@@ -185,3 +185,23 @@ def test_pairing_correlations_same_side_exact(W, L, ne, U, phi):
     np.testing.assert_allclose(m, P[:1, 1:], atol=1e-6)
     with pytest.raises(ValueError):
         om.pairing_correlations_sys(d, [(1, 3)], [(2, 4)])
+
+
+def test_tj_electron_and_pairing_correlations_exact():
+    """t-J ladder (projected site operators): the oracle's electron
+    correlations for all pairs and its cross-cut and same-side singlet-pair
+    correlations against the exact singlet ground state."""
+    from oracle import measure as om
+    lat = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
+    bonds = PAIR_SYS + PAIR_ENV + [(3, 4)]
+    e0, G, P = ed.tj_singlet_correlations(lat, 6, bonds)
+    np.testing.assert_allclose(G, G.conj().T, atol=1e-12)
+    assert np.trace(G).real == pytest.approx(6.0, abs=1e-10)
+    e, d = _dmrg(lat, 6, m=300, sweeps=1)
+    assert e == pytest.approx(e0, abs=1e-9)
+    d.left_to_right(1, lat.N // 2 - 1)
+    np.testing.assert_allclose(om.electron_correlations_all(d), G, atol=1e-6)
+    np.testing.assert_allclose(om.pairing_correlations(d, PAIR_SYS, PAIR_ENV), P[:1, 1:7], atol=1e-6)
+    _, d = _dmrg(lat, 6, m=300, sweeps=1)
+    d.left_to_right(1, 5)
+    np.testing.assert_allclose(om.pairing_correlations_sys(d, [(1, 2)], [(3, 4)]), P[:1, 7:], atol=1e-6)
