@@ -219,6 +219,28 @@ def _pair_pair_operator(dev, up, dn, bond_x, bond_y, length, bases, truns):
     return X
 
 
+def structure_factor(corr, W, L, nx_cut=0):
+    """Get_structure_factor_cut (code/measure.f90:2159-2236) on the host:
+    S(kx, ky) = Re(f^T C f*) / N' over the sites outside nx_cut columns at
+    either end, f_x = exp(i (kx X_x + ky Y_x)), C the real part of the
+    correlation matrix (the diagonal enters with phase 1), kx = 2 pi i /
+    (L - 2 nx_cut), i = 0..L - 2 nx_cut, ky = 2 pi j / W, j = 0..W.  Returns
+    (kx / pi, ky / pi, S[i, j])."""
+    C = np.real(np.asarray(corr, dtype=np.complex128))
+    N = W * L
+    if C.shape != (N, N) or not 0 <= 2 * nx_cut < L:
+        raise ValueError("correlation matrix must be N x N and 2 nx_cut < L")
+    kxn = L - 2 * nx_cut
+    kx = 2.0 * np.pi * np.arange(kxn + 1) / kxn
+    ky = 2.0 * np.pi * np.arange(W + 1) / W
+    sites = np.arange(nx_cut * W, N - nx_cut * W)
+    X, Y = sites // W, sites % W
+    Cw = C[np.ix_(sites, sites)]
+    f = np.exp(1j * (kx[:, None, None] * X[None, None, :] + ky[None, :, None] * Y[None, None, :]))
+    S = np.einsum("ijx,xy,ijy->ij", f, Cw, np.conj(f)).real / len(sites)
+    return kx / np.pi, ky / np.pi, S
+
+
 class Measurement:
     """Measurements on the current superblock of a ``GPUDMRG`` (its last
     Lanczos state and the bases and truncations it keeps on the device)."""

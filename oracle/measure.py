@@ -564,3 +564,33 @@ def pairing_correlations_sys(d, bonds_x, bonds_y):
     sys_bs = d.sys_bases[d.wave.sys_len]
     return np.array([[measure_sys_block(pair_pair_operator(d, x, y), sys_bs, d.wave) for y in bonds_y]
                      for x in bonds_x])
+
+
+def structure_factor_cut(corr, W, L, nx_cut):
+    """Get_structure_factor_cut (code/measure.f90:2159-2236): for the sites
+    outside nx_cut columns at either end, S(kx, ky) = (sum_x C_xx +
+    sum_{x != y} exp(i (kx (X_x - X_y) + ky (Y_x - Y_y))) C_xy) / N' with
+    C the real part of the correlation matrix, kx = 2 pi i / (L - 2 nx_cut),
+    i = 0..L - 2 nx_cut, ky = 2 pi j / W, j = 0..W; site s sits at
+    X = (s - 1) // W + 1, Y = (s - 1) % W + 1.  Returns the real part,
+    indexed [i, j]."""
+    C = np.real(np.asarray(corr))
+    N = W * L
+    kxn, kyn = L - 2 * nx_cut, W
+    lo, hi = nx_cut * W + 1, N - nx_cut * W
+    out = np.zeros((kxn + 1, kyn + 1))
+    for i in range(kxn + 1):
+        kx = 2.0 * np.pi * i / kxn
+        for j in range(kyn + 1):
+            ky = 2.0 * np.pi * j / kyn
+            s = 0.0 + 0.0j
+            for x in range(lo, hi + 1):
+                s += C[x - 1, x - 1]
+            for x in range(lo, hi + 1):
+                for y in range(lo, hi + 1):
+                    if x != y:
+                        dx = (x - 1) // W - (y - 1) // W
+                        dy = (x - 1) % W - (y - 1) % W
+                        s += np.exp(1j * (kx * dx + ky * dy)) * C[x - 1, y - 1]
+            out[i, j] = (s / (N - 2 * nx_cut * W)).real
+    return out

@@ -205,3 +205,34 @@ def test_tj_electron_and_pairing_correlations_exact():
     _, d = _dmrg(lat, 6, m=300, sweeps=1)
     d.left_to_right(1, 5)
     np.testing.assert_allclose(om.pairing_correlations_sys(d, [(1, 2)], [(3, 4)]), P[:1, 7:], atol=1e-6)
+
+
+@pytest.mark.parametrize("W,L,cut", [(2, 4, 0), (2, 6, 1), (4, 5, 1), (3, 4, 0)])
+def test_structure_factor_matches_oracle(W, L, cut):
+    """The host structure factor (vectorised) equals the oracle's restatement
+    of Get_structure_factor_cut on a random complex matrix (real part used);
+    a diagonal C = c 1 gives S = c at every k."""
+    from oracle import measure as om
+    from hofstadter_hubbard_tsc_gb300.measure import structure_factor
+    rng = np.random.default_rng(W * 100 + L * 10 + cut)
+    N = W * L
+    C = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+    kx, ky, S = structure_factor(C, W, L, cut)
+    np.testing.assert_allclose(S, om.structure_factor_cut(C, W, L, cut), atol=1e-12)
+    assert kx[0] == 0.0 and kx[-1] == pytest.approx(2.0) and ky[-1] == pytest.approx(2.0)
+    _, _, S1 = structure_factor(0.7 * np.eye(N), W, L, cut)
+    np.testing.assert_allclose(S1, 0.7, atol=1e-12)
+    with pytest.raises(ValueError):
+        structure_factor(C[:-1, :-1], W, L, cut)
+
+
+def test_spin_structure_factor_sum_rule():
+    """For the exact singlet, sum_j <S_i . S_j> = 0 for every i (total spin
+    zero), so the spin structure factor at k = 0 over the whole ladder
+    vanishes."""
+    from hofstadter_hubbard_tsc_gb300.measure import structure_factor
+    lat = Lattice(2, 4, U=8.0, phi=0.25)
+    _, ss, _ = ed.hubbard_spin_correlations(lat, 3, 3)
+    _, _, S = structure_factor(ss, 2, 4, 0)
+    assert abs(S[0, 0]) < 1e-10
+    assert S.max() > 0.1
