@@ -101,10 +101,11 @@ def _run(device, apply, sweeps=3):
 def test_learned_guess_ab(device):
     """Plain transformed guess (A) against the learned correction (B), the same
     trajectory until the network is first applied.  Reports the iterations of
-    the last sweep of both; the converged energy judges the correction (equal
-    to 1e-8 relative: the runs part ways once corrections start), and the
-    corrected run may not need more than 2 % more Lanczos iterations.  The gain is bounded by about 1 % on this ladder: restarting
-    from the exact converged sector weights saves no more."""
+    the last sweep of both; the converged energies must agree (to 1e-8
+    relative: the runs part ways once corrections start), and the corrected
+    run may not need more than 2 % more Lanczos iterations.  The gain is
+    bounded by about 1 % on this ladder: restarting from the exact converged
+    sector weights saves no more."""
     ea, its_a, ha, _ = _run(device, apply=False)
     eb, its_b, hb, _ = _run(device, apply=True)
     used = sum(1 for r in hb.log if r[2])
