@@ -11,6 +11,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libhh_dmrg.so")
 
 HH_OK = 0
+# status codes (include/hh_dmrg.h)
+HH_ERR_INVALID, HH_ERR_CUDA, HH_ERR_NOMEM, HH_ERR_QN = -1, -2, -3, -4
+HH_ERR_TIMEOUT, HH_ERR_NUMERIC, HH_ERR_UNSUPPORTED = -5, -6, -7
 HH_PREC_FP64 = 0
 HH_PREC_BF16X6 = 1  # three BF16 parts, six products: ~2^-24 per product
 HH_PREC_BF16X3 = 2  # two BF16 parts, three products: ~2^-16 per product

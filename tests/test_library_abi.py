@@ -33,3 +33,22 @@ def test_binding_covers_header(lib_path):
     lib = _lib.load(lib_path)
     assert lib.hh_version() >= 100
     assert lib.hh_status_string(-4) == b"quantum number mismatch"
+
+
+def test_null_handles_are_rejected(lib_path):
+    """Every entry point that takes handles or buffers rejects null ones with
+    HH_ERR_INVALID before any device work (hh_host_free(NULL) is a no-op, as
+    free(NULL) is)."""
+    lib = _lib.load(lib_path)
+    skip = {"hh_init", "hh_version", "hh_status_string", "hh_last_error", "hh_host_free"}
+    checked = 0
+    for name, (_, args) in sorted(_lib.SIGNATURES.items()):
+        if name in skip:
+            continue
+        codes = [getattr(a, "_type_", "P") for a in args]
+        vals = [0 if isinstance(c, str) and c in "bBhHiIlLqQ" else 0.0 if c in ("f", "d") else None
+                for c in codes]
+        assert getattr(lib, name)(*vals) == _lib.HH_ERR_INVALID, name
+        checked += 1
+    assert checked > 40
+    assert lib.hh_host_free(None) == 0
