@@ -54,6 +54,29 @@ def block_sectors(n_sites, n_fill, m, rng, sigma_n=2.5, s_scale=1.5, max_dim=Non
     return out
 
 
+def lognormal_sectors(n_sites, n_center, n_sectors, median, max_dim, rng, min_dim=8, tj=False):
+    """(N, 2S, dim) of a synthetic block: the n_sectors (N, 2S) nearest to
+    (n_center, 0) (2S = N mod 2, 2S <= N and <= 2 n_sites - N; t-J: N <=
+    n_sites), a region that the rank-1/2 operators (N +- 1, 2S +- 1) connect;
+    dims clip(round(exp(ln median + sigma z)), min_dim, max_dim), z ~ N(0, 1)
+    seeded, with sigma = ln(max_dim / median) / max z so that the largest
+    sector has max_dim states."""
+    cands = []
+    nmax = n_sites if tj else 2 * n_sites
+    for N in range(0, nmax + 1):
+        smax = N if tj else min(N, 2 * n_sites - N)
+        for S2 in range(N % 2, smax + 1, 2):
+            cands.append(((N - n_center) ** 2 / 4.0 + S2 ** 2 / 9.0, N, S2))
+    cands.sort()
+    chosen = [(N, S2) for _, N, S2 in cands[:n_sectors]]
+    z = rng.standard_normal(len(chosen))
+    sigma = np.log(max_dim / median) / z.max()
+    dims = np.clip(np.round(np.exp(np.log(median) + sigma * z)), min_dim, max_dim).astype(int)
+    out = [(N, S2, int(d)) for (N, S2), d in zip(chosen, dims)]
+    out.sort(key=lambda q: (-q[1], -q[0]))
+    return out
+
+
 def _herm(rng, d):
     a = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
     return (a + a.conj().T) / 2.0
@@ -108,9 +131,12 @@ class Workload:
     """A synthetic mid-chain superblock: models, bases, super basis, geometry."""
 
     def __init__(self, W=4, L=32, n_elec=112, m=2000, U=8.0, phi=0.25, seed=20261203, sys_len=None,
-                 model="hubbard", J=0.0):
+                 model="hubbard", J=0.0, lognormal=None):
+        """lognormal = (sectors per block, median, max dim): block sectors
+        from lognormal_sectors instead of the finite-size profile (m is then
+        unused)."""
         self.W, self.L, self.n_elec, self.m, self.U, self.phi, self.seed = W, L, n_elec, m, U, phi, seed
-        self.model, self.J = model, J
+        self.model, self.J, self.lognormal = model, J, lognormal
         tj = model == "tj"
         if tj:
             self.U = U = 0.0
@@ -121,8 +147,13 @@ class Workload:
         le = N - ls - 2
         fill = n_elec / N
         names = ("elec_up", "elec_down", "spin_sd", "num_sn") if tj else ("elec_up", "elec_down")
-        self.sys_sectors = block_sectors(ls, fill * ls, m, rng, tj=tj)
-        self.env_sectors = block_sectors(le, fill * le, m, rng, tj=tj)
+        if lognormal is None:
+            self.sys_sectors = block_sectors(ls, fill * ls, m, rng, tj=tj)
+            self.env_sectors = block_sectors(le, fill * le, m, rng, tj=tj)
+        else:
+            ns, med, mx = lognormal
+            self.sys_sectors = lognormal_sectors(ls, fill * ls, ns, med, mx, rng, min_dim=min(8, mx), tj=tj)
+            self.env_sectors = lognormal_sectors(le, fill * le, ns, med, mx, rng, min_dim=min(8, mx), tj=tj)
         self.sys = synthetic_model(ls, self.sys_sectors, max(1, self.lat.nleg11[ls]), rng, names)
         self.env = synthetic_model(le, self.env_sectors, max(1, self.lat.nleg11[le]), rng, names)
         st = SiteOperators(model)
@@ -130,7 +161,10 @@ class Workload:
         self.env_bs = get_basis(self.env.ham, st.sz)
         self.sup = get_super_basis(self.sys_bs, self.env_bs, n_elec, 0)
         self.geo = self.lat.geometry(ls, le)
-        if tj:
+        if lognormal is not None:
+            ns, med, mx = lognormal
+            self.name = (f"synthetic-{W}x{L}-{model}-midchain-{2 * ns}sectors-lognormal-median{med:g}-max{mx}")
+        elif tj:
             self.name = f"tj-cylinder-{W}x{L}-phi{phi:.4g}-J{J:g}-Ne{n_elec}-m{m}-midchain"
         else:
             self.name = f"hubbard-cylinder-{W}x{L}-phi{phi:.4g}-U{U:g}-Ne{n_elec}-m{m}-midchain"
@@ -138,12 +172,31 @@ class Workload:
     def describe(self):
         return {
             "workload": self.name,
+            "block_dims": [sum(d for *_, d in self.sys_sectors), sum(d for *_, d in self.env_sectors)],
             "lattice": f"{self.W}x{self.L} {'ladder' if self.W == 2 else 'cylinder (periodic y, open x)'}, "
                        f"Landau gauge, {self.model}",
-            "phi": self.phi, "U": self.U, "J": self.J, "t": 1.0, "n_elec": self.n_elec, "kept_multiplets": self.m,
+            "phi": self.phi, "U": self.U, "J": self.J, "t": 1.0, "n_elec": self.n_elec,
+            "kept_multiplets": self.m if self.lognormal is None else None,
             "sys_len": self.sys.len, "env_len": self.env.len,
             "block_sectors": [len(self.sys_sectors), len(self.env_sectors)],
             "enlarged_dims": [self.sys_bs.dim, self.env_bs.dim],
             "wave_sectors": self.sup.num, "wave_dim": self.sup.dim,
             "operators": "synthetic N(0,1) complex, Hermitian block Hamiltonians, seed %d" % self.seed,
         }
+
+
+def uneven_batch(sup_dim_sectors, nbatch, rng):
+    """nbatch uneven wavefunctions over a superblock layout given as the list
+    of its sector sizes: N(0,1) complex entries, each sector scaled by a
+    lognormal weight drawn per vector and each vector by 10^(b - nbatch/2),
+    flattened in layout order; shape (nbatch, total)."""
+    total = sum(sup_dim_sectors)
+    out = np.empty((nbatch, total), dtype=np.complex128)
+    for b in range(nbatch):
+        v = rng.normal(scale=np.sqrt(0.5), size=total) + 1j * rng.normal(scale=np.sqrt(0.5), size=total)
+        o = 0
+        for n in sup_dim_sectors:
+            v[o:o + n] *= np.exp(rng.normal())
+            o += n
+        out[b] = v * 10.0 ** (b - nbatch / 2)
+    return out
