@@ -145,9 +145,11 @@ class LearnedGuess:
     method with the same bookkeeping)."""
 
     def __init__(self, dev, n_sites, n_elec, seed=20261203, apply=True, min_samples=64, epochs=400, lr=3e-3,
-                 rq_check=False):
+                 rq_check=False, mlp=None):
+        """mlp: the network (SectorMLP on dev when None; anything with its
+        forward / train / free methods otherwise)."""
         self.dev, self.n_sites, self.n_elec = dev, n_sites, n_elec
-        self.mlp = SectorMLP(dev, NFEAT, seed)
+        self.mlp = SectorMLP(dev, NFEAT, seed) if mlp is None else mlp
         self.apply = apply
         self.min_samples, self.epochs, self.lr = min_samples, epochs, lr
         self.X, self.T, self.W = [], [], []
