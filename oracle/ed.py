@@ -400,3 +400,33 @@ def tj_singlet_correlations(lat, n_elec, bonds, k=10):
         vecs.append({c: x / np.sqrt(2.0) for c, x in vec.items()})
     P = np.array([[sum(np.conj(vx.get(c, 0.0)) * y for c, y in vy.items()) for vy in vecs] for vx in vecs])
     return float(w[i0]), G, P
+
+
+def tj_singlet_spin_correlations(lat, n_elec, k=10):
+    """<S_i . S_j> (N x N) of the t-J singlet ground state of
+    tj_singlet_correlations: S^z_i S^z_j + (S^+_i S^-_j + S^-_i S^+_j) / 2,
+    with S^+_i = c+_i,up c_i,dn; the diagonal is 3/4 <n_i>."""
+    N = lat.N
+    e_s = tj_singlet_ground_energy(lat, n_elec)
+    H, confs = _tj_hamiltonian(lat, n_elec // 2, n_elec // 2)
+    w, v = np.linalg.eigh(H.toarray()) if H.shape[0] <= 3000 else spla.eigsh(H, k=k, which="SA", tol=1e-13)
+    i0 = int(np.argmin(np.abs(w - e_s)))
+    psi = v[:, i0]
+    amp = dict(zip(confs, psi))
+    ss = np.zeros((N, N))
+    for i in range(N):
+        for j in range(N):
+            if i == j:
+                ss[i, i] = sum(abs(a) ** 2 * 0.75 * (((c >> i) & 1) + ((c >> (i + N)) & 1)) for c, a in amp.items())
+                continue
+            val = 0.0
+            for c, a in amp.items():
+                szi = 0.5 * (((c >> i) & 1) - ((c >> (i + N)) & 1))
+                szj = 0.5 * (((c >> j) & 1) - ((c >> (j + N)) & 1))
+                val += abs(a) ** 2 * szi * szj
+                for ops in ([(i, 1), (i + N, 0), (j + N, 1), (j, 0)], [(i + N, 1), (i, 0), (j, 1), (j + N, 0)]):
+                    sgn, c2 = _tj_apply(c, ops, N)
+                    if c2 is not None:
+                        val += 0.5 * (np.conj(amp.get(c2, 0.0)) * sgn * a).real
+            ss[i, j] = val
+    return float(w[i0]), ss

@@ -155,9 +155,9 @@ def test_pairing_correlations_same_side_exact(device, precision):
 
 @pytest.mark.parametrize("precision", [_lib.HH_PREC_FP64, _lib.HH_PREC_BF16X3])
 def test_tj_electron_and_pairing_correlations_exact(device, precision):
-    """t-J ladder (projected site operators) on the GPU: electron correlations
-    for all pairs, cross-cut and same-side singlet-pair correlations against
-    the exact singlet ground state."""
+    """t-J ladder (projected site operators) on the GPU: electron and spin
+    correlations for all pairs, cross-cut and same-side singlet-pair
+    correlations against the exact singlet ground state."""
     lat_o = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
     sys_bonds, env_bonds = [(1, 2)], [(8, 7), (7, 6), (6, 5), (8, 6), (7, 5), (8, 5)]
     _, G, P = ed.tj_singlet_correlations(lat_o, 6, sys_bonds + env_bonds + [(3, 4)])
@@ -171,6 +171,8 @@ def test_tj_electron_and_pairing_correlations_exact(device, precision):
 
     m = state(lat_o.N // 2 - 1)
     np.testing.assert_allclose(m.electron_correlations_all(), G, atol=1e-6)
+    _, ss = ed.tj_singlet_spin_correlations(lat_o, 6)
+    np.testing.assert_allclose(m.spin_correlations_all(), ss, atol=1e-6)
     np.testing.assert_allclose(m.pairing_correlations(sys_bonds, env_bonds), P[:1, 1:7], atol=1e-6)
     m = state(5)
     np.testing.assert_allclose(m.pairing_correlations_sys([(1, 2)], [(3, 4)]), P[:1, 7:], atol=1e-6)

@@ -236,3 +236,15 @@ def test_spin_structure_factor_sum_rule():
     _, _, S = structure_factor(ss, 2, 4, 0)
     assert abs(S[0, 0]) < 1e-10
     assert S.max() > 0.1
+
+
+def test_tj_spin_correlations_all_pairs():
+    """t-J ladder: the oracle's <S_i . S_j> for every pair against the exact
+    singlet ground state (rows sum to zero: total spin 0)."""
+    from oracle import measure as om
+    lat = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
+    _, ss = ed.tj_singlet_spin_correlations(lat, 6)
+    np.testing.assert_allclose(ss.sum(axis=1), 0.0, atol=1e-10)
+    _, d = _dmrg(lat, 6, m=300, sweeps=1)
+    d.left_to_right(1, lat.N // 2 - 1)
+    np.testing.assert_allclose(om.spin_correlations_all(d), ss, atol=1e-6)
