@@ -8,7 +8,8 @@ are known answers of this project's own independent code paths:
   which shares nothing with the SU(2) code) of a Hubbard flux ladder and a
   t-J ladder: singlet ground energies, and for the Hubbard ladder the density,
   spin and electron (sum_s <c+_i c_j>, complex) correlation matrices and
-  singlet-pair correlations <D+_x D_y> of bonds on either side of the middle;
+  singlet-pair correlations <D+_x D_y> of bonds on either side of the middle
+  (for the t-J ladder: spin, electron and pair correlations of its singlet);
 * matvec_tj_2x6.npz and matvec_hubbard_4x4.npz: a seeded input vector and the
   oracle's model_wave of it on small synthetic mid-chain superblocks
   (hofstadter_hubbard_tsc_gb300/synth.py).
@@ -44,12 +45,16 @@ def ed_fixtures():
     _, P = ed.hubbard_pair_correlations(hub, 3, 3, PAIR_BONDS)
     tj = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
     e_t = ed.tj_singlet_ground_energy(tj, 6)
+    _, Gt, Pt = ed.tj_singlet_correlations(tj, 6, [tuple(b) for b in PAIR_BONDS])
+    _, sst = ed.tj_singlet_spin_correlations(tj, 6)
     return {
         "hubbard_2x4_U8_phi0.25_Ne6": {"energy": float(e_h), "density": dens.tolist(), "nn": corr.tolist(),
                                        "ss": ss.tolist(), "green_re": G.real.tolist(), "green_im": G.imag.tolist(),
                                        "pair_bonds": PAIR_BONDS, "pair_re": P.real.tolist(),
                                        "pair_im": P.imag.tolist()},
-        "tj_2x4_J0.4_phi1/6_Ne6": {"energy": float(e_t)},
+        "tj_2x4_J0.4_phi1/6_Ne6": {"energy": float(e_t), "ss": sst.tolist(), "green_re": Gt.real.tolist(),
+                                   "green_im": Gt.imag.tolist(), "pair_bonds": PAIR_BONDS,
+                                   "pair_re": Pt.real.tolist(), "pair_im": Pt.imag.tolist()},
     }
 
 

@@ -46,6 +46,12 @@ def test_ed_reproduces_fixture():
     np.testing.assert_allclose(G, _green(g), atol=1e-12)
     _, P = ed.hubbard_pair_correlations(hub, 3, 3, [tuple(b) for b in g["pair_bonds"]])
     np.testing.assert_allclose(P, _pair(g), atol=1e-12)
+    h = _ed()["tj_2x4_J0.4_phi1/6_Ne6"]
+    tj = Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0)
+    _, Gt, Pt = ed.tj_singlet_correlations(tj, 6, [tuple(b) for b in h["pair_bonds"]])
+    np.testing.assert_allclose(Gt, _green(h), atol=1e-12)
+    np.testing.assert_allclose(Pt, _pair(h), atol=1e-12)
+    np.testing.assert_allclose(ed.tj_singlet_spin_correlations(tj, 6)[1], np.array(h["ss"]), atol=1e-12)
 
 
 def test_oracle_dmrg_reproduces_fixture():
@@ -63,6 +69,12 @@ def test_oracle_dmrg_reproduces_fixture():
     t = DMRG(Lattice(2, 4, model="tj", J=0.4, U=0.0, phi=1.0 / 6.0), 6, kept_min=300, kept_max=300, trun_err=1e-14,
              lanzero=1e-11, seed=3)
     assert t.run(sweeps=1) == pytest.approx(g["tj_2x4_J0.4_phi1/6_Ne6"]["energy"], abs=1e-9)
+    t.left_to_right(1, 3)
+    h = g["tj_2x4_J0.4_phi1/6_Ne6"]
+    bonds = [tuple(b) for b in h["pair_bonds"]]
+    np.testing.assert_allclose(om.spin_correlations_all(t), np.array(h["ss"]), atol=1e-6)
+    np.testing.assert_allclose(om.electron_correlations_all(t), _green(h), atol=1e-6)
+    np.testing.assert_allclose(om.pairing_correlations(t, bonds[:1], bonds[1:]), _pair(h)[:1, 1:], atol=1e-6)
 
 
 @pytest.mark.parametrize("name", sorted(MATVEC_CASES))
