@@ -100,3 +100,30 @@ def test_lognormal_batched_uneven(device):
     win.free()
     wout.free()
     sb.free()
+
+
+def test_full_size_properties(device):
+    """The 4x32 Hubbard cylinder at m = 2000 (wave dimension 1.94 M, the
+    headline workload), where the oracle is too slow: the FP64 matvec is
+    Hermitian and linear, and BF16x3 stays within 2e-5 of FP64."""
+    wl = Workload()
+    sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
+    rng = np.random.default_rng(11)
+    n = wl.sup.dim
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    y = rng.normal(size=n) + 1j * rng.normal(size=n)
+
+    def hv(v, prec=_lib.HH_PREC_FP64):
+        sb.w_in.upload(v)
+        device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, prec))
+        return sb.w_out.download()
+
+    hx, hy = hv(x), hv(y)
+    lhs, rhs = np.vdot(x, hy), np.conj(np.vdot(y, hx))
+    assert abs(lhs - rhs) < 1e-10 * abs(lhs)
+    a, b = 0.6 - 0.3j, -1.2 + 0.5j
+    hz = hv(a * x + b * y)
+    assert np.linalg.norm(hz - (a * hx + b * hy)) < 1e-12 * np.linalg.norm(hz)
+    x3 = hv(x, _lib.HH_PREC_BF16X3)
+    assert np.linalg.norm(x3 - hx) / np.linalg.norm(hx) < 2e-5
+    sb.free()
