@@ -107,6 +107,45 @@ def _fock_hamiltonian(lat, sites, n_elec=None):
     return sp.csr_matrix((vals, (rows, cols)), shape=(dim, dim), dtype=complex)
 
 
+def _fock_hamiltonian_tj(lat, sites, n_elec):
+    """-t sum P (phase c+_i c_j + h.c.) P + J sum (S_i . S_j - n_i n_j / 4)
+    on the bonds inside `sites` (no double occupancy), same mode order as
+    _fock_hamiltonian; a spin flip S+_i = c+_i,up c_i,dn moves one electron
+    between two adjacent modes and carries no sign."""
+    sites = sorted(sites)
+    pos = {s: k for k, s in enumerate(sites)}
+    bonds = [(i, j) for (i, j) in ed._bonds(lat) if i in pos and j in pos]
+    n = len(sites)
+    rows, cols, vals = [], [], []
+
+    def occ(c, k):
+        return (c >> (2 * k)) & 1, (c >> (2 * k + 1)) & 1
+
+    for c in range(4 ** n):
+        if bin(c).count("1") != n_elec or any(occ(c, k) == (1, 1) for k in range(n)):
+            continue
+        for (i, j) in bonds:
+            a, b = pos[i], pos[j]
+            amp = -lat.t * lat.phase(i, j)
+            for s in (0, 1):
+                for p_, q_, am in ((a, b, amp), (b, a, np.conj(amp))):
+                    ma, mb = 2 * p_ + s, 2 * q_ + s
+                    if not (c >> mb) & 1 or (c >> ma) & 1 or (c >> (2 * p_ + 1 - s)) & 1:
+                        continue
+                    n1 = bin(c & ((1 << mb) - 1)).count("1")
+                    c1 = c ^ (1 << mb)
+                    n2 = bin(c1 & ((1 << ma) - 1)).count("1")
+                    rows.append(c1 | (1 << ma)); cols.append(c); vals.append(am * (-1) ** (n1 + n2))
+            (ua, da), (ub, db) = occ(c, a), occ(c, b)
+            diag = lat.J * (0.25 * (ua - da) * (ub - db) - 0.25 * (ua + da) * (ub + db))
+            if diag:
+                rows.append(c); cols.append(c); vals.append(diag)
+            if (ua, da, ub, db) in ((0, 1, 1, 0), (1, 0, 0, 1)):
+                c2 = c ^ (3 << (2 * a)) ^ (3 << (2 * b))
+                rows.append(c2); cols.append(c); vals.append(0.5 * lat.J)
+    return sp.csr_matrix((vals, (rows, cols)), shape=(4 ** n, 4 ** n), dtype=complex)
+
+
 def _expand_wave(w, S, E, N):
     v = np.zeros(4 ** N, dtype=complex)
     for ws in w.subs:
@@ -184,3 +223,23 @@ def test_model_wave_equals_dense_hamiltonian(run, which):
     np.testing.assert_allclose(red, phi.flat(), atol=1e-12 * np.abs(phi.flat()).max())
     if which == -1:
         assert np.linalg.norm(HF @ pf - hf) < 1e-12 * np.linalg.norm(hf)
+
+
+def test_model_wave_tj_equals_dense_hamiltonian():
+    """The t-J branch of model_wave (projected hopping, S.S and n n bond
+    terms on blocks and sites): on an untruncated superblock of a t-J ladder
+    the oracle's H psi equals the dense projected t-J Hamiltonian applied to
+    the expanded psi."""
+    lat, d = H.record_superblocks(2, 4, 6, 300, U=0.0, phi=1.0 / 6.0, model="tj", J=0.4)
+    d.left_to_right(1, lat.N // 2 - 1)
+    rec = d.record[-1]
+    sys_bs, env_bs, sup = rec[2], rec[3], rec[5]
+    N = lat.N
+    S = _expand(d.sys_bases, d.sys_truns, sys_bs.len, True, False, sys_bs)
+    E = {k: np.conj(v) for k, v in _expand(d.env_bases, d.env_truns, env_bs.len, False, False, env_bs).items()}
+    psi = H.random_wave(sup, 6)
+    phi = H.oracle_hpsi(rec, d.st, psi)
+    HF = _fock_hamiltonian_tj(lat, range(1, N + 1), 6)
+    pf, hf = _expand_wave(psi, S, E, N), _expand_wave(phi, S, E, N)
+    assert np.linalg.norm(pf) == pytest.approx(np.sqrt(sum(np.vdot(w.vec, w.vec).real for w in psi.subs)), rel=1e-12)
+    assert np.linalg.norm(HF @ pf - hf) < 1e-12 * np.linalg.norm(hf)
