@@ -243,3 +243,37 @@ def test_model_wave_tj_equals_dense_hamiltonian():
     pf, hf = _expand_wave(psi, S, E, N), _expand_wave(phi, S, E, N)
     assert np.linalg.norm(pf) == pytest.approx(np.sqrt(sum(np.vdot(w.vec, w.vec).real for w in psi.subs)), rel=1e-12)
     assert np.linalg.norm(HF @ pf - hf) < 1e-12 * np.linalg.norm(hf)
+
+
+def test_wave_transforms_preserve_the_state(run):
+    """wave_trans_LR and wave_trans_RL (code/warm_up.f90:1855-2170) carry the
+    converged psi of one superblock to the guess on the next as the same
+    Fock-space state: left to right (nothing truncated in between) the
+    expansions are equal; right to left (the environment block grows and is
+    truncated) the guess is the old state's coefficients on the new basis,
+    V_new^H V_old psi."""
+    from oracle.blocks import allocate_wave
+    from oracle.dmrg import wave_trans_lr, wave_trans_rl
+
+    def exp(d, rec):
+        S = _expand(d.sys_bases, d.sys_truns, rec[2].len, True, False, rec[2])
+        E = {k: np.conj(v) for k, v in _expand(d.env_bases, d.env_truns, rec[3].len, False, False, rec[3]).items()}
+        return S, E
+
+    lat, d = run
+    N = lat.N
+    old, new = d.record[-2], d.record[-1]
+    guess = allocate_wave(new[5])
+    wave_trans_lr(new[2], d.env_bases[old[3].len], d.sys_truns[old[2].len], d.env_truns[new[3].len], old[6], guess)
+    vo, vn = _expand_wave(old[6], *exp(d, old), N), _expand_wave(guess, *exp(d, new), N)
+    assert np.linalg.norm(vn - vo) < 1e-12
+
+    lat, d = H.record_superblocks(2, 4, 6, 256, U=8.0, phi=0.25)
+    old, new = d.record[-2], d.record[-1]
+    label = new[2].len
+    guess = allocate_wave(new[5])
+    wave_trans_rl(d.sys_bases[label + 1], new[3], d.sys_truns[label], d.env_truns[N - label - 1], old[6], guess)
+    Sn, En = exp(d, new)
+    red = _reduce_wave(_expand_wave(old[6], *exp(d, old), N), guess, Sn, En, N, label).flat()
+    g = guess.flat()
+    assert np.linalg.norm(red / np.linalg.norm(red) - g / np.linalg.norm(g)) < 1e-12
