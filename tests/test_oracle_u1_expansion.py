@@ -277,3 +277,27 @@ def test_wave_transforms_preserve_the_state(run):
     red = _reduce_wave(_expand_wave(old[6], *exp(d, old), N), guess, Sn, En, N, label).flat()
     g = guess.flat()
     assert np.linalg.norm(red / np.linalg.norm(red) - g / np.linalg.norm(g)) < 1e-12
+
+
+def test_density_matrix_spectra_are_schmidt_spectra(run):
+    """Get_density_matrix_sys / _env (code/get_den.f90:4-177): every
+    eigenvalue x of a sector (2S) density matrix, spread as x / (2S+1) over
+    the multiplet's 2S+1 states, gives the spectrum of the Fock-space reduced
+    density matrix of that half of the expanded ground state (the Schmidt
+    spectrum, the same on both halves)."""
+    from oracle.density import get_density_matrix_env, get_density_matrix_sys
+    lat, d = run
+    N = lat.N
+    rec = d.record[-1]
+    psi = rec[6]
+    S = _expand(d.sys_bases, d.sys_truns, rec[2].len, True, False, rec[2])
+    E = {k: np.conj(v) for k, v in _expand(d.env_bases, d.env_truns, rec[3].len, False, False, rec[3]).items()}
+    M = _expand_wave(psi, S, E, N).reshape(4 ** (N - rec[2].len), 4 ** rec[2].len).T
+    schmidt = np.sort(np.linalg.svd(M, compute_uv=False) ** 2)[::-1]
+    for den in (get_density_matrix_sys(psi), get_density_matrix_env(psi)):
+        spread = np.sort(np.concatenate([np.repeat(np.linalg.eigvalsh(s.mat) / (s.num_down + 1), s.num_down + 1)
+                                         for s in den.subs]))[::-1]
+        spread = spread / spread.sum()
+        k = min(len(spread), len(schmidt))
+        np.testing.assert_allclose(spread[:k], schmidt[:k], atol=1e-13)
+        assert abs(spread[k:]).sum() < 1e-13 and schmidt[k:].sum() < 1e-13
