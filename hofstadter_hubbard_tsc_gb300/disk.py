@@ -230,3 +230,22 @@ def basis_from_disk(path) -> TotalBasis:
             subs.append(SubBasisMap(spos, sdim, int(a[10:14]), int(a[28:32]), int(b[10:14]), int(b[28:32])))
         sectors.append(BasisMap(up, down, subs))
     return TotalBasis(length, sectors)
+
+
+def restart_to_disk(path, restart1, sys_len_start, restart2):
+    """restart.dat (code/warm_up.f90:1580-1584, read at code/quantum.f90:43-46):
+    two list-directed records, 'restart1 sys_len_start' and 'restart2'. The
+    left-to-right sweep writes (1, label + 1) and 1 after each step so that a
+    rerun resumes there. Integers are written in gfortran's layout (a leading
+    blank, 12 columns each); the reader takes any whitespace."""
+    with open(path, "w") as f:
+        f.write(f" {int(restart1):11d} {int(sys_len_start):11d}\n {int(restart2):11d}\n")
+
+
+def restart_from_disk(path):
+    """(restart1, sys_len_start, restart2) of a restart.dat written by the
+    reference or by restart_to_disk (list-directed: free format)."""
+    with open(path) as f:
+        lines = [ln for ln in f.read().split("\n") if ln.strip()]
+    first = lines[0].split()
+    return int(first[0]), int(first[1]), int(lines[1].split()[0])

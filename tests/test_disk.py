@@ -96,3 +96,16 @@ def test_basis_fixed_format(tmp_path):
         assert (x.new_num_up, x.new_num_down, x.dim) == (y.new_num_up, y.new_num_down, y.dim)
         assert [(u.spos, u.sdim, u.bl_num_up, u.bl_num_down, u.st_num_up, u.st_num_down) for u in x.subs] == \
                [(u.spos, u.sdim, u.bl_num_up, u.bl_num_down, u.st_num_up, u.st_num_down) for u in y.subs]
+
+
+def test_restart_flags_round_trip(tmp_path):
+    """restart.dat: the reference's own file (restart1 = 0, sys_len_start = 0,
+    restart2 = 0, free-format spacing) and what a left-to-right step writes."""
+    from hofstadter_hubbard_tsc_gb300.disk import restart_from_disk, restart_to_disk
+    ref = tmp_path / "restart_ref.dat"
+    ref.write_text("         0 0  \n          0\n")
+    assert restart_from_disk(ref) == (0, 0, 0)
+    p = tmp_path / "restart.dat"
+    restart_to_disk(p, 1, 17, 1)
+    assert p.read_text() == "           1          17\n           1\n"
+    assert restart_from_disk(p) == (1, 17, 1)
