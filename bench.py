@@ -13,6 +13,13 @@ steps); ``e2e`` is the same through the C-ABI call with host buffers
 (hh_matvec_host: pinned H2D copy of psi, matvec, D2H copy of H psi every
 step).  --impl reference times the CPU restatement of the reference's
 model_wave (numpy, all host cores) on the same workload.
+
+Sweep time, the metric's second half, is measured twice: on the 2x16 ladder
+of the plain method (one whole finite sweep per arm at m = 256 and 512), and
+as a window of mid-chain steps of the 4x32 cylinder at m = 2000 (the headline
+configuration): the state is grown once by the infinite-system warm-up in
+split precision (untimed), then the FP64 arm and the split-precision arm each
+run the same K steps of the left-to-right sweep from one in-memory copy of it.
 Multi-GPU: replicas only (the step does not exchange data): each rank runs the
 workload, value = sum of matvecs over ranks / max time over ranks.
 """
@@ -67,9 +74,14 @@ def parse():
     p.add_argument("--sweep-precision", default="bf16x6", choices=["bf16x6", "bf16x3"],
                    help="split precision of the sweep's mixed arm (at m = 256-512 the matvecs are launch bound: "
                         "BF16x6 costs about the same as BF16x3 and keeps |dE/E| near 1e-10 instead of 1e-9)")
-    p.add_argument("--energy-check", action="store_true",
-                   help="also run Lanczos (100 vectors) in FP64 and in split precision from one start "
-                        "vector and report |dE/E| (outside the timed region)")
+    p.add_argument("--no-energy-check", action="store_true",
+                   help="skip the Lanczos (100 vectors) in FP64 and in split precision from one start vector "
+                        "on the matvec workload (|dE/E|, outside the timed region)")
+    p.add_argument("--no-window", action="store_true",
+                   help="skip the sweep window of the 4x32 cylinder at m = 2000")
+    p.add_argument("--window-m", type=int, default=2000, help="kept multiplets of the sweep window")
+    p.add_argument("--window-steps", type=int, default=4, help="timed mid-chain steps per arm in the sweep window")
+    p.add_argument("--window-L", type=int, default=32, help="cylinder length of the sweep window (N_e = 3.5 L)")
     return p.parse_args()
 
 
@@ -309,20 +321,102 @@ def sweep_bench(dev, args):
     return results
 
 
+def window_bench(dev, args):
+    """Sweep window at the headline configuration: the W = 4, L = 32 cylinder,
+    phi = 1/4 (Landau gauge), t = 1, U = 8, N_e = 112 (1/8 hole doping),
+    singlet, m kept multiplets (2000), Lanczos tol 1e-10.
+
+    The infinite-system warm-up (warm_up_point, code/warm_up.f90:1284-1491)
+    grows both blocks to the middle of the cylinder at m in split precision,
+    untimed, and one left-to-right step moves the system block to the middle.
+    That state is copied in device memory (the models, truncations and bases
+    are shared, immutable handles; the wave is copied).  Each arm -- plain FP64,
+    and split precision with the learned guess corrector -- restarts from the
+    copy and runs the same K steps of left_to_right (code/warm_up.f90:1495-1671),
+    each from the transformed guess of the step before, timed on the host with
+    the device synchronised on both sides.  The corrector has no earlier sweep
+    to learn from here, so it records and stays on the plain guess."""
+    from hofstadter_hubbard_tsc_gb300 import _lib
+    from hofstadter_hubbard_tsc_gb300.device import DWave
+    from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
+    from hofstadter_hubbard_tsc_gb300.sweep import GPUDMRG
+    from hofstadter_hubbard_tsc_gb300.guess import LearnedGuess
+    L, m, K = args.window_L, args.window_m, args.window_steps
+    ne = int(round(3.5 * L))
+    lat = SquareLattice(4, L, U=8.0, phi=0.25)
+    N = lat.N
+    split = PREC[args.precision] if args.precision != "fp64" else PREC["bf16x3"]
+    kw = dict(kept_min=m, kept_max=m, trun_err=1e-12, lanzero=1e-10, seed=11)
+    hook = LearnedGuess(dev, N, ne)
+    d = GPUDMRG(dev, lat, ne, precision=split, guess_hook=hook, **kw)
+    dev.sync()
+    t0 = time.perf_counter()
+    d.warm_up()
+    d.left_to_right(N // 2 - 1, N // 2)
+    dev.sync()
+    grow_s = time.perf_counter() - t0
+    grow_phase = {k: round(v, 3) for k, v in d.phase_s.items()}
+    grow_steps = len(d.energies)
+
+    def copy_wave(wave):
+        wv, sup = wave
+        w2 = DWave(dev, wv.layout, wv.sys_len, wv.env_len)
+        dev.check(dev.lib.hh_wave_copy(w2.h, wv.h))
+        return w2, sup
+
+    snap = (dict(d.sys_models), dict(d.env_models), dict(d.sys_truns), dict(d.env_truns), dict(d.sys_bases),
+            dict(d.env_bases), copy_wave(d.wave), len(d.energies))
+    out = {"config": f"hubbard-cylinder-4x{L}-phi0.25-U8-Ne{ne}-m{m}-midchain-window", "steps": K,
+           "lanzero": 1e-10, "split_precision": args.precision if args.precision != "fp64" else "bf16x3",
+           "start": f"infinite-system warm-up to the middle + 1 left-to-right step in split precision "
+                    f"({grow_steps} steps, {grow_s:.1f} s, untimed), copied in device memory for both arms",
+           "grow_s": round(grow_s, 2), "grow_phase_s": grow_phase}
+    for name, prec in (("fp64", _lib.HH_PREC_FP64), ("split", split)):
+        d.sys_models = {k: v.copy() for k, v in snap[0].items()}
+        d.env_models = {k: v.copy() for k, v in snap[1].items()}
+        d.sys_truns, d.env_truns, d.sys_bases, d.env_bases = (dict(snap[2]), dict(snap[3]), dict(snap[4]),
+                                                              dict(snap[5]))
+        d.wave = copy_wave(snap[6])
+        del d.energies[snap[7]:]
+        d.precision = prec
+        d.guess_hook = hook if name == "split" else None
+        d.phase_s.clear()
+        dev.sync()
+        t0 = time.perf_counter()
+        d.left_to_right(N // 2, N // 2 + K)
+        dev.sync()
+        dt = time.perf_counter() - t0
+        steps = d.energies[-K:]
+        out[name] = {"window_s": dt, "s_per_step": dt / K, "E0": [e[2] for e in steps],
+                     "lanczos_iterations": [int(e[3]) for e in steps],
+                     "phase_s": {k: round(v, 4) for k, v in d.phase_s.items()},
+                     "kept": int(d.last_trunc[0]) if hasattr(d, "last_trunc") else None}
+    out["split"]["learned_guess"] = {"samples": int(len(hook.data()[1])), "applied": bool(hook.enabled),
+                                     "note": "no earlier sweep to train on inside the window"}
+    e64, esp = np.array(out["fp64"]["E0"]), np.array(out["split"]["E0"])
+    out["rel_dE_per_step"] = (np.abs(esp - e64) / np.abs(e64)).tolist()
+    out["rel_dE"] = float(np.max(out["rel_dE_per_step"]))
+    out["sweep_speedup_split_vs_fp64"] = out["fp64"]["window_s"] / out["split"]["window_s"]
+    hook.free()
+    d.sys_models = d.env_models = d.sys_truns = d.env_truns = d.sys_bases = d.env_bases = {}
+    d.wave = None
+    return out
+
+
 def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
     wl = make_workload(args)
     rng = np.random.default_rng(1)
     psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
-    steps = max(1, min(args.steps, 3))
-    for _ in range(min(args.warmup, 1)):
+    steps = max(1, args.steps)
+    for _ in range(args.warmup):
         cpu_matvec_timer(wl, psi, 1)
     dt, _ = cpu_matvec_timer(wl, psi, steps)
     v = 1.0 / dt
     cores = os.cpu_count()
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-            "warmup": min(args.warmup, 1), "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
             "config": dict(wl.describe(), **{"timing": "host wall clock per matvec"}),
             "impl": "reference",
@@ -354,15 +448,29 @@ def main():
     prec = PREC[args.precision]
     t0 = time.perf_counter()
     wl = make_workload(args)
+    workload_s = time.perf_counter() - t0
     dev = Device(local)
+    # host-side cost of one superblock at this size: operator upload, hmerge
+    # and the task list (hh_plan_create), then the split-precision schedule
+    # and operator images, built by the first split-precision matvec
+    dev.sync()
+    t0 = time.perf_counter()
     sb = Superblock(dev, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo, precision=prec)
-    setup_s = time.perf_counter() - t0
+    dev.sync()
+    plan_build_s = time.perf_counter() - t0
     stats = sb.stats()
     rng = np.random.default_rng(1 + rank)
     psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
     psi /= np.linalg.norm(psi)
     w_in, w_out = sb.w_in, sb.w_out
     w_in.upload(psi)
+    image_build_s = None
+    if prec != _lib.HH_PREC_FP64:
+        dev.sync()
+        t0 = time.perf_counter()
+        dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, prec))
+        dev.sync()
+        image_build_s = time.perf_counter() - t0
 
     stream = torch.cuda.ExternalStream(dev.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
@@ -485,7 +593,9 @@ def main():
                                                           if prec != _lib.HH_PREC_FP64 else None),
                                              "ref_gflop_per_matvec": counts[0] / 1e9,
                                              "exec_gflop_per_matvec": counts[1] / 1e9,
-                                             "plan_setup_s": setup_s}),
+                                             "workload_generation_s": round(workload_s, 3)}),
+            "plan_build_s": plan_build_s,
+            "image_build_s": image_build_s,
             "roofline": roofline, "e2e": e2e, "clocks": clk,
             "stage_ms": {"wave_images": s0 / args.steps, "stage1": s1 / args.steps,
                          "stage2_and_copy_terms": s2 / args.steps},
@@ -497,9 +607,25 @@ def main():
         dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, prec))
         hmx = w_out.download()
         line["rel_err_vs_fp64_gpu"] = float(np.linalg.norm(hmx - h64) / np.linalg.norm(h64))
+        # the FP64 GPU path on the same workload (the metric's comparison arm):
+        # CUDA events on the library's stream, L2 flushed before each matvec
+        n64 = 3
+        ev64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n64)]
+        with torch.cuda.stream(stream):
+            for a, b in ev64:
+                flush.zero_()
+                a.record(stream)
+                dev.check(dev.lib.hh_matvec_async(sb.plan, w_in.h, w_out.h, _lib.HH_PREC_FP64))
+                b.record(stream)
+        dev.check(dev.lib.hh_plan_check(sb.plan))
+        t64 = sum(a.elapsed_time(b) for a, b in ev64) / n64
+        line["fp64_gpu"] = {"value": 1e3 / t64, "unit": UNIT, "ms_per_step": t64, "steps": n64,
+                            "split_vs_fp64_matvec": (1e3 / t64) and value / (1e3 / t64)}
     if rank == 0 and not args.no_sweep and args.config == "c2":
         line["sweep"] = sweep_bench(dev, args)
-    if args.energy_check:
+    if rank == 0 and not args.no_window and args.config == "c2":
+        line["sweep_window"] = window_bench(dev, args)
+    if not args.no_energy_check:
         rs = np.random.default_rng(7)
         start = rs.normal(size=wl.sup.dim) + 1j * rs.normal(size=wl.sup.dim)
         res = {}
@@ -519,7 +645,10 @@ def main():
         rel = float(np.linalg.norm(hpsi_gpu - hpsi_cpu) / np.linalg.norm(hpsi_cpu))
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{n} full matvec(s) of the same workload (numpy restatement of "
-                                          f"model_wave, OpenBLAS on all host cores)"}
+                                          f"model_wave, OpenBLAS on all host cores)",
+                                "achieved_gflops": counts[0] / 1e9 / dt,
+                                "gflops_note": "reference FLOPs of the matvec (8MNK over its ZGEMM calls + 8 per "
+                                               "copied element) / wall time"}
         line["parity_rel_err_vs_oracle"] = rel
     if rank == 0:
         print(json.dumps(line), flush=True)

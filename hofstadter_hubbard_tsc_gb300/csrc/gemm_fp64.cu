@@ -385,6 +385,16 @@ cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, do
   return cudaGetLastError();
 }
 
+// Loads the two kernels above into the current context now (CUDA loads
+// modules and functions lazily, at first launch, by default), so that a later
+// launch reserves no device memory for their code.
+cudaError_t preload_segment_gemm_fp64() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, seg_gemm_fp64_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, seg_reduce_kernel);
+  return e;
+}
+
 cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_out, cudaStream_t s) {
   // d_out must hold >= 1 + nblocks doubles: [0] result, [1..] partials
   int g = grid_for(n, RB);

@@ -283,6 +283,7 @@ int hh_init(int device, hh_ctx_t** out) {
   }
   uint64_t keep = UINT64_MAX;  // freed memory stays in the pool for the next step
   cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  noalloc_setup(c);
   *out = c;
   return HH_OK;
 }

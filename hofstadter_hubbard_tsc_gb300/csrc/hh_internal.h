@@ -47,6 +47,11 @@ struct hh_ctx {
   // density-matrix eigensolver state (streams, solver handles, workspace),
   // created on first use (eig.cu)
   void* eig = nullptr;
+  // device address of the static scratch array of hh_matvec_noalloc, looked
+  // up by hh_init in this context (noalloc.cu); null with a reason if that
+  // lookup failed
+  void* noalloc_scratch = nullptr;
+  std::string noalloc_status;
 };
 
 struct hh_sub_qn {
@@ -246,9 +251,13 @@ int fail(hh_ctx* ctx, int code, const std::string& msg);
 cudaError_t dev_alloc(hh_ctx* ctx, void** p, size_t bytes);
 void dev_free(hh_ctx* ctx, void* p);
 int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what);
+// looks up the static scratch of hh_matvec_noalloc for ctx->device (noalloc.cu)
+void noalloc_setup(hh_ctx* ctx);
 // grouped segment GEMM (FP64); bases[4] = {abs(unused), in, scr, out}
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
                                      double2* base_out, cudaStream_t s);
+// loads the segment GEMM kernels into the current context (gemm_fp64.cu)
+cudaError_t preload_segment_gemm_fp64();
 // wave vector kernels
 cudaError_t wave_dot(const double2* a, const double2* b, long long n, double* d_out, cudaStream_t s);
 // device-resident scalars (Lanczos): *result = Re<a|b> (part: >= 1024 partials),

@@ -12,15 +12,19 @@
 // Limits and sharing:
 //   * the array holds HH_NOALLOC_SCRATCH_BYTES (64 MiB); a plan whose stage-1
 //     products need more is rejected with HH_ERR_INVALID and a message;
-//   * every GPU that loads the library holds the array until the process exits;
+//   * the array belongs to this file's module, which CUDA loads (lazily, by
+//     default) when its address is first looked up.  hh_init does that lookup
+//     for its device, with that device current, so the module and its 64 MiB
+//     are loaded when the context is created, never inside a matvec; every GPU
+//     that loads it holds the array until the process exits;
+//   * the address belongs to the CUDA context that was current in hh_init (the
+//     device's primary context for runtime-API callers), and it is kept in the
+//     hh_ctx: calls must run with that same context current;
 //   * all calls on a device share the one array and it keeps the contents of
 //     the last call: calls that overlap on the GPU (several streams or
 //     contexts at once) race on it; stage 1 overwrites every scratch element it
-//     later reads, so nothing needs clearing between calls;
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current) and caches it.
-#include <mutex>
-
+//     later reads, so nothing needs clearing between calls, and the vectors of
+//     a batched wave run one after another in stream order on the same array.
 #include "hh_internal.h"
 
 #define HH_NOALLOC_SCRATCH_BYTES (64ull << 20)
@@ -29,46 +33,57 @@
 // address returned by cudaGetSymbolAddress to kernels, never the name itself.
 static __device__ __align__(256) double2 g_noalloc_scratch[HH_NOALLOC_SCRATCH_BYTES / sizeof(double2)];
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double2* g_scratch_ptr[kMaxDevices] = {nullptr};
+namespace hh {
 
-int scratch_address(hh_ctx* ctx, double2** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return hh::cuda_check(ctx, e, "cudaGetDevice");
-  if (dev != ctx->device)
-    return hh::fail(ctx, HH_ERR_INVALID, "hh_matvec_noalloc: the context's device is not the current device");
-  if (dev < 0 || dev >= kMaxDevices) return hh::fail(ctx, HH_ERR_INVALID, "device index out of range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return hh::cuda_check(ctx, e, "cudaGetSymbolAddress(static scratch)");
-    g_scratch_ptr[dev] = static_cast<double2*>(p);
+// Called by hh_init with ctx->device current.  It also loads the two FP64
+// kernels the entry point launches, so that not even its first call makes
+// CUDA load code.  A failed lookup does not fail hh_init: the context works
+// without the allocation-free entry point, which then reports the failure.
+void noalloc_setup(hh_ctx* ctx) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e == cudaSuccess) e = preload_segment_gemm_fp64();
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // the failure is recorded here, not left to the next call
+    ctx->noalloc_status = std::string("static scratch set-up failed: ") + cudaGetErrorString(e);
+    ctx->noalloc_scratch = nullptr;
+    return;
   }
-  *out = g_scratch_ptr[dev];
-  return HH_OK;
+  ctx->noalloc_scratch = p;
+  ctx->noalloc_status.clear();
 }
-}  // namespace
+
+}  // namespace hh
 
 extern "C" int hh_matvec_noalloc(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out) {
   if (!p || !in || !out) return HH_ERR_INVALID;
   hh_ctx* ctx = p->ctx;
-  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out)
-    return hh::fail(ctx, HH_ERR_INVALID, "hh_matvec_noalloc: wave layout does not match the plan (or in == out)");
+  if (in->nelem != p->nelem || out->nelem != p->nelem || in == out || in->nbatch != out->nbatch)
+    return hh::fail(ctx, HH_ERR_INVALID,
+                    "hh_matvec_noalloc: wave layout does not match the plan (or in == out, or the two waves "
+                    "hold different numbers of vectors)");
   const unsigned long long need = (unsigned long long)p->scratch_elems * sizeof(double2);
   if (need > HH_NOALLOC_SCRATCH_BYTES)
     return hh::fail(ctx, HH_ERR_INVALID,
                     "hh_matvec_noalloc: the plan needs " + std::to_string(need) +
                         " bytes of stage-1 scratch, the static buffer holds " +
                         std::to_string(HH_NOALLOC_SCRATCH_BYTES) + " bytes; use hh_matvec");
-  double2* scr = nullptr;
-  int st = scratch_address(ctx, &scr);
-  if (st != HH_OK) return st;
-  cudaError_t e = cudaMemsetAsync(out->d, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
-  if (e == cudaSuccess) e = hh::launch_segment_gemm_fp64(p->stage1, in->d, scr, out->d, ctx->stream);
-  if (e == cudaSuccess) e = hh::launch_segment_gemm_fp64(p->stage2, in->d, scr, out->d, ctx->stream);
+  if (!ctx->noalloc_scratch)
+    return hh::fail(ctx, HH_ERR_CUDA, "hh_matvec_noalloc: " + ctx->noalloc_status);
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return hh::cuda_check(ctx, e, "cudaGetDevice");
+  if (dev != ctx->device)
+    return hh::fail(ctx, HH_ERR_INVALID, "hh_matvec_noalloc: the context's device is not the current device");
+  double2* scr = static_cast<double2*>(ctx->noalloc_scratch);
+  // one vector at a time: each stage 2 finishes reading the scratch before the
+  // next stage 1 (same stream) overwrites it
+  for (int b = 0; b < in->nbatch && e == cudaSuccess; ++b) {
+    double2* x = in->d + (size_t)b * p->nelem;
+    double2* y = out->d + (size_t)b * p->nelem;
+    e = cudaMemsetAsync(y, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
+    if (e == cudaSuccess) e = hh::launch_segment_gemm_fp64(p->stage1, x, scr, y, ctx->stream);
+    if (e == cudaSuccess) e = hh::launch_segment_gemm_fp64(p->stage2, x, scr, y, ctx->stream);
+  }
   return hh::cuda_check(ctx, e, "hh_matvec_noalloc");
 }

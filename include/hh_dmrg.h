@@ -173,9 +173,13 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
  * device budget is reserved up front).  The stage-1 scratch is a static
  * device array of 64 MiB that every GPU loading the library holds until exit;
  * larger plans are rejected with HH_ERR_INVALID.  All calls on a device share
- * the array: calls that overlap on the GPU race.  The first call on a device
- * looks up the array's address (cudaGetSymbolAddress) with that device
- * current; the context's device must be the current device.               */
+ * the array: calls that overlap on the GPU race.  hh_init looks up the
+ * array's address (cudaGetSymbolAddress) with its device current, which loads
+ * the array's module and reserves its 64 MiB when the context is created, not
+ * in a matvec; calls must run with the CUDA context that was current in
+ * hh_init (the device's primary context for runtime-API callers).  Waves of
+ * nbatch vectors are multiplied vector by vector, in and out holding the same
+ * number.                                                                  */
 int hh_matvec_noalloc(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out);
 
 /* pinned host memory for the caller's wave buffers (fast H2D/D2H copies)   */
