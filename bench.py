@@ -82,6 +82,9 @@ def parse():
     p.add_argument("--window-m", type=int, default=2000, help="kept multiplets of the sweep window")
     p.add_argument("--window-steps", type=int, default=4, help="timed mid-chain steps per arm in the sweep window")
     p.add_argument("--window-L", type=int, default=32, help="cylinder length of the sweep window (N_e = 3.5 L)")
+    p.add_argument("--eigensolver", default="own", choices=["own", "cusolver"],
+                   help="density-matrix eigensolver of both arms: the library's own FP64 kernels (default) or "
+                        "cuSOLVER zheevd above 32 states (comparison)")
     return p.parse_args()
 
 
@@ -450,6 +453,8 @@ def main():
     wl = make_workload(args)
     workload_s = time.perf_counter() - t0
     dev = Device(local)
+    dev.check(dev.lib.hh_ctx_set_eigensolver(dev.h, _lib.HH_EIG_OWN if args.eigensolver == "own"
+                                             else _lib.HH_EIG_CUSOLVER))
     # host-side cost of one superblock at this size: operator upload, hmerge
     # and the task list (hh_plan_create), then the split-precision schedule
     # and operator images, built by the first split-precision matvec
@@ -584,6 +589,7 @@ def main():
             "dtype": "c128" if prec == _lib.HH_PREC_FP64 else f"{args.precision}(c128 io)",
             "data": "synthetic",
             "config": dict(wl.describe(), **{"precision": args.precision, "l2": "flushed between steps (256 MB write)",
+                                             "density_eigensolver": args.eigensolver,
                                              "parallelism": f"replicas x{ws}",
                                              "matvec_launch": ("one CUDA-graph replay per step (hh_matvec_async)"
                                                                if prec != _lib.HH_PREC_FP64 else "eager"),

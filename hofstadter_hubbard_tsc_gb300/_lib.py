@@ -17,6 +17,7 @@ HH_ERR_TIMEOUT, HH_ERR_NUMERIC, HH_ERR_UNSUPPORTED = -5, -6, -7
 HH_PREC_FP64 = 0
 HH_PREC_BF16X6 = 1  # three BF16 parts, six products: ~2^-24 per product
 HH_PREC_BF16X3 = 2  # two BF16 parts, three products: ~2^-16 per product
+HH_EIG_OWN, HH_EIG_CUSOLVER = 0, 1  # density-matrix eigensolver (hh_ctx_set_eigensolver)
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
           -4: "quantum number mismatch", -5: "bounded device wait timed out",
@@ -64,6 +65,8 @@ SIGNATURES = {
     "hh_ctx_stream": (I, [P, PP]),
     "hh_ctx_sync": (I, [P]),
     "hh_version": (I, []),
+    "hh_ctx_set_eigensolver": (I, [P, I]),
+    "hh_eig_selftest": (I, [P, I, DP, DP, DP]),
     "hh_block_create": (I, [P, I, I, I, I, IP, DP, PP]),
     "hh_block_zeros": (I, [P, I, I, I, I, IP, PP]),
     "hh_block_info": (I, [P, IP, IP, IP, IP, LLP]),

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libhh_dmrg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
           "--expt-relaxed-constexpr"]
-SOURCES = ["su2.cpp", "plan.cpp", "gemm_fp64.cu", "hh_api.cu", "noalloc.cu", "tc_gemm.cu", "tc_plan.cpp", "step.cu", "eig.cu", "mlp.cu", "enlarge.cu"]
+SOURCES = ["su2.cpp", "plan.cpp", "gemm_fp64.cu", "hh_api.cu", "noalloc.cu", "tc_gemm.cu", "tc_plan.cpp", "step.cu", "eig.cu", "eig_tri.cu", "mlp.cu", "enlarge.cu"]
 LIBS = ["-lcudart", "-lcusolver"]
 
 

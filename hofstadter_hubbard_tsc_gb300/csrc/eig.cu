@@ -1,6 +1,16 @@
 // Batched Hermitian eigensolver for the sectors of a reduced density matrix:
 // the per-sector ZHEEV('V','U') of code/get_den.f90:242, eigenvalues
-// ascending, eigenvectors in place of each sector.
+// ascending.
+//
+// Default path (eig_values, then eig_vectors once the host has chosen the
+// kept states): sectors of up to kJacobiMaxN states are solved completely by
+// the Jacobi kernel below; larger ones go through the tridiagonal pipeline of
+// eig_tri.cu (cluster Householder reduction, bisection for every eigenvalue,
+// inverse iteration and back-transformation for the kept eigenvectors only).
+// Everything is FP64 and the library's own code.
+//
+// Comparison path (eig_hermitian_sectors, HH_EIG_CUSOLVER): every eigenpair,
+// sectors above kJacobiMaxN through cuSOLVER zheevd.
 //
 // Sectors of up to kJacobiMaxN states are solved together in ONE launch, one
 // CTA per sector: cyclic two-sided Jacobi with the round-robin parallel
@@ -8,12 +18,12 @@
 // in an L2-resident scratch matrix.  Jacobi costs about 150 n^3 FP64 flops
 // against zheevd's 22 n^3, and a GB300 SM retires about two FP64 FMAs per
 // clock, so it only pays where zheevd's per-call latency (0.4 ms at n = 8,
-// 1.2 ms at n = 32, 3.7 ms at n = 64, measured) dominates: n <= 32.  Larger
-// sectors go to cuSOLVER zheevd.  Most of a small zheevd's time is host-side
-// work between its kernels, so the large sectors are shared out over kPool
-// host threads, each with its own solver handle and stream; they run
-// concurrently with the Jacobi launch.  A canonical phase is applied to every
-// eigenvector afterwards (one launch).
+// 1.2 ms at n = 32, 3.7 ms at n = 64, measured) dominates: n <= 32.  In the
+// comparison path, larger sectors go to cuSOLVER zheevd; most of a small
+// zheevd's time is host-side work between its kernels, so the large sectors
+// are shared out over kPool host threads, each with its own solver handle and
+// stream, concurrently with the Jacobi launch.  A canonical phase (largest-
+// modulus component real positive) is applied to every eigenvector.
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -22,6 +32,7 @@
 #include <thread>
 #include <vector>
 
+#include "eig_tri.h"
 #include "hh_internal.h"
 
 namespace hh {
@@ -40,13 +51,36 @@ struct EigItem {
   int jacobi;      // 1: Jacobi kernel, 0: zheevd
 };
 
+// What eig_values leaves for eig_vectors.
+struct TriRun {
+  bool valid = false;
+  double2* A = nullptr;                // the sectors (reflectors of the reduced ones)
+  std::vector<long long> offs;
+  std::vector<int> dims;
+  std::vector<long long> woff;         // first eigenvalue of each sector
+  std::vector<int> tri_pos;            // sector -> index in secs, -1 when the Jacobi kernel solved it
+  std::vector<tri::Sector> secs;       // reduced sectors, largest first
+  std::vector<double> w;               // every eigenvalue (host copy)
+  tri::Sector* d_secs = nullptr;
+  double* d_d = nullptr;
+  double* d_e = nullptr;
+  double* d_w = nullptr;
+  double2* d_tau = nullptr;
+};
+
 struct EigState {
+  bool pool_ready = false;             // zheevd streams and handles (comparison path only)
   cusolverDnHandle_t solver[kPool] = {};
   cudaStream_t stream[kPool] = {};
   cudaEvent_t fork = nullptr, join[kPool] = {};
-  void* d_buf = nullptr;
+  void* d_buf = nullptr;               // eig_hermitian_sectors
   size_t cap = 0;
+  void* d_buf2 = nullptr;              // eig_values (kept until eig_vectors)
+  size_t cap2 = 0;
+  void* d_buf3 = nullptr;              // eig_vectors
+  size_t cap3 = 0;
   bool smem_set = false;
+  TriRun run;
 };
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
@@ -226,12 +260,15 @@ __global__ void canonical_phase_kernel(double2* den, const EigItem* __restrict__
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
 int get_state(hh_ctx* ctx, EigState** out) {
-  if (ctx->eig) {
-    *out = (EigState*)ctx->eig;
-    return HH_OK;
-  }
-  EigState* s = new EigState();
-  ctx->eig = s;  // partial state is released by release_step_resources
+  if (!ctx->eig) ctx->eig = new EigState();  // released by release_step_resources
+  *out = (EigState*)ctx->eig;
+  return HH_OK;
+}
+
+// zheevd host threads, streams and handles, created on the first use of the
+// comparison path
+int ensure_pool(hh_ctx* ctx, EigState* s) {
+  if (s->pool_ready) return HH_OK;
   for (int i = 0; i < kPool; ++i) {
     if (cudaStreamCreateWithFlags(&s->stream[i], cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->join[i], cudaEventDisableTiming) != cudaSuccess)
@@ -242,9 +279,33 @@ int get_state(hh_ctx* ctx, EigState** out) {
   }
   if (cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess)
     return fail(ctx, HH_ERR_CUDA, "eigensolver event");
-  *out = s;
+  s->pool_ready = true;
   return HH_OK;
 }
+
+// grow-only device buffer from the context's pool
+int reserve(hh_ctx* ctx, void** buf, size_t* cap, size_t need, const char* what) {
+  if (*cap >= need) return HH_OK;
+  dev_free(ctx, *buf);
+  *buf = nullptr;
+  *cap = 0;
+  cudaError_t e = dev_alloc(ctx, buf, need);
+  if (e != cudaSuccess) return cuda_check(ctx, e, what);
+  *cap = need;
+  return HH_OK;
+}
+
+// bump allocation inside one buffer (256-byte aligned pieces)
+struct Carve {
+  char* base = nullptr;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t n) {
+    T* p = reinterpret_cast<T*>(base + off);
+    off += (std::max<size_t>(1, n) * sizeof(T) + 255) / 256 * 256;
+    return p;
+  }
+};
 
 }  // namespace
 
@@ -258,6 +319,8 @@ void release_step_resources(hh_ctx* ctx) {
   }
   if (s->fork) cudaEventDestroy(s->fork);
   dev_free(ctx, s->d_buf);
+  dev_free(ctx, s->d_buf2);
+  dev_free(ctx, s->d_buf3);
   delete s;
   ctx->eig = nullptr;
 }
@@ -267,6 +330,8 @@ int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>&
   EigState* S = nullptr;
   int st = get_state(ctx, &S);
   if (st) return st;
+  if ((st = ensure_pool(ctx, S))) return st;
+  S->run.valid = false;
   const size_t ns = dims.size();
   std::vector<EigItem> items(ns);
   long long nev = 0, vtot = 0;
@@ -382,6 +447,239 @@ int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>&
                       std::to_string(k));
   }
   *d_w_out = d_w;
+  return HH_OK;
+}
+
+int eig_values(hh_ctx* ctx, double2* A, const std::vector<long long>& offs, const std::vector<int>& dims,
+               bool force_tri, std::vector<double>& w_host) {
+  EigState* S = nullptr;
+  int st = get_state(ctx, &S);
+  if (st) return st;
+  TriRun& R = S->run;
+  R = TriRun();
+  R.A = A;
+  R.offs = offs;
+  R.dims = dims;
+  const size_t ns = dims.size();
+  std::vector<EigItem> items(ns);
+  R.woff.resize(ns);
+  R.tri_pos.assign(ns, -1);
+  long long nev = 0, vtot = 0, ttot = 0;
+  int maxj = 0, maxn = 0;
+  std::vector<int> tri;
+  for (size_t k = 0; k < ns; ++k) {
+    const int n = dims[k];
+    const bool jac = n > 0 && n <= kJacobiMaxN && !force_tri;
+    items[k] = EigItem{offs[k], 0, nev, n, jac ? 1 : 0};
+    R.woff[k] = nev;
+    nev += n;
+    if (jac) {
+      items[k].voff = vtot;
+      vtot += (long long)n * n;
+      maxj = std::max(maxj, n);
+    } else if (n > 0) {
+      tri.push_back((int)k);
+      maxn = std::max(maxn, n);
+    }
+  }
+  if (maxn > tri::kMaxN)
+    return fail(ctx, HH_ERR_UNSUPPORTED, "density sector of " + std::to_string(maxn) +
+                                             " states: the eigensolver takes at most " +
+                                             std::to_string(tri::kMaxN));
+  // largest sectors first: their clusters start first
+  std::stable_sort(tri.begin(), tri.end(), [&](int a, int b) { return dims[a] > dims[b]; });
+  for (size_t q = 0; q < tri.size(); ++q) {
+    const int k = tri[q];
+    R.secs.push_back(tri::Sector{offs[k], ttot, R.woff[k], dims[k], 0});
+    R.tri_pos[k] = (int)q;
+    ttot += dims[k];
+  }
+  const int ntri = (int)R.secs.size();
+  // workspace
+  size_t need = 0;
+  {
+    Carve c;
+    c.take<EigItem>(ns);
+    c.take<int>(ns + 1);
+    c.take<double>(nev);
+    c.take<double2>(vtot);
+    c.take<tri::Sector>(ntri);
+    c.take<double>(ttot);
+    c.take<double>(ttot);
+    c.take<double2>(ttot);
+    c.take<double2>(ttot);
+    c.take<double2>((size_t)ntri * tri::kCluster);
+    need = c.off;
+  }
+  if ((st = reserve(ctx, &S->d_buf2, &S->cap2, need, "allocate eigensolver workspace"))) return st;
+  Carve c;
+  c.base = (char*)S->d_buf2;
+  EigItem* d_items = c.take<EigItem>(ns);
+  int* d_status = c.take<int>(ns + 1);
+  R.d_w = c.take<double>(nev);
+  double2* d_v = c.take<double2>(vtot);
+  R.d_secs = c.take<tri::Sector>(ntri);
+  R.d_d = c.take<double>(ttot);
+  R.d_e = c.take<double>(ttot);
+  R.d_tau = c.take<double2>(ttot);
+  double2* d_p = c.take<double2>(ttot);
+  double2* d_dots = c.take<double2>((size_t)ntri * tri::kCluster);
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (ns > 0) e = cudaMemcpyAsync(d_items, items.data(), ns * sizeof(EigItem), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && ntri > 0)
+    e = cudaMemcpyAsync(R.d_secs, R.secs.data(), ntri * sizeof(tri::Sector), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_status, 0, (ns + 1) * sizeof(int), s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "eigensolver set-up");
+  if (maxj > 0) {
+    if (!S->smem_set) {
+      e = cudaFuncSetAttribute(jacobi_herm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kJacobiMaxN * kJacobiMaxN * (int)sizeof(double2));
+      if (e != cudaSuccess) return cuda_check(ctx, e, "Jacobi shared memory");
+      S->smem_set = true;
+    }
+    jacobi_herm_kernel<<<(unsigned)ns, kJacobiThreads, (size_t)maxj * maxj * sizeof(double2), s>>>(A, d_v, R.d_w,
+                                                                                                  d_items, d_status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_check(ctx, e, "Jacobi eigensolver launch");
+  }
+  e = tri::reduce(R.d_secs, ntri, maxn, A, R.d_d, R.d_e, R.d_tau, d_p, d_dots, s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "tridiagonal reduction");
+  e = tri::bisect(R.d_secs, ntri, maxn, R.d_d, R.d_e, R.d_w, s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "bisection");
+  w_host.assign((size_t)std::max<long long>(1, nev), 0.0);
+  std::vector<int> status(ns + 1, 0);
+  if (nev > 0) e = cudaMemcpyAsync(w_host.data(), R.d_w, nev * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && ns > 0)
+    e = cudaMemcpyAsync(status.data(), d_status, ns * sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "density eigenvalues");
+  for (size_t k = 0; k < ns; ++k)
+    if (items[k].jacobi && status[k] < 0)
+      return fail(ctx, HH_ERR_NUMERIC, "Jacobi eigensolver did not converge in sector " + std::to_string(k));
+  for (long long i = 0; i < nev; ++i)
+    if (!std::isfinite(w_host[i])) return fail(ctx, HH_ERR_NUMERIC, "non-finite density eigenvalue");
+  R.w.assign(w_host.begin(), w_host.begin() + nev);
+  R.valid = true;
+  return HH_OK;
+}
+
+int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std::vector<long long>& xoff) {
+  EigState* S = (EigState*)ctx->eig;
+  if (!S || !S->run.valid) return fail(ctx, HH_ERR_INVALID, "eig_vectors without eig_values");
+  TriRun& R = S->run;
+  const size_t ns = R.dims.size();
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaSuccess;
+  std::vector<tri::InvItem> inv;
+  std::vector<tri::CgsBlock> cgs;
+  std::vector<tri::BtItem> bt;
+  std::vector<tri::PhaseItem> ph;
+  struct Blk { long long zoff, goff; int n, k; };
+  std::vector<Blk> blks;
+  long long zt = 0, gt = 0;
+  int maxn = 0, maxk = 0, maxcols = 0;
+  for (size_t k = 0; k < ns; ++k) {
+    const int n = R.dims[k], nc = ncol[k];
+    if (n <= 0 || nc <= 0) continue;
+    ph.push_back(tri::PhaseItem{xoff[k], n, nc});
+    maxcols = std::max(maxcols, nc);
+    if (R.tri_pos[k] < 0) {  // Jacobi sector: its top nc eigenvectors, ascending
+      e = cudaMemcpyAsync(X + xoff[k], R.A + R.offs[k] + (long long)(n - nc) * n, (size_t)n * nc * sizeof(double2),
+                          cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_check(ctx, e, "kept eigenvectors");
+      continue;
+    }
+    const int q = R.tri_pos[k];
+    for (int col = 0; col < nc; ++col) inv.push_back(tri::InvItem{q, n - nc + col, col, nc, zt});
+    // numerically degenerate kept eigenvalues: Gram-Schmidt before Newton-Schulz
+    const double* wk = R.w.data() + R.woff[k];
+    const double tn = std::max(std::fabs(wk[0]), std::fabs(wk[n - 1]));
+    bool degenerate = false;
+    for (int j = n - nc; j + 1 < n; ++j)
+      if (wk[j + 1] - wk[j] <= 1e-13 * tn) degenerate = true;
+    if (degenerate) cgs.push_back(tri::CgsBlock{zt, n, nc});
+    for (int c0 = 0; c0 < nc; c0 += tri::kBtCols)
+      bt.push_back(tri::BtItem{q, c0, std::min(tri::kBtCols, nc - c0), nc, zt, xoff[k]});
+    blks.push_back(Blk{zt, gt, n, nc});
+    zt += (long long)n * nc;
+    gt += (long long)nc * nc;
+    maxn = std::max(maxn, n);
+    maxk = std::max(maxk, nc);
+  }
+  // Newton-Schulz: three steps Z -> Z1 -> Z -> Z1, each G = Z^T Z then
+  // Z' = 1.5 Z - 0.5 Z G (buffer: Z at 0, Z1 at zt, G at 2 zt)
+  constexpr int kSteps = 3;
+  std::vector<tri::GemmItem> gi[2 * kSteps];
+  int ntiles[2 * kSteps] = {};
+  for (int stp = 0; stp < kSteps; ++stp) {
+    const long long zin = (stp % 2 == 0) ? 0 : zt, zout = (stp % 2 == 0) ? zt : 0, g0 = 2 * zt;
+    for (const Blk& b : blks) {
+      tri::GemmItem G{};
+      G.a = zin + b.zoff; G.b = zin + b.zoff; G.c = g0 + b.goff; G.c0 = G.c;
+      G.M = b.k; G.N = b.k; G.K = b.n;
+      G.a_r = 1; G.a_c = b.k; G.b_r = b.k; G.b_c = 1; G.c_r = b.k; G.c_c = 1;
+      G.alpha = 1.0; G.beta = 0.0;
+      G.tiles_n = (b.k + 63) / 64;
+      G.tile0 = ntiles[2 * stp];
+      ntiles[2 * stp] += ((b.k + 63) / 64) * G.tiles_n;
+      gi[2 * stp].push_back(G);
+      tri::GemmItem H{};
+      H.a = zin + b.zoff; H.b = g0 + b.goff; H.c = zout + b.zoff; H.c0 = zin + b.zoff;
+      H.M = b.n; H.N = b.k; H.K = b.k;
+      H.a_r = b.k; H.a_c = 1; H.b_r = b.k; H.b_c = 1; H.c_r = b.k; H.c_c = 1;
+      H.alpha = -0.5; H.beta = 1.5;
+      H.tiles_n = (b.k + 63) / 64;
+      H.tile0 = ntiles[2 * stp + 1];
+      ntiles[2 * stp + 1] += ((b.n + 63) / 64) * H.tiles_n;
+      gi[2 * stp + 1].push_back(H);
+    }
+  }
+  const long long final_z = (kSteps % 2 == 1) ? zt : 0;
+  const int nitems = (int)inv.size();
+  size_t need = 0;
+  {
+    Carve c;
+    c.take<tri::InvItem>(inv.size());
+    c.take<double>((size_t)5 * maxn * std::max(1, nitems));
+    c.take<double>((size_t)(2 * zt + gt));
+    for (auto& v : gi) c.take<tri::GemmItem>(v.size());
+    c.take<tri::BtItem>(bt.size());
+    c.take<tri::PhaseItem>(ph.size());
+    c.take<tri::CgsBlock>(cgs.size());
+    need = c.off;
+  }
+  int st = reserve(ctx, &S->d_buf3, &S->cap3, need, "allocate eigenvector workspace");
+  if (st) return st;
+  Carve c;
+  c.base = (char*)S->d_buf3;
+  tri::InvItem* d_inv = c.take<tri::InvItem>(inv.size());
+  double* d_lu = c.take<double>((size_t)5 * maxn * std::max(1, nitems));
+  double* d_z = c.take<double>((size_t)(2 * zt + gt));
+  tri::GemmItem* d_gi[2 * kSteps];
+  for (int q = 0; q < 2 * kSteps; ++q) d_gi[q] = c.take<tri::GemmItem>(gi[q].size());
+  tri::BtItem* d_bt = c.take<tri::BtItem>(bt.size());
+  tri::PhaseItem* d_ph = c.take<tri::PhaseItem>(ph.size());
+  tri::CgsBlock* d_cgs = c.take<tri::CgsBlock>(cgs.size());
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess && bytes > 0) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+  };
+  up(d_inv, inv.data(), inv.size() * sizeof(tri::InvItem));
+  for (int q = 0; q < 2 * kSteps; ++q) up(d_gi[q], gi[q].data(), gi[q].size() * sizeof(tri::GemmItem));
+  up(d_bt, bt.data(), bt.size() * sizeof(tri::BtItem));
+  up(d_ph, ph.data(), ph.size() * sizeof(tri::PhaseItem));
+  up(d_cgs, cgs.data(), cgs.size() * sizeof(tri::CgsBlock));
+  if (e != cudaSuccess) return cuda_check(ctx, e, "eigenvector work lists");
+  if (nitems > 0) {
+    e = tri::inverse_iteration(R.d_secs, d_inv, nitems, maxn, R.d_d, R.d_e, R.d_w, d_z, d_lu, s);
+    if (e == cudaSuccess) e = tri::cgs2(d_cgs, (int)cgs.size(), maxk, d_z, s);
+    for (int q = 0; q < 2 * kSteps && e == cudaSuccess; ++q) e = tri::gemm(d_gi[q], (int)gi[q].size(), ntiles[q], d_z, s);
+    if (e == cudaSuccess) e = tri::backtransform(R.d_secs, d_bt, (int)bt.size(), R.A, R.d_tau, d_z + final_z, X, s);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "kept eigenvectors (inverse iteration)");
+  }
+  e = tri::phase_columns(d_ph, (int)ph.size(), maxcols, X, s);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "canonical phase");
+  R.valid = false;
   return HH_OK;
 }
 

@@ -45,8 +45,10 @@ struct hh_ctx {
   double* h_red = nullptr;  // pinned
   size_t h_red_cap = 0;
   // density-matrix eigensolver state (streams, solver handles, workspace),
-  // created on first use (eig.cu)
+  // created on first use (eig.cu), and the eigensolver in use
+  // (HH_EIG_OWN or HH_EIG_CUSOLVER)
   void* eig = nullptr;
+  int eig_solver = 0;
   // device address of the static scratch array of hh_matvec_noalloc, looked
   // up by hh_init in this context (noalloc.cu); null with a reason if that
   // lookup failed
@@ -298,6 +300,17 @@ int tridiag_lowest(int n, const double* alpha, const double* beta, double* e0, d
 // size dims[k]; *d_w is context-owned scratch valid until the next call.
 int eig_hermitian_sectors(hh_ctx* ctx, double2* A, const std::vector<long long>& offs,
                           const std::vector<int>& dims, double** d_w);
+// The library's own two-phase eigensolver of the same sectors (eig.cu):
+// eig_values returns every eigenvalue (ascending per sector, sectors in
+// order) on the host and leaves the reduced sectors in A; eig_vectors then
+// writes the eigenvectors of the ncol[k] largest eigenvalues of sector k,
+// ascending, in the canonical phase, to X + xoff[k] (column-major, ld dims[k])
+// on the context stream.  force_tri sends every sector through the
+// tridiagonal pipeline (tests), otherwise sectors of up to 32 states are
+// solved by the Jacobi kernel.
+int eig_values(hh_ctx* ctx, double2* A, const std::vector<long long>& offs, const std::vector<int>& dims,
+               bool force_tri, std::vector<double>& w_host);
+int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std::vector<long long>& xoff);
 // frees the eigensolver state held by the context
 void release_step_resources(hh_ctx* ctx);
 }  // namespace hh

@@ -138,8 +138,8 @@ extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side
     hh_block_free(den);
     return st;
   }
-  // ---- per-sector eigensolve (ZHEEV 'V','U', ascending; code/get_den.f90:242)
-  double* d_w = nullptr;
+  // ---- per-sector eigensolve (ZHEEV 'V','U', ascending; code/get_den.f90:242):
+  // every eigenvalue now, the eigenvectors of the kept states once they are known
   long long nev = 0;
   std::vector<long long> offs;
   std::vector<int> dims;
@@ -148,15 +148,22 @@ extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side
     dims.push_back(sq.sdim);
     nev += sq.sdim;
   }
-  if ((st = eig_hermitian_sectors(ctx, den->d, offs, dims, &d_w))) {
+  const bool own = ctx->eig_solver == HH_EIG_OWN;
+  std::vector<double> w(std::max<long long>(1, nev));
+  cudaError_t e = cudaSuccess;
+  if (own) {
+    st = eig_values(ctx, den->d, offs, dims, false, w);
+  } else {
+    double* d_w = nullptr;
+    st = eig_hermitian_sectors(ctx, den->d, offs, dims, &d_w);
+    if (!st) {
+      e = cudaMemcpy(w.data(), d_w, nev * sizeof(double), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) st = cuda_check(ctx, e, "density eigenvalues");
+    }
+  }
+  if (st) {
     hh_block_free(den);
     return st;
-  }
-  std::vector<double> w(std::max<long long>(1, nev));
-  cudaError_t e = cudaMemcpy(w.data(), d_w, nev * sizeof(double), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    hh_block_free(den);
-    return cuda_check(ctx, e, "density eigenvalues");
   }
   // ---- global sort, renormalisation, selection (code/get_den.f90:268-311)
   std::vector<double> arr(w.begin(), w.begin() + nev);
@@ -202,12 +209,27 @@ extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side
     hh_block_free(den);
     return st;
   }
-  for (size_t t = 0; t < tcols.size(); ++t) {
-    const auto& ds = den->subs[tcols[t].first];
-    const int n = ds.sdim, ncol = tcols[t].second;
-    e = cudaMemcpyAsync(trun->d + trun->subs[t].off, den->d + ds.off + (long long)(n - ncol) * n,
-                        (size_t)n * ncol * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream);
-    if (e != cudaSuccess) break;
+  if (own) {
+    std::vector<int> ncolv(den->subs.size(), 0);
+    std::vector<long long> xoff(den->subs.size(), 0);
+    for (size_t t = 0; t < tcols.size(); ++t) {
+      ncolv[tcols[t].first] = tcols[t].second;
+      xoff[tcols[t].first] = trun->subs[t].off;
+    }
+    st = eig_vectors(ctx, ncolv, trun->d, xoff);
+    if (st) {
+      hh_block_free(den);
+      hh_block_free(trun);
+      return st;
+    }
+  } else {
+    for (size_t t = 0; t < tcols.size(); ++t) {
+      const auto& ds = den->subs[tcols[t].first];
+      const int n = ds.sdim, ncol = tcols[t].second;
+      e = cudaMemcpyAsync(trun->d + trun->subs[t].off, den->d + ds.off + (long long)(n - ncol) * n,
+                          (size_t)n * ncol * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream);
+      if (e != cudaSuccess) break;
+    }
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   hh_block_free(den);
@@ -222,6 +244,34 @@ extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side
   if (spectrum)
     for (long long i = 0; i < nev; ++i) spectrum[i] = arr[i];
   return HH_OK;
+}
+
+extern "C" int hh_ctx_set_eigensolver(hh_ctx_t* ctx, int solver) {
+  if (!ctx || (solver != HH_EIG_OWN && solver != HH_EIG_CUSOLVER)) return HH_ERR_INVALID;
+  ctx->eig_solver = solver;
+  return HH_OK;
+}
+
+extern "C" int hh_eig_selftest(hh_ctx_t* ctx, int n, const double* A, double* w, double* V) {
+  if (!ctx || n <= 0 || !A || !w || !V) return HH_ERR_INVALID;
+  const size_t bytes = (size_t)n * n * sizeof(double2);
+  double2 *dA = nullptr, *dX = nullptr;
+  cudaError_t e = dev_alloc(ctx, (void**)&dA, bytes);
+  if (e == cudaSuccess) e = dev_alloc(ctx, (void**)&dX, bytes);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dA, A, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  int st = e == cudaSuccess ? HH_OK : cuda_check(ctx, e, "eig selftest set-up");
+  std::vector<double> wh;
+  if (!st) st = eig_values(ctx, dA, {0}, {n}, true, wh);
+  if (!st) st = eig_vectors(ctx, {n}, dX, {0});
+  if (!st) {
+    e = cudaMemcpyAsync(V, dX, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) st = cuda_check(ctx, e, "eig selftest");
+    for (int i = 0; i < n && !st; ++i) w[i] = wh[i];
+  }
+  dev_free(ctx, dA);
+  dev_free(ctx, dX);
+  return st;
 }
 
 extern "C" int hh_renormalize(hh_ctx_t* ctx, const hh_block_t* ori, const hh_block_t* trun, int dia,

@@ -56,6 +56,24 @@ int hh_ctx_stream(hh_ctx_t* ctx, void** stream);   /* cudaStream_t of the contex
 int hh_ctx_sync(hh_ctx_t* ctx);
 int hh_version(void);
 
+/* Eigensolver of the density-matrix sectors (hh_density_truncate), all FP64:
+ * HH_EIG_OWN (default): the library's own kernels -- sectors of up to 32
+ *   states by one-CTA Jacobi, larger ones by Householder reduction to a real
+ *   tridiagonal on a thread-block cluster, bisection for every eigenvalue,
+ *   and inverse iteration plus back-transformation for the kept
+ *   eigenvectors only;
+ * HH_EIG_CUSOLVER: every eigenpair, sectors above 32 states by cuSOLVER
+ *   zheevd (kept for comparison).                                          */
+#define HH_EIG_OWN 0
+#define HH_EIG_CUSOLVER 1
+int hh_ctx_set_eigensolver(hh_ctx_t* ctx, int solver);
+/* Diagnostic: every eigenpair of one dense Hermitian matrix A (n x n,
+ * column-major, interleaved complex) through the tridiagonal pipeline of
+ * HH_EIG_OWN (whatever n): w ascending (n doubles), V the eigenvectors
+ * (n x n interleaved complex, canonical phase: the largest-modulus component
+ * of each column real positive).                                          */
+int hh_eig_selftest(hh_ctx_t* ctx, int n, const double* A, double* w, double* V);
+
 /* ----------------------------------------------- Total_Block (operators)
  * Replaces the in-memory Total_Block of code/pubdata.f90:141-149 with a
  * device-resident copy.  sub_qn holds 5 ints per sub: num_up, num_down,
