@@ -543,7 +543,14 @@ int eig_values(hh_ctx* ctx, double2* A, const std::vector<long long>& offs, cons
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_check(ctx, e, "Jacobi eigensolver launch");
   }
-  e = tri::reduce(R.d_secs, ntri, maxn, A, R.d_d, R.d_e, R.d_tau, d_p, d_dots, s);
+  // sectors that fit a cluster's shared memory are reduced there; the few
+  // larger ones (first in the list) by the global-memory kernel
+  const int ds_max = tri::ds_max_n();
+  int nglob = 0;
+  while (nglob < ntri && R.secs[nglob].n > ds_max) ++nglob;
+  if (nglob > 0) e = tri::reduce(R.d_secs, nglob, maxn, A, R.d_d, R.d_e, R.d_tau, d_p, d_dots, s);
+  if (e == cudaSuccess && nglob < ntri)
+    e = tri::reduce_ds(R.d_secs + nglob, ntri - nglob, R.secs[nglob].n, A, R.d_d, R.d_e, R.d_tau, s);
   if (e != cudaSuccess) return cuda_check(ctx, e, "tridiagonal reduction");
   e = tri::bisect(R.d_secs, ntri, maxn, R.d_d, R.d_e, R.d_w, s);
   if (e != cudaSuccess) return cuda_check(ctx, e, "bisection");

@@ -6,12 +6,16 @@
 //
 //   1. reduce: Householder reduction of each sector to a real symmetric
 //      tridiagonal T = Q^H A Q (the unblocked lower-triangle algorithm of
-//      zhetd2).  One thread-block cluster of kCluster CTAs per sector: the
-//      sector stays in global memory (L2-resident), the rows of the trailing
-//      block are split over the CTAs, and two cluster barriers per column
-//      order the matrix-vector product and the rank-2 update;
+//      zhetd2).  One thread-block cluster per sector: sectors of up to about
+//      600 states are held in the cluster's distributed shared memory
+//      (reduce_ds_kernel, 16 CTAs where the device allows, else 8); larger
+//      ones stay in global memory (reduce_kernel, L2-resident, rows of the
+//      trailing block split over the CTAs);
 //   2. bisect: every eigenvalue of every T by bisection on Sturm counts, one
-//      thread per eigenvalue, to an absolute accuracy of a few eps ||T||;
+//      thread per eigenvalue: first in FP32 on a scaled copy of T, which
+//      brackets the eigenvalue to a few FP32 eps ||T|| at a sixty-fourth of
+//      the FP64 cost on GB300, then (bracket confirmed by FP64 counts) in
+//      FP64 to an absolute accuracy of a few eps ||T||;
 //   (the host sorts all eigenvalues and selects the kept states)
 //   3. inverse_iteration: each kept eigenvector of T from three steps of
 //      inverse iteration (Gaussian elimination with partial pivoting of
@@ -27,6 +31,7 @@
 #include "eig_tri.h"
 
 #include <cfloat>
+#include <cmath>
 #include <cstdint>
 
 namespace hh {
@@ -49,6 +54,19 @@ __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {
 // c + conj(a) b
 __device__ __forceinline__ double2 cfmac(double2 a, double2 b, double2 c) {
   return make_double2(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+
+// b - v_i conj(w_j) - w_i conj(v_j) as eight FMAs
+__device__ __forceinline__ double2 rank2(double2 b, double2 vi, double2 wi, double2 vj, double2 wj) {
+  double re = fma(-vi.x, wj.x, b.x);
+  re = fma(-vi.y, wj.y, re);
+  re = fma(-wi.x, vj.x, re);
+  re = fma(-wi.y, vj.y, re);
+  double im = fma(-vi.y, wj.x, b.y);
+  im = fma(vi.x, wj.y, im);
+  im = fma(-wi.y, vj.x, im);
+  im = fma(wi.x, vj.y, im);
+  return make_double2(re, im);
 }
 
 // Sum over the CTA; every thread receives it.  scratch holds >= 32 entries.
@@ -77,10 +95,10 @@ __device__ double2 block_sum2(double2 v, double2* scratch) {
   return s;
 }
 
-// Release/acquire barrier over the CTAs of the cluster: global-memory writes
-// before it are visible to every CTA of the cluster after it.  Every thread of
-// every CTA calls it the same number of times (no CTA-dependent branches
-// around it).
+// Release/acquire barrier over the CTAs of the cluster: global- and shared-
+// memory writes before it are visible to every CTA of the cluster after it.
+// Every thread of every CTA calls it the same number of times (no
+// CTA-dependent branches around it).
 __device__ __forceinline__ void cluster_barrier() {
   __threadfence();
   asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
@@ -211,49 +229,334 @@ __global__ void __launch_bounds__(kReduceThreads)
   }
 }
 
+// ------------------------------------------------------- reduce (DSMEM)
+// The same reduction with the sector held in the cluster's distributed
+// shared memory.  CTA r of the C-CTA cluster owns the columns j = r, r + C,
+// r + 2C, ... (cyclic, so the shrinking trailing block stays balanced) and
+// keeps only their lower parts, rows j .. n-1, packed one after another;
+// B(i, j) for i < j is conj(B(j, i)).  Per column k, three cluster barriers:
+//   (A) the owner of column k forms the reflector (d_k, e_k, tau_k, v) from
+//       its copy of the column, writes v to global memory (for the back-
+//       transformation) and to its vector slot;                  barrier 1
+//   (B) every CTA copies v from the owner and forms its partial B v from its
+//       own columns: rows i >= j of column j (row part) and the column's
+//       conjugate dot with v (column part);                       barrier 2
+//   (C) reduce-scatter: CTA r sums the C partials of the rows i = r (mod C),
+//       scales them by tau and forms its share of p^H v;          barrier 3
+//   (D) every CTA gathers p, forms w = p - (tau/2)(p^H v) v and applies
+//       B <- B - v w^H - w v^H to its own lower columns.
+// The vector slots sit at the front of the dynamic allocation, so at the same
+// offsets in every CTA, and are read remotely through mapa addresses.  A CTA
+// does about 8 m^2 / C FP64 FMAs per column (m = n - k - 1): with GB300's
+// FP64 pipe the kernel is FP64-bound above ~100 states and barrier-bound
+// below.
+__host__ __device__ __forceinline__ long long ds_col_off(int q, int n, int C, int r) {
+  // packed offset of owned column q (column q C + r): sum over q' < q of n - (q' C + r)
+  return (long long)q * (n - r) - (long long)C * q * (q - 1) / 2;
+}
+
+// shared::cluster address of the same shared-memory object in CTA `rank`
+__device__ __forceinline__ uint32_t ds_map(const void* p, int rank) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+  uint32_t ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  return ra;
+}
+
+__device__ __forceinline__ double2 ds_ld2(uint32_t addr) {
+  double2 v;
+  asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(addr) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return (int)r;
+}
+
+__device__ __forceinline__ int cluster_nctas() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return (int)r;
+}
+
+__global__ void __launch_bounds__(kDsThreads, 1)
+    reduce_ds_kernel(double2* __restrict__ den, const Sector* __restrict__ secs, double* __restrict__ dvec,
+                     double* __restrict__ evec, double2* __restrict__ tauv) {
+  constexpr int kWarps = kDsThreads / 32;
+  const int C = cluster_nctas();
+  const int r = cluster_rank();
+  const Sector S = secs[blockIdx.x / C];
+  const int n = S.n;
+  double2* A = den + S.aoff;
+  extern __shared__ double2 sm[];
+  double2* vb = sm;           // v, indexed by row (rows k+1 .. n-1)
+  double2* wb = sm + n;       // p, then w
+  double2* pp = sm + 2 * n;   // this CTA's partial B v
+  double2* ps = sm + 3 * n;   // tau (B v) of the rows i = r (mod C), summed over the cluster
+  double2* col = sm + 4 * n;  // the owned lower columns
+  __shared__ double2 s_tau, s_dot, s_dots[kClusterMax];
+  __shared__ double red_d[32];
+  __shared__ double2 red_c[kWarps];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int nq = n > r ? (n - r + C - 1) / C : 0;
+  for (int q = 0; q < nq; ++q) {
+    const int j = q * C + r;
+    const long long o = ds_col_off(q, n, C, r);
+    for (int i = j + t; i < n; i += kDsThreads) col[o + (i - j)] = A[(long long)j * n + i];
+  }
+  __syncthreads();
+  for (int k = 0; k + 1 < n; ++k) {
+    const int owner = k % C;
+    // ---- (A) reflector of column k (zlarfg)
+    if (owner == r) {
+      const double2* x = col + ds_col_off(k / C, n, C, r);  // x[i - k] = B(i, k), i >= k
+      double xn = 0.0;
+      for (int i = k + 2 + t; i < n; i += kDsThreads) {
+        const double2 xi = x[i - k];
+        xn += xi.x * xi.x + xi.y * xi.y;
+      }
+      xn = block_sum(xn, red_d);
+      const double2 alpha = x[1];
+      double2 tau = make_double2(0.0, 0.0), scale = make_double2(0.0, 0.0);
+      double beta = alpha.x;
+      if (xn > 0.0 || alpha.y != 0.0) {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn), alpha.x);
+        tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+        const double2 den_ = make_double2(alpha.x - beta, alpha.y);  // 1 / (alpha - beta)
+        const double r2 = den_.x * den_.x + den_.y * den_.y;
+        scale = make_double2(den_.x / r2, -den_.y / r2);
+      }
+      if (t == 0) {
+        dvec[S.toff + k] = x[0].x;
+        evec[S.toff + k] = beta;
+        tauv[S.toff + k] = tau;
+        s_tau = tau;
+      }
+      for (int i = k + 1 + t; i < n; i += kDsThreads) {
+        const double2 vi = i == k + 1 ? make_double2(1.0, 0.0) : cmul(x[i - k], scale);
+        vb[i] = vi;
+        A[(long long)k * n + i] = vi;
+      }
+    }
+    cluster_barrier();  // 1: the owner's v and tau are complete
+    // ---- (B) v from the owner, then this CTA's partial B v
+    double2 tau;
+    if (owner != r) {
+      const uint32_t rv = ds_map(vb, owner);
+      for (int i = k + 1 + t; i < n; i += kDsThreads) vb[i] = ds_ld2(rv + (uint32_t)(i * sizeof(double2)));
+      tau = ds_ld2(ds_map(&s_tau, owner));
+    } else {
+      tau = s_tau;
+    }
+    __syncthreads();
+    const int qlo = k + 1 > r ? (k + 1 - r + C - 1) / C : 0;  // first owned column > k
+    const long long olo = ds_col_off(qlo, n, C, r);
+    // row part: pp[i] = sum over owned j in (k, i] of B(i, j) v_j
+    for (int i = k + 1 + t; i < n; i += kDsThreads) {
+      double2 acc = make_double2(0.0, 0.0);
+      long long o = olo;
+      for (int j = qlo * C + r; j <= i; j += C) {
+        acc = cfma(col[o + (i - j)], vb[j], acc);
+        o += n - j;
+      }
+      pp[i] = acc;
+    }
+    __syncthreads();
+    // column part: pp[j] += sum over i > j of conj(B(i, j)) v_i, one warp per owned column
+    for (int q = qlo + warp, j = (qlo + warp) * C + r; j < n; q += kWarps, j += kWarps * C) {
+      const long long o = ds_col_off(q, n, C, r);
+      double2 sum = make_double2(0.0, 0.0);
+      for (int i = j + 1 + lane; i < n; i += 32) sum = cfmac(col[o + (i - j)], vb[i], sum);
+      for (int sh = 16; sh > 0; sh >>= 1) {
+        sum.x += __shfl_xor_sync(0xffffffffu, sum.x, sh);
+        sum.y += __shfl_xor_sync(0xffffffffu, sum.y, sh);
+      }
+      if (lane == 0) pp[j] = cadd(pp[j], sum);
+    }
+    cluster_barrier();  // 2: every CTA's partial is complete
+    // ---- (C) reduce-scatter of the rows i = r (mod C) and this CTA's share of p^H v
+    {
+      const int i0 = k + 1 + ((r - (k + 1)) % C + C) % C;  // first row > k with i = r (mod C)
+      const int nr = i0 < n ? (n - 1 - i0) / C + 1 : 0;
+      const int src = t % C, slot = t / C, per = kDsThreads / C;
+      const uint32_t rp = ds_map(pp, src);
+      double2 dot = make_double2(0.0, 0.0);
+      for (int base = 0; base < nr; base += per) {  // the same trip count in every thread
+        const int ri = base + slot, i = i0 + ri * C;
+        // every lane of a C-lane group takes part in its shuffles
+        double2 val = ri < nr ? ds_ld2(rp + (uint32_t)(i * sizeof(double2))) : make_double2(0.0, 0.0);
+        for (int sh = C >> 1; sh > 0; sh >>= 1) {
+          val.x += __shfl_xor_sync(0xffffffffu, val.x, sh);
+          val.y += __shfl_xor_sync(0xffffffffu, val.y, sh);
+        }
+        if (src == 0 && ri < nr) {
+          const double2 p = cmul(tau, val);
+          ps[i] = p;
+          dot = cfmac(p, vb[i], dot);  // conj(p_i) v_i
+        }
+      }
+      for (int sh = 16; sh > 0; sh >>= 1) {
+        dot.x += __shfl_xor_sync(0xffffffffu, dot.x, sh);
+        dot.y += __shfl_xor_sync(0xffffffffu, dot.y, sh);
+      }
+      if (lane == 0) red_c[warp] = dot;
+      __syncthreads();
+      if (t == 0) {
+        double2 sd = make_double2(0.0, 0.0);
+        for (int w = 0; w < kWarps; ++w) sd = cadd(sd, red_c[w]);
+        s_dot = sd;
+      }
+    }
+    cluster_barrier();  // 3: p and the partial dots are complete
+    // ---- (D) w = p + a2 v with a2 = -(tau/2) (p^H v); rank-2 update of the owned columns
+    if (t < C) s_dots[t] = ds_ld2(ds_map(&s_dot, t));
+    for (int i = k + 1 + t; i < n; i += kDsThreads) wb[i] = ds_ld2(ds_map(ps + i, i % C));
+    __syncthreads();
+    {
+      double2 sdot = make_double2(0.0, 0.0);
+      for (int c = 0; c < C; ++c) sdot = cadd(sdot, s_dots[c]);
+      const double2 a2 = cmul(make_double2(-0.5 * tau.x, -0.5 * tau.y), sdot);
+      for (int i = k + 1 + t; i < n; i += kDsThreads) wb[i] = cfma(a2, vb[i], wb[i]);
+    }
+    __syncthreads();
+    for (int i = k + 1 + t; i < n; i += kDsThreads) {
+      const double2 vi = vb[i], wi = wb[i];
+      long long o = olo;
+      for (int j = qlo * C + r; j <= i; j += C) {
+        col[o + (i - j)] = rank2(col[o + (i - j)], vi, wi, vb[j], wb[j]);
+        o += n - j;
+      }
+    }
+    __syncthreads();  // the owner of column k + 1 reads its updated column next
+  }
+  if (n > 0 && (n - 1) % C == r && t == 0) {
+    dvec[S.toff + n - 1] = col[ds_col_off((n - 1) / C, n, C, r)].x;
+    evec[S.toff + n - 1] = 0.0;
+    tauv[S.toff + n - 1] = make_double2(0.0, 0.0);
+  }
+  cluster_barrier();  // no CTA leaves while another may still read its shared memory
+}
+
 // ---------------------------------------------------------------- bisect
-// Number of eigenvalues of T (d, e) below x: negative pivots of the LDL^T
-// factorisation of T - x I, q_i = (d_i - x) - e_{i-1}^2 / q_{i-1}, a pivot
-// smaller than pivmin replaced by -pivmin (Sturm sequence, as dstebz counts).
-__device__ __forceinline__ int sturm_count(const double* d, const double* e, int n, double x, double pivmin) {
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  int c = q < 0.0;
+// Number of eigenvalues of T (d, e) below x: the negative pivots q_i of the
+// LDL^T factorisation of T - x I, a pivot smaller than pivmin replaced by
+// -pivmin (the Sturm count of dstebz).  The FP64 count runs on the leading
+// principal minors p_{i+1} = (d_i - x) p_i - e_{i-1}^2 p_{i-1} (q_i =
+// p_{i+1} / p_i, so a negative pivot is a sign change) without the division
+// per step, which costs GB300's FP64 pipe several operations; the pair of
+// minors is rescaled by powers of two to stay in range, and a minor below
+// pivmin times the previous one stands for the pivot -pivmin.  e2 holds e^2.
+__device__ __forceinline__ int sturm_count(const double* d, const double* e2, int n, double x, double pivmin) {
+  double pm = 1.0, p = d[0] - x;
+  if (fabs(p) < pivmin) p = -pivmin;
+  int c = p < 0.0;
   for (int i = 1; i < n; ++i) {
-    const double ei = e[i - 1];
-    q = (d[i] - x) - ei * ei / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    c += q < 0.0;
+    double pn = fma(d[i] - x, p, -e2[i - 1] * pm);
+    const double ap = fabs(p);
+    if (fabs(pn) < pivmin * ap) pn = p < 0.0 ? pivmin * ap : -pivmin * ap;
+    c += (pn < 0.0) != (p < 0.0);
+    pm = p;
+    p = pn;
+    const double a = fabs(p);
+    if (a > 0x1p+400 || a < 0x1p-400) {
+      int ex;
+      frexp(a, &ex);
+      p = ldexp(p, -ex);
+      pm = ldexp(pm, -ex);
+    }
   }
   return c;
 }
 
+// The pivot count in FP32 on T scaled by a power of two (d32 = s d, e32 =
+// (s e)^2, s ||T|| in [1/2, 1)).
+__device__ __forceinline__ int sturm_count32(const float* d, const float* e2, int n, float x, float pivmin) {
+  float q = d[0] - x;
+  if (fabsf(q) < pivmin) q = -pivmin;
+  int c = q < 0.0f;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - e2[i - 1] / q;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    c += q < 0.0f;
+  }
+  return c;
+}
+
+// One warp per CTA, blockIdx.y = sector, thread = eigenvalue index j: T is
+// staged in shared memory in FP64 and, scaled, in FP32.  The FP32 bisection
+// brackets lambda_j to a few FP32 eps ||T||; the bracket, widened by
+// 16 FP32 eps ||T|| (beyond the FP32 count's backward error), is kept when
+// FP64 counts confirm it, else the Gershgorin interval is used; FP64
+// bisection then closes it to 2 eps ||T|| + 4 pivmin.
 __global__ void bisect_kernel(const Sector* __restrict__ secs, const double* __restrict__ dvec,
                               const double* __restrict__ evec, double* __restrict__ w) {
   const Sector S = secs[blockIdx.y];
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= S.n) return;
   const int n = S.n;
-  const double* d = dvec + S.toff;
-  const double* e = evec + S.toff;
-  // Gershgorin interval and the scale of T
-  double lo = 0.0, hi = 0.0, emax2 = 0.0;
-  for (int i = 0; i < n; ++i) {
-    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
-    lo = i == 0 ? d[i] - r : fmin(lo, d[i] - r);
-    hi = i == 0 ? d[i] + r : fmax(hi, d[i] + r);
+  if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole CTA is beyond this sector
+  extern __shared__ double sh[];
+  double* d = sh;                                      // n
+  double* e2 = sh + n;                                 // n: e_i^2
+  float* d32 = reinterpret_cast<float*>(sh + 2 * n);   // n
+  float* e32 = d32 + n;                                // n: (s e_i)^2
+  const int lane = threadIdx.x;                        // blockDim.x == 32
+  double lo = 1e300, hi = -1e300, emax2 = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double di = dvec[S.toff + i];
+    const double ei = i + 1 < n ? evec[S.toff + i] : 0.0;
+    const double em = i > 0 ? evec[S.toff + i - 1] : 0.0;
+    const double rr = fabs(ei) + fabs(em);
+    d[i] = di;
+    e2[i] = ei * ei;
+    emax2 = fmax(emax2, ei * ei);
+    lo = fmin(lo, di - rr);
+    hi = fmax(hi, di + rr);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
   }
   const double tnorm = fmax(fabs(lo), fabs(hi));
   const double pivmin = DBL_MIN * fmax(1.0, emax2);
   const double tol = 2.0 * DBL_EPSILON * tnorm + 4.0 * pivmin;
+  int ex = 0;
+  frexp(tnorm > 0.0 ? tnorm : 1.0, &ex);
+  const double sc = ldexp(1.0, -ex);
+  for (int i = lane; i < n; i += 32) {
+    d32[i] = (float)(sc * d[i]);
+    const double es = sc * sqrt(e2[i]);
+    e32[i] = (float)(es * es);
+  }
+  __syncwarp();
+  const int j = blockIdx.x * blockDim.x + lane;
+  if (j >= n) return;
   lo -= tol;
   hi += tol;
+  {
+    float l32 = (float)(sc * lo), h32 = (float)(sc * hi);
+    const float tol32 = 4.0f * FLT_EPSILON, piv32 = 16.0f * FLT_MIN;
+    for (int it = 0; it < 64 && h32 - l32 > tol32; ++it) {
+      const float mid = 0.5f * (l32 + h32);
+      if (mid <= l32 || mid >= h32) break;
+      if (sturm_count32(d32, e32, n, mid, piv32) > j)
+        h32 = mid;
+      else
+        l32 = mid;
+    }
+    const double widen = 16.0 * FLT_EPSILON;
+    const double blo = fmax(lo, ((double)l32 - widen) / sc), bhi = fmin(hi, ((double)h32 + widen) / sc);
+    if (blo < bhi && sturm_count(d, e2, n, blo, pivmin) <= j && sturm_count(d, e2, n, bhi, pivmin) > j) {
+      lo = blo;
+      hi = bhi;
+    }
+  }
   // j-th smallest eigenvalue: count(x) > j  <=>  lambda_j < x
   for (int it = 0; it < 128 && hi - lo > tol; ++it) {
     const double mid = 0.5 * (lo + hi);
     if (mid <= lo || mid >= hi) break;
-    if (sturm_count(d, e, n, mid, pivmin) > j)
+    if (sturm_count(d, e2, n, mid, pivmin) > j)
       hi = mid;
     else
       lo = mid;
@@ -562,18 +865,115 @@ cudaError_t reduce(const Sector* d_secs, int nsec, int maxn, double2* den, doubl
   return cudaLaunchKernelEx(&cfg, reduce_kernel, den, d_secs, d, e, tau, p, dots);
 }
 
+namespace {
+
+// dynamic shared memory of reduce_ds_kernel for sectors of at most n states:
+// the four vector slots and the packed lower columns of cluster rank 0 (the
+// most of any rank)
+size_t ds_smem_bytes(int n, int C) {
+  const int nq = (n + C - 1) / C;
+  return (size_t)(4LL * n + ds_col_off(nq, n, C, 0)) * sizeof(double2);
+}
+
+// dynamic shared memory one CTA of reduce_ds_kernel may use on this device
+size_t ds_smem_limit() {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, reduce_ds_kernel) != cudaSuccess) return 0;
+  return optin > (int)fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
+}
+
+}  // namespace
+
+int ds_cluster_size() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 8;
+  static int cached[64] = {0};
+  if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+  // 16 CTAs per cluster is beyond the portable size: used where the device
+  // can place such a cluster with the kernel's largest shared-memory use
+  int size = 8;
+  const size_t smem = ds_smem_limit();
+  if (smem > 0 &&
+      cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+      cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+          cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kClusterMax, 1, 1);
+    cfg.blockDim = dim3(kDsThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterMax;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, reduce_ds_kernel, &cfg) == cudaSuccess && nclusters >= 1)
+      size = kClusterMax;
+  }
+  cudaGetLastError();  // a refused query leaves no error behind
+  if (dev >= 0 && dev < 64) cached[dev] = size;
+  return size;
+}
+
+int ds_max_n() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  static int cached[64] = {0};
+  if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+  const int C = ds_cluster_size();
+  const size_t lim = ds_smem_limit();
+  int n = 0;
+  while (n < kMaxN && ds_smem_bytes(n + 1, C) <= lim) ++n;
+  cudaGetLastError();
+  if (dev >= 0 && dev < 64) cached[dev] = n;
+  return n;
+}
+
+cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, double2* den, double* d, double* e, double2* tau,
+                      cudaStream_t s) {
+  if (nsec <= 0) return cudaSuccess;
+  if (maxn > ds_max_n()) return cudaErrorInvalidValue;
+  const int C = ds_cluster_size();
+  const size_t smem = ds_smem_bytes(maxn, C);
+  cudaError_t e0 = cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e0 == cudaSuccess && C > 8)
+    e0 = cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e0 != cudaSuccess) return e0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nsec * C), 1, 1);
+  cfg.blockDim = dim3(kDsThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, reduce_ds_kernel, den, d_secs, d, e, tau);
+}
+
 cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, const double* e, double* w,
                    cudaStream_t s) {
   if (nsec <= 0) return cudaSuccess;
-  constexpr int kT = 64;
-  bisect_kernel<<<dim3((unsigned)((maxn + kT - 1) / kT), (unsigned)nsec), kT, 0, s>>>(d_secs, d, e, w);
+  constexpr int kT = 32;  // one warp per CTA: the counts of a large sector spread over many SMs
+  const size_t smem = (size_t)maxn * (2 * sizeof(double) + 2 * sizeof(float));
+  cudaError_t e0 = cudaFuncSetAttribute(bisect_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e0 != cudaSuccess) return e0;
+  bisect_kernel<<<dim3((unsigned)((maxn + kT - 1) / kT), (unsigned)nsec), kT, smem, s>>>(d_secs, d, e, w);
   return cudaGetLastError();
 }
 
 cudaError_t inverse_iteration(const Sector* d_secs, const InvItem* d_items, int nitems, int maxn, const double* d,
                               const double* e, const double* w, double* Z, double* lu, cudaStream_t s) {
   if (nitems <= 0) return cudaSuccess;
-  constexpr int kT = 64;
+  constexpr int kT = 32;
   inverse_iteration_kernel<<<(unsigned)((nitems + kT - 1) / kT), kT, 0, s>>>(d_secs, d_items, nitems, maxn, d, e,
                                                                             w, Z, lu);
   return cudaGetLastError();

@@ -7,8 +7,10 @@
 namespace hh {
 namespace tri {
 
-constexpr int kCluster = 8;        // CTAs of the thread-block cluster that reduces one sector
+constexpr int kCluster = 8;        // CTAs of the global-memory reduction's cluster (sectors above ds_max_n())
 constexpr int kReduceThreads = 256;
+constexpr int kClusterMax = 16;    // CTAs of the distributed-shared-memory reduction's cluster (at most)
+constexpr int kDsThreads = 512;    // threads of one CTA of that reduction
 constexpr int kMaxN = 4096;        // largest sector (shared memory holds two n-vectors)
 constexpr int kBtCols = 8;         // columns per CTA of the back-transformation (one warp each)
 
@@ -65,6 +67,13 @@ struct PhaseItem {
 // tau; p (n per sector) and dots (kCluster per sector) are scratch
 cudaError_t reduce(const Sector* d_secs, int nsec, int maxn, double2* den, double* d, double* e, double2* tau,
                    double2* p, double2* dots, cudaStream_t s);
+// the same reduction with each sector held in the distributed shared memory of
+// a cluster of ds_cluster_size() CTAs (16 where the device can place such a
+// cluster, else 8): sectors of at most ds_max_n() states, maxn the largest
+int ds_cluster_size();
+int ds_max_n();
+cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, double2* den, double* d, double* e, double2* tau,
+                      cudaStream_t s);
 // all eigenvalues of every T, ascending, by bisection
 cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, const double* e, double* w,
                    cudaStream_t s);
