@@ -234,22 +234,24 @@ __global__ void __launch_bounds__(kReduceThreads)
 // shared memory.  CTA r of the C-CTA cluster owns the columns j = r, r + C,
 // r + 2C, ... (cyclic, so the shrinking trailing block stays balanced) and
 // keeps only their lower parts, rows j .. n-1, packed one after another;
-// B(i, j) for i < j is conj(B(j, i)).  Per column k, three cluster barriers:
-//   (A) the owner of column k forms the reflector (d_k, e_k, tau_k, v) from
-//       its copy of the column, writes v to global memory (for the back-
-//       transformation) and to its vector slot;                  barrier 1
-//   (B) every CTA copies v from the owner and forms its partial B v from its
-//       own columns: rows i >= j of column j (row part) and the column's
-//       conjugate dot with v (column part);                       barrier 2
+// B(i, j) for i < j is conj(B(j, i)).  Column k, three cluster barriers:
+//   (B) every CTA copies v_k and tau_k from the column's owner and forms its
+//       partial B v from its own columns: rows i >= j of column j (row part)
+//       and the column's conjugate dot with v (column part);     barrier
 //   (C) reduce-scatter: CTA r sums the C partials of the rows i = r (mod C),
-//       scales them by tau and forms its share of p^H v;          barrier 3
+//       scales them by tau and forms its share of p^H v;          barrier
 //   (D) every CTA gathers p, forms w = p - (tau/2)(p^H v) v and applies
-//       B <- B - v w^H - w v^H to its own lower columns.
-// The vector slots sit at the front of the dynamic allocation, so at the same
-// offsets in every CTA, and are read remotely through mapa addresses.  A CTA
-// does about 8 m^2 / C FP64 FMAs per column (m = n - k - 1): with GB300's
-// FP64 pipe the kernel is FP64-bound above ~100 states and barrier-bound
-// below.
+//       B <- B - v w^H - w v^H to its own lower columns.  The owner of column
+//       k + 1 updates that column first and forms the next reflector
+//       (zlarfg: d, e, tau, v; v also to global memory for the back-
+//       transformation) while the other CTAs are still updating;   barrier
+// GB300's FP64 pipe issues one warp instruction per SM sub-partition every
+// 64 cycles or so, so the scalar chain between barriers (reductions, the
+// reflector's square root and divisions) is kept short: shuffle trees, two
+// divisions per reflector, and the next reflector overlapped with the
+// update.  The vector slots sit at the front of the dynamic allocation, so at
+// the same offsets in every CTA, and are read remotely through mapa
+// addresses; v and tau are double-buffered by column parity.
 __host__ __device__ __forceinline__ long long ds_col_off(int q, int n, int C, int r) {
   // packed offset of owned column q (column q C + r): sum over q' < q of n - (q' C + r)
   return (long long)q * (n - r) - (long long)C * q * (q - 1) / 2;
@@ -281,6 +283,76 @@ __device__ __forceinline__ int cluster_nctas() {
   return (int)r;
 }
 
+// Cluster barrier of the distributed-shared-memory kernel: its shared-memory
+// writes before it are visible to the whole cluster after it.  The global
+// writes (d, e, tau, reflectors) are read only by later kernels, so no
+// GPU-scope fence.
+__device__ __forceinline__ void ds_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
+// Sum over a kDsThreads CTA, received by every thread: two shuffle trees.
+__device__ __forceinline__ double ds_block_sum(double v, double* scratch) {
+  static_assert(kDsThreads / 32 <= 32, "one warp sums the warp partials");
+  v = warp_sum(v);
+  __syncthreads();  // scratch is free
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  return warp_sum(lane < kDsThreads / 32 ? scratch[lane] : 0.0);
+}
+
+// Reflector of column k (zlarfg) from x[i - k] = B(i, k), i >= k, by every
+// thread of the owning CTA: H = I - tau v v^H with H^H x = beta e_1, v_{k+1} = 1.
+__device__ __forceinline__ void ds_reflector(int k, int n, const double2* x, double2* vb, double2* tau_slot,
+                                             double* scratch, double2* A, const Sector& S, double* dvec,
+                                             double* evec, double2* tauv) {
+  const int t = threadIdx.x;
+  double xn = 0.0;
+  for (int i = k + 2 + t; i < n; i += kDsThreads) {
+    const double2 xi = x[i - k];
+    xn = fma(xi.x, xi.x, fma(xi.y, xi.y, xn));
+  }
+  xn = ds_block_sum(xn, scratch);
+  const double2 alpha = x[1];
+  double2 tau = make_double2(0.0, 0.0), scale = make_double2(0.0, 0.0);
+  double beta = alpha.x;
+  if (xn > 0.0 || alpha.y != 0.0) {
+    beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn))), alpha.x);
+    const double ib = 1.0 / beta;
+    tau = make_double2((beta - alpha.x) * ib, -alpha.y * ib);
+    const double dr = alpha.x - beta, di = alpha.y;  // scale = 1 / (alpha - beta)
+    const double ir2 = 1.0 / fma(dr, dr, di * di);
+    scale = make_double2(dr * ir2, -di * ir2);
+  }
+  if (t == 0) {
+    dvec[S.toff + k] = x[0].x;
+    evec[S.toff + k] = beta;
+    tauv[S.toff + k] = tau;
+    *tau_slot = tau;
+  }
+  double2* Ak = A + (long long)k * n;
+  for (int i = k + 1 + t; i < n; i += kDsThreads) {
+    const double2 vi = i == k + 1 ? make_double2(1.0, 0.0) : cmul(x[i - k], scale);
+    vb[i] = vi;
+    Ak[i] = vi;
+  }
+}
+
 __global__ void __launch_bounds__(kDsThreads, 1)
     reduce_ds_kernel(double2* __restrict__ den, const Sector* __restrict__ secs, double* __restrict__ dvec,
                      double* __restrict__ evec, double2* __restrict__ tauv) {
@@ -291,13 +363,13 @@ __global__ void __launch_bounds__(kDsThreads, 1)
   const int n = S.n;
   double2* A = den + S.aoff;
   extern __shared__ double2 sm[];
-  double2* vb = sm;           // v, indexed by row (rows k+1 .. n-1)
-  double2* wb = sm + n;       // p, then w
-  double2* pp = sm + 2 * n;   // this CTA's partial B v
-  double2* ps = sm + 3 * n;   // tau (B v) of the rows i = r (mod C), summed over the cluster
-  double2* col = sm + 4 * n;  // the owned lower columns
-  __shared__ double2 s_tau, s_dot, s_dots[kClusterMax];
-  __shared__ double red_d[32];
+  double2* vbuf = sm;         // 2 n: v of the even / odd columns, indexed by row
+  double2* wb = sm + 2 * n;   // p, then w
+  double2* pp = sm + 3 * n;   // this CTA's partial B v
+  double2* ps = sm + 4 * n;   // tau (B v) of the rows i = r (mod C), summed over the cluster
+  double2* col = sm + 5 * n;  // the owned lower columns
+  __shared__ double2 s_tau[2], s_dot, s_a2;
+  __shared__ double red_d[kWarps];
   __shared__ double2 red_c[kWarps];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int nq = n > r ? (n - r + C - 1) / C : 0;
@@ -307,48 +379,27 @@ __global__ void __launch_bounds__(kDsThreads, 1)
     for (int i = j + t; i < n; i += kDsThreads) col[o + (i - j)] = A[(long long)j * n + i];
   }
   __syncthreads();
+  if (r == 0) {  // column 0
+    if (n > 1) {
+      ds_reflector(0, n, col, vbuf, &s_tau[0], red_d, A, S, dvec, evec, tauv);
+    } else if (t == 0) {
+      dvec[S.toff] = col[0].x;
+      evec[S.toff] = 0.0;
+      tauv[S.toff] = make_double2(0.0, 0.0);
+    }
+  }
+  ds_sync();
   for (int k = 0; k + 1 < n; ++k) {
     const int owner = k % C;
-    // ---- (A) reflector of column k (zlarfg)
-    if (owner == r) {
-      const double2* x = col + ds_col_off(k / C, n, C, r);  // x[i - k] = B(i, k), i >= k
-      double xn = 0.0;
-      for (int i = k + 2 + t; i < n; i += kDsThreads) {
-        const double2 xi = x[i - k];
-        xn += xi.x * xi.x + xi.y * xi.y;
-      }
-      xn = block_sum(xn, red_d);
-      const double2 alpha = x[1];
-      double2 tau = make_double2(0.0, 0.0), scale = make_double2(0.0, 0.0);
-      double beta = alpha.x;
-      if (xn > 0.0 || alpha.y != 0.0) {
-        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn), alpha.x);
-        tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
-        const double2 den_ = make_double2(alpha.x - beta, alpha.y);  // 1 / (alpha - beta)
-        const double r2 = den_.x * den_.x + den_.y * den_.y;
-        scale = make_double2(den_.x / r2, -den_.y / r2);
-      }
-      if (t == 0) {
-        dvec[S.toff + k] = x[0].x;
-        evec[S.toff + k] = beta;
-        tauv[S.toff + k] = tau;
-        s_tau = tau;
-      }
-      for (int i = k + 1 + t; i < n; i += kDsThreads) {
-        const double2 vi = i == k + 1 ? make_double2(1.0, 0.0) : cmul(x[i - k], scale);
-        vb[i] = vi;
-        A[(long long)k * n + i] = vi;
-      }
-    }
-    cluster_barrier();  // 1: the owner's v and tau are complete
-    // ---- (B) v from the owner, then this CTA's partial B v
+    double2* vb = vbuf + (k & 1) * n;
+    // ---- (B) v and tau from the owner, then this CTA's partial B v
     double2 tau;
     if (owner != r) {
       const uint32_t rv = ds_map(vb, owner);
       for (int i = k + 1 + t; i < n; i += kDsThreads) vb[i] = ds_ld2(rv + (uint32_t)(i * sizeof(double2)));
-      tau = ds_ld2(ds_map(&s_tau, owner));
+      tau = ds_ld2(ds_map(&s_tau[k & 1], owner));
     } else {
-      tau = s_tau;
+      tau = s_tau[k & 1];
     }
     __syncthreads();
     const int qlo = k + 1 > r ? (k + 1 - r + C - 1) / C : 0;  // first owned column > k
@@ -369,13 +420,10 @@ __global__ void __launch_bounds__(kDsThreads, 1)
       const long long o = ds_col_off(q, n, C, r);
       double2 sum = make_double2(0.0, 0.0);
       for (int i = j + 1 + lane; i < n; i += 32) sum = cfmac(col[o + (i - j)], vb[i], sum);
-      for (int sh = 16; sh > 0; sh >>= 1) {
-        sum.x += __shfl_xor_sync(0xffffffffu, sum.x, sh);
-        sum.y += __shfl_xor_sync(0xffffffffu, sum.y, sh);
-      }
+      sum = warp_sum2(sum);
       if (lane == 0) pp[j] = cadd(pp[j], sum);
     }
-    cluster_barrier();  // 2: every CTA's partial is complete
+    ds_sync();  // every CTA's partial is complete
     // ---- (C) reduce-scatter of the rows i = r (mod C) and this CTA's share of p^H v
     {
       const int i0 = k + 1 + ((r - (k + 1)) % C + C) % C;  // first row > k with i = r (mod C)
@@ -397,112 +445,147 @@ __global__ void __launch_bounds__(kDsThreads, 1)
           dot = cfmac(p, vb[i], dot);  // conj(p_i) v_i
         }
       }
-      for (int sh = 16; sh > 0; sh >>= 1) {
-        dot.x += __shfl_xor_sync(0xffffffffu, dot.x, sh);
-        dot.y += __shfl_xor_sync(0xffffffffu, dot.y, sh);
-      }
-      if (lane == 0) red_c[warp] = dot;
-      __syncthreads();
-      if (t == 0) {
-        double2 sd = make_double2(0.0, 0.0);
-        for (int w = 0; w < kWarps; ++w) sd = cadd(sd, red_c[w]);
-        s_dot = sd;
+      if (nr > 0) {  // uniform over the CTA
+        dot = warp_sum2(dot);
+        if (lane == 0) red_c[warp] = dot;
+        __syncthreads();
+        if (warp == 0) {
+          double2 sd = warp_sum2(lane < kWarps ? red_c[lane] : make_double2(0.0, 0.0));
+          if (lane == 0) s_dot = sd;
+        }
+      } else if (t == 0) {
+        s_dot = make_double2(0.0, 0.0);
       }
     }
-    cluster_barrier();  // 3: p and the partial dots are complete
-    // ---- (D) w = p + a2 v with a2 = -(tau/2) (p^H v); rank-2 update of the owned columns
-    if (t < C) s_dots[t] = ds_ld2(ds_map(&s_dot, t));
+    ds_sync();  // p and the partial dots are complete
+    // ---- (D) w = p + a2 v with a2 = -(tau/2) (p^H v); rank-2 update; next reflector
+    if (warp == 0) {
+      const double2 sd = warp_sum2(lane < C ? ds_ld2(ds_map(&s_dot, lane)) : make_double2(0.0, 0.0));
+      if (lane == 0) s_a2 = cmul(make_double2(-0.5 * tau.x, -0.5 * tau.y), sd);
+    }
     for (int i = k + 1 + t; i < n; i += kDsThreads) wb[i] = ds_ld2(ds_map(ps + i, i % C));
     __syncthreads();
     {
-      double2 sdot = make_double2(0.0, 0.0);
-      for (int c = 0; c < C; ++c) sdot = cadd(sdot, s_dots[c]);
-      const double2 a2 = cmul(make_double2(-0.5 * tau.x, -0.5 * tau.y), sdot);
+      const double2 a2 = s_a2;
       for (int i = k + 1 + t; i < n; i += kDsThreads) wb[i] = cfma(a2, vb[i], wb[i]);
     }
     __syncthreads();
+    const int nx = k + 1;  // the next column
+    const bool own_next = nx % C == r;
+    if (own_next) {
+      // column nx first (rows nx .. n-1), then its reflector or, for the last
+      // column, its diagonal
+      const long long o = ds_col_off(nx / C, n, C, r);
+      const double2 vj = vb[nx], wj = wb[nx];
+      for (int i = nx + t; i < n; i += kDsThreads) col[o + (i - nx)] = rank2(col[o + (i - nx)], vb[i], wb[i], vj, wj);
+      __syncthreads();
+      if (nx + 1 < n) {
+        ds_reflector(nx, n, col + o, vbuf + (nx & 1) * n, &s_tau[nx & 1], red_d, A, S, dvec, evec, tauv);
+      } else if (t == 0) {
+        dvec[S.toff + nx] = col[o].x;
+        evec[S.toff + nx] = 0.0;
+        tauv[S.toff + nx] = make_double2(0.0, 0.0);
+      }
+    }
     for (int i = k + 1 + t; i < n; i += kDsThreads) {
       const double2 vi = vb[i], wi = wb[i];
       long long o = olo;
       for (int j = qlo * C + r; j <= i; j += C) {
-        col[o + (i - j)] = rank2(col[o + (i - j)], vi, wi, vb[j], wb[j]);
+        if (j != nx || !own_next) col[o + (i - j)] = rank2(col[o + (i - j)], vi, wi, vb[j], wb[j]);
         o += n - j;
       }
     }
-    __syncthreads();  // the owner of column k + 1 reads its updated column next
+    ds_sync();  // the next v is posted and every column is updated
   }
-  if (n > 0 && (n - 1) % C == r && t == 0) {
-    dvec[S.toff + n - 1] = col[ds_col_off((n - 1) / C, n, C, r)].x;
-    evec[S.toff + n - 1] = 0.0;
-    tauv[S.toff + n - 1] = make_double2(0.0, 0.0);
-  }
-  cluster_barrier();  // no CTA leaves while another may still read its shared memory
 }
 
 // ---------------------------------------------------------------- bisect
 // Number of eigenvalues of T (d, e) below x: the negative pivots q_i of the
-// LDL^T factorisation of T - x I, a pivot smaller than pivmin replaced by
-// -pivmin (the Sturm count of dstebz).  The FP64 count runs on the leading
-// principal minors p_{i+1} = (d_i - x) p_i - e_{i-1}^2 p_{i-1} (q_i =
-// p_{i+1} / p_i, so a negative pivot is a sign change) without the division
-// per step, which costs GB300's FP64 pipe several operations; the pair of
-// minors is rescaled by powers of two to stay in range, and a minor below
-// pivmin times the previous one stands for the pivot -pivmin.  e2 holds e^2.
-__device__ __forceinline__ int sturm_count(const double* d, const double* e2, int n, double x, double pivmin) {
+// LDL^T factorisation of T - x I (the Sturm count of dstebz).  The FP64 count
+// runs on the leading principal minors p_{i+1} = (d_i - x) p_i - e_{i-1}^2
+// p_{i-1} (q_i = p_{i+1} / p_i: a negative pivot is a sign change), three
+// FP64 operations per step and no division; signs, exponents and the
+// rescaling of the pair by powers of two are integer operations on the bit
+// patterns, so they stay off GB300's slow FP64 pipe.  A pivot below 2^-200 in
+// magnitude counts as -2^-200 (dstebz uses -pivmin; either way the next pivot
+// is huge and positive and the count is the same).  e2 holds e^2; the minors
+// stay in [2^-600, 2^500] between rescalings.
+__device__ __forceinline__ int sturm_count(const double* d, const double* e2, int n, double x) {
+  constexpr long long kSign = (long long)0x8000000000000000ull;
   double pm = 1.0, p = d[0] - x;
-  if (fabs(p) < pivmin) p = -pivmin;
-  int c = p < 0.0;
+  long long bp = __double_as_longlong(p);
+  int ep = (int)((bp >> 52) & 0x7ff);
+  if (ep < 1023 - 200) {  // |p| < 2^-200 (zero included): the pivot -2^-200
+    p = -0x1p-200;
+    bp = __double_as_longlong(p);
+    ep = 1023 - 200;
+  }
+  int c = (int)((unsigned long long)bp >> 63);
   for (int i = 1; i < n; ++i) {
     double pn = fma(d[i] - x, p, -e2[i - 1] * pm);
-    const double ap = fabs(p);
-    if (fabs(pn) < pivmin * ap) pn = p < 0.0 ? pivmin * ap : -pivmin * ap;
-    c += (pn < 0.0) != (p < 0.0);
+    long long bn = __double_as_longlong(pn);
+    int en = (int)((bn >> 52) & 0x7ff);
+    if (en + 200 < ep) {  // tiny pivot: -sign(p) 2^(exp(p) - 200)
+      bn = ((bp ^ kSign) & kSign) | ((long long)(ep - 200) << 52);
+      pn = __longlong_as_double(bn);
+      en = ep - 200;
+    }
+    c += (int)((unsigned long long)(bn ^ bp) >> 63);
     pm = p;
     p = pn;
-    const double a = fabs(p);
-    if (a > 0x1p+400 || a < 0x1p-400) {
-      int ex;
-      frexp(a, &ex);
-      p = ldexp(p, -ex);
-      pm = ldexp(pm, -ex);
+    bp = bn;
+    ep = en;
+    if (ep > 1023 + 400 || ep < 1023 - 400) {  // rescale the pair by 2^-(ep - 1023): |p| into [1, 2)
+      const double f = __longlong_as_double((long long)(2046 - ep) << 52);
+      p *= f;
+      pm *= f;
+      bp = __double_as_longlong(p);
+      ep = 1023;
     }
   }
   return c;
 }
 
 // The pivot count in FP32 on T scaled by a power of two (d32 = s d, e32 =
-// (s e)^2, s ||T|| in [1/2, 1)).
-__device__ __forceinline__ int sturm_count32(const float* d, const float* e2, int n, float x, float pivmin) {
+// (s e)^2, s ||T|| in [1/2, 1)), pivots below 16 FLT_MIN counted as negative.
+__device__ __forceinline__ int sturm_count32(const float* d, const float* e2, int n, float x) {
+  constexpr float kPiv = 16.0f * FLT_MIN;
   float q = d[0] - x;
-  if (fabsf(q) < pivmin) q = -pivmin;
+  if (fabsf(q) < kPiv) q = -kPiv;
   int c = q < 0.0f;
   for (int i = 1; i < n; ++i) {
     q = (d[i] - x) - e2[i - 1] / q;
-    if (fabsf(q) < pivmin) q = -pivmin;
+    if (fabsf(q) < kPiv) q = -kPiv;
     c += q < 0.0f;
   }
   return c;
 }
 
-// One warp per CTA, blockIdx.y = sector, thread = eigenvalue index j: T is
-// staged in shared memory in FP64 and, scaled, in FP32.  The FP32 bisection
-// brackets lambda_j to a few FP32 eps ||T||; the bracket, widened by
-// 16 FP32 eps ||T|| (beyond the FP32 count's backward error), is kept when
-// FP64 counts confirm it, else the Gershgorin interval is used; FP64
-// bisection then closes it to 2 eps ||T|| + 4 pivmin.
-__global__ void bisect_kernel(const Sector* __restrict__ secs, const double* __restrict__ dvec,
-                              const double* __restrict__ evec, double* __restrict__ w) {
+constexpr int kBisectWarps = 4;  // eigenvalues per CTA, one warp each
+
+// Every eigenvalue of every T, ascending: one warp per eigenvalue j, whose 32
+// lanes count at 32 interior points of the current bracket at once (a
+// 33-section: five bits per round).  T is staged in shared memory in FP64
+// and, scaled by a power of two, in FP32.  The FP32 rounds bracket lambda_j
+// to a few FP32 eps ||T||; the bracket, widened by 16 FP32 eps ||T|| (beyond
+// the FP32 count's backward error), is kept when two FP64 counts confirm it,
+// else the Gershgorin interval is used; FP64 rounds then close it to
+// 2 eps ||T|| + 4 DBL_MIN.
+__global__ void __launch_bounds__(kBisectWarps * 32)
+    bisect_kernel(const Sector* __restrict__ secs, const double* __restrict__ dvec,
+                  const double* __restrict__ evec, double* __restrict__ w) {
   const Sector S = secs[blockIdx.y];
   const int n = S.n;
-  if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole CTA is beyond this sector
+  if ((int)blockIdx.x * kBisectWarps >= n) return;  // the whole CTA is beyond this sector
   extern __shared__ double sh[];
   double* d = sh;                                      // n
   double* e2 = sh + n;                                 // n: e_i^2
   float* d32 = reinterpret_cast<float*>(sh + 2 * n);   // n
   float* e32 = d32 + n;                                // n: (s e_i)^2
-  const int lane = threadIdx.x;                        // blockDim.x == 32
+  __shared__ double s_red[3][kBisectWarps];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   double lo = 1e300, hi = -1e300, emax2 = 0.0;
-  for (int i = lane; i < n; i += 32) {
+  for (int i = t; i < n; i += kBisectWarps * 32) {
     const double di = dvec[S.toff + i];
     const double ei = i + 1 < n ? evec[S.toff + i] : 0.0;
     const double em = i > 0 ? evec[S.toff + i - 1] : 0.0;
@@ -518,50 +601,77 @@ __global__ void bisect_kernel(const Sector* __restrict__ secs, const double* __r
     hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
     emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
   }
+  if (lane == 0) {
+    s_red[0][warp] = lo;
+    s_red[1][warp] = hi;
+    s_red[2][warp] = emax2;
+  }
+  __syncthreads();
+  for (int q = 0; q < kBisectWarps; ++q) {
+    lo = fmin(lo, s_red[0][q]);
+    hi = fmax(hi, s_red[1][q]);
+  }
   const double tnorm = fmax(fabs(lo), fabs(hi));
-  const double pivmin = DBL_MIN * fmax(1.0, emax2);
-  const double tol = 2.0 * DBL_EPSILON * tnorm + 4.0 * pivmin;
+  const double tol = 2.0 * DBL_EPSILON * tnorm + 4.0 * DBL_MIN;
   int ex = 0;
   frexp(tnorm > 0.0 ? tnorm : 1.0, &ex);
-  const double sc = ldexp(1.0, -ex);
-  for (int i = lane; i < n; i += 32) {
+  const double sc = ldexp(1.0, -ex);  // s ||T|| in [1/2, 1)
+  for (int i = t; i < n; i += kBisectWarps * 32) {
     d32[i] = (float)(sc * d[i]);
     const double es = sc * sqrt(e2[i]);
     e32[i] = (float)(es * es);
   }
-  __syncwarp();
-  const int j = blockIdx.x * blockDim.x + lane;
-  if (j >= n) return;
+  __syncthreads();
+  const int j = blockIdx.x * kBisectWarps + warp;
+  if (j >= n) return;  // whole warps only
   lo -= tol;
   hi += tol;
-  {
-    float l32 = (float)(sc * lo), h32 = (float)(sc * hi);
-    const float tol32 = 4.0f * FLT_EPSILON, piv32 = 16.0f * FLT_MIN;
-    for (int it = 0; it < 64 && h32 - l32 > tol32; ++it) {
-      const float mid = 0.5f * (l32 + h32);
-      if (mid <= l32 || mid >= h32) break;
-      if (sturm_count32(d32, e32, n, mid, piv32) > j)
-        h32 = mid;
-      else
-        l32 = mid;
+  // FP32 rounds on the scaled matrix
+  float l32 = (float)(sc * lo), h32 = (float)(sc * hi);
+  for (int it = 0; it < 12 && h32 - l32 > 4.0f * FLT_EPSILON; ++it) {
+    const float x = l32 + (h32 - l32) * (float)(lane + 1) * (1.0f / 33.0f);
+    const unsigned above = __ballot_sync(0xffffffffu, x > l32 && x < h32 && sturm_count32(d32, e32, n, x) > j);
+    // the first point above lambda_j bounds it from above, the point before from below
+    float nl = l32, nh = h32;
+    if (above) {
+      const int f = __ffs(above) - 1;
+      nh = __shfl_sync(0xffffffffu, x, f);
+      if (f > 0) nl = __shfl_sync(0xffffffffu, x, f - 1);
+    } else {
+      nl = __shfl_sync(0xffffffffu, x, 31);
     }
+    if (nl == l32 && nh == h32) break;
+    l32 = nl;
+    h32 = nh;
+  }
+  {
     const double widen = 16.0 * FLT_EPSILON;
     const double blo = fmax(lo, ((double)l32 - widen) / sc), bhi = fmin(hi, ((double)h32 + widen) / sc);
-    if (blo < bhi && sturm_count(d, e2, n, blo, pivmin) <= j && sturm_count(d, e2, n, bhi, pivmin) > j) {
+    // lanes 0 and 1 confirm the bracket with FP64 counts
+    const int cnt = lane < 2 && blo < bhi ? sturm_count(d, e2, n, lane == 0 ? blo : bhi) : 0;
+    const int c0 = __shfl_sync(0xffffffffu, cnt, 0), c1 = __shfl_sync(0xffffffffu, cnt, 1);
+    if (blo < bhi && c0 <= j && c1 > j) {
       lo = blo;
       hi = bhi;
     }
   }
-  // j-th smallest eigenvalue: count(x) > j  <=>  lambda_j < x
-  for (int it = 0; it < 128 && hi - lo > tol; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (sturm_count(d, e2, n, mid, pivmin) > j)
-      hi = mid;
-    else
-      lo = mid;
+  // FP64 rounds: count(x) > j  <=>  lambda_j < x
+  for (int it = 0; it < 24 && hi - lo > tol; ++it) {
+    const double x = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 33.0);
+    const unsigned above = __ballot_sync(0xffffffffu, x > lo && x < hi && sturm_count(d, e2, n, x) > j);
+    double nl = lo, nh = hi;
+    if (above) {
+      const int f = __ffs(above) - 1;
+      nh = __shfl_sync(0xffffffffu, x, f);
+      if (f > 0) nl = __shfl_sync(0xffffffffu, x, f - 1);
+    } else {
+      nl = __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (nl == lo && nh == hi) break;
+    lo = nl;
+    hi = nh;
   }
-  w[S.woff + j] = 0.5 * (lo + hi);
+  if (lane == 0) w[S.woff + j] = 0.5 * (lo + hi);
 }
 
 // ------------------------------------------------------ inverse iteration
@@ -575,7 +685,9 @@ __device__ __forceinline__ double start_value(unsigned long long a, unsigned lon
 
 // Eigenvector of T for lambda_j: Gaussian elimination with partial pivoting
 // of M = T - lambda I (row i of M has e_{i-1}, d_i - lambda, e_i), kept as
-// the rows (u0, u1, u2) of U, the multipliers and the row swaps; then three
+// the rows (1 / u0, u1, u2) of U (the pivot's reciprocal, so that the solves
+// multiply: an FP64 division costs GB300 several FP64-pipe operations), the
+// multipliers and the row swaps; then three
 // solves M x_{t+1} = x_t from a pseudo-random x_0, normalised each time.
 // Pivots below eps ||T|| are raised to eps ||T|| (the exact-eigenvalue case).
 __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const InvItem* __restrict__ items,
@@ -609,8 +721,9 @@ __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const 
     const double s = e[i], tt = d[i + 1] - lam, r = i + 2 < n ? e[i + 1] : 0.0;
     if (fabs(u0) >= fabs(s)) {  // keep row i as the pivot row
       u0 = guard(u0);
-      const double mult = s / u0;
-      U0[i * stride] = u0;
+      const double inv = 1.0 / u0;
+      const double mult = s * inv;
+      U0[i * stride] = inv;
       U1[i * stride] = u1;
       U2[i * stride] = 0.0;
       ML[i * stride] = mult;
@@ -618,8 +731,9 @@ __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const 
       u0 = tt - mult * u1;
       u1 = r;
     } else {  // row i + 1 is the pivot row
-      const double mult = u0 / s;
-      U0[i * stride] = s;
+      const double inv = 1.0 / s;
+      const double mult = u0 * inv;
+      U0[i * stride] = inv;
       U1[i * stride] = tt;
       U2[i * stride] = r;
       ML[i * stride] = mult;
@@ -629,7 +743,7 @@ __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const 
       u0 = nu0;
     }
   }
-  U0[(long long)(n - 1) * stride] = guard(u0);
+  U0[(long long)(n - 1) * stride] = 1.0 / guard(u0);
   U1[(long long)(n - 1) * stride] = 0.0;
   U2[(long long)(n - 1) * stride] = 0.0;
   for (int i = 0; i < n; ++i) x[i * ldz] = start_value(((unsigned long long)I.sec << 32) + (unsigned)I.j, i);
@@ -651,7 +765,7 @@ __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const 
     // back substitution with U
     double x1 = 0.0, x2 = 0.0, nrm = 0.0;  // x_{i+1}, x_{i+2}
     for (int i = n - 1; i >= 0; --i) {
-      const double xi = (x[i * ldz] - U1[i * stride] * x1 - U2[i * stride] * x2) / U0[i * stride];
+      const double xi = (x[i * ldz] - U1[i * stride] * x1 - U2[i * stride] * x2) * U0[i * stride];
       x[i * ldz] = xi;
       x2 = x1;
       x1 = xi;
@@ -868,11 +982,11 @@ cudaError_t reduce(const Sector* d_secs, int nsec, int maxn, double2* den, doubl
 namespace {
 
 // dynamic shared memory of reduce_ds_kernel for sectors of at most n states:
-// the four vector slots and the packed lower columns of cluster rank 0 (the
+// the five vector slots and the packed lower columns of cluster rank 0 (the
 // most of any rank)
 size_t ds_smem_bytes(int n, int C) {
   const int nq = (n + C - 1) / C;
-  return (size_t)(4LL * n + ds_col_off(nq, n, C, 0)) * sizeof(double2);
+  return (size_t)(5LL * n + ds_col_off(nq, n, C, 0)) * sizeof(double2);
 }
 
 // dynamic shared memory one CTA of reduce_ds_kernel may use on this device
@@ -962,11 +1076,11 @@ cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, double2* den, do
 cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, const double* e, double* w,
                    cudaStream_t s) {
   if (nsec <= 0) return cudaSuccess;
-  constexpr int kT = 32;  // one warp per CTA: the counts of a large sector spread over many SMs
   const size_t smem = (size_t)maxn * (2 * sizeof(double) + 2 * sizeof(float));
   cudaError_t e0 = cudaFuncSetAttribute(bisect_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e0 != cudaSuccess) return e0;
-  bisect_kernel<<<dim3((unsigned)((maxn + kT - 1) / kT), (unsigned)nsec), kT, smem, s>>>(d_secs, d, e, w);
+  bisect_kernel<<<dim3((unsigned)((maxn + kBisectWarps - 1) / kBisectWarps), (unsigned)nsec), kBisectWarps * 32,
+                  smem, s>>>(d_secs, d, e, w);
   return cudaGetLastError();
 }
 
