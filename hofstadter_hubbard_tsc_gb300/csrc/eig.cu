@@ -80,6 +80,8 @@ struct EigState {
   void* d_buf3 = nullptr;              // eig_vectors
   size_t cap3 = 0;
   bool smem_set = false;
+  cudaStream_t side = nullptr;         // the larger sectors' reduction beside the smaller ones'
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   TriRun run;
 };
 
@@ -318,6 +320,9 @@ void release_step_resources(hh_ctx* ctx) {
     if (s->join[i]) cudaEventDestroy(s->join[i]);
   }
   if (s->fork) cudaEventDestroy(s->fork);
+  if (s->side) cudaStreamDestroy(s->side);
+  if (s->side_fork) cudaEventDestroy(s->side_fork);
+  if (s->side_join) cudaEventDestroy(s->side_join);
   dev_free(ctx, s->d_buf);
   dev_free(ctx, s->d_buf2);
   dev_free(ctx, s->d_buf3);
@@ -543,14 +548,37 @@ int eig_values(hh_ctx* ctx, double2* A, const std::vector<long long>& offs, cons
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_check(ctx, e, "Jacobi eigensolver launch");
   }
-  // sectors that fit a cluster's shared memory are reduced there; the few
-  // larger ones (first in the list) by the global-memory kernel
-  const int ds_max = tri::ds_max_n();
-  int nglob = 0;
-  while (nglob < ntri && R.secs[nglob].n > ds_max) ++nglob;
-  if (nglob > 0) e = tri::reduce(R.d_secs, nglob, maxn, A, R.d_d, R.d_e, R.d_tau, d_p, d_dots, s);
-  if (e == cudaSuccess && nglob < ntri)
-    e = tri::reduce_ds(R.d_secs + nglob, ntri - nglob, R.secs[nglob].n, A, R.d_d, R.d_e, R.d_tau, s);
+  // three groups of sectors, largest first in the list: beyond the cluster
+  // kernel's vector slots (the row-split kernel, rare), lower columns in place
+  // in global memory, lower columns in the cluster's shared memory.  The
+  // larger groups run on a side stream beside the shared-memory group.
+  const int max_g = tri::ds_max_n(true), max_s = tri::ds_max_n(false);
+  int n_old = 0, n_glob = 0;
+  while (n_old < ntri && R.secs[n_old].n > max_g) ++n_old;
+  while (n_old + n_glob < ntri && R.secs[n_old + n_glob].n > max_s) ++n_glob;
+  const int n_smem = ntri - n_old - n_glob;
+  const bool fork = n_smem > 0 && n_old + n_glob > 0;
+  cudaStream_t big = s;
+  if (fork) {
+    if (!S->side) {
+      if (cudaStreamCreateWithFlags(&S->side, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&S->side_fork, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&S->side_join, cudaEventDisableTiming) != cudaSuccess)
+        return fail(ctx, HH_ERR_CUDA, "eigensolver side stream");
+    }
+    big = S->side;
+    e = cudaEventRecord(S->side_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(big, S->side_fork, 0);
+  }
+  if (e == cudaSuccess && n_old > 0)
+    e = tri::reduce(R.d_secs, n_old, maxn, A, R.d_d, R.d_e, R.d_tau, d_p, d_dots, big);
+  if (e == cudaSuccess && n_glob > 0)
+    e = tri::reduce_ds(R.d_secs + n_old, n_glob, R.secs[n_old].n, true, A, R.d_d, R.d_e, R.d_tau, big);
+  if (e == cudaSuccess && fork) e = cudaEventRecord(S->side_join, big);
+  if (e == cudaSuccess && n_smem > 0)
+    e = tri::reduce_ds(R.d_secs + n_old + n_glob, n_smem, R.secs[n_old + n_glob].n, false, A, R.d_d, R.d_e,
+                       R.d_tau, s);
+  if (e == cudaSuccess && fork) e = cudaStreamWaitEvent(s, S->side_join, 0);
   if (e != cudaSuccess) return cuda_check(ctx, e, "tridiagonal reduction");
   e = tri::bisect(R.d_secs, ntri, maxn, R.d_d, R.d_e, R.d_w, s);
   if (e != cudaSuccess) return cuda_check(ctx, e, "bisection");

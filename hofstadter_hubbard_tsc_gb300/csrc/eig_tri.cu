@@ -316,35 +316,50 @@ __device__ __forceinline__ double ds_block_sum(double v, double* scratch) {
   return warp_sum(lane < kDsThreads / 32 ? scratch[lane] : 0.0);
 }
 
-// Reflector of column k (zlarfg) from x[i - k] = B(i, k), i >= k, by every
-// thread of the owning CTA: H = I - tau v v^H with H^H x = beta e_1, v_{k+1} = 1.
+// Reflector of column k (zlarfg) from x[i - k] = B(i, k), i >= k, by the
+// owning CTA: H = I - tau v v^H with H^H x = beta e_1, v_{k+1} = 1.  Only
+// warps holding elements take part in the norm's first tree and warp 0 alone
+// forms the scalars (square root, two divisions): an FP64 warp instruction
+// costs GB300 the same whatever the number of active lanes, so redundant
+// copies in idle warps would cost as much as real work.  sc holds the scale
+// for the other warps.
 __device__ __forceinline__ void ds_reflector(int k, int n, const double2* x, double2* vb, double2* tau_slot,
-                                             double* scratch, double2* A, const Sector& S, double* dvec,
-                                             double* evec, double2* tauv) {
-  const int t = threadIdx.x;
+                                             double2* sc, double* scratch, double2* A, const Sector& S,
+                                             double* dvec, double* evec, double2* tauv) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   double xn = 0.0;
-  for (int i = k + 2 + t; i < n; i += kDsThreads) {
-    const double2 xi = x[i - k];
-    xn = fma(xi.x, xi.x, fma(xi.y, xi.y, xn));
+  if (warp * 32 < n - (k + 2)) {  // warps holding elements of x_2: (uniform per warp)
+    for (int i = k + 2 + t; i < n; i += kDsThreads) {
+      const double2 xi = x[i - k];
+      xn = fma(xi.x, xi.x, fma(xi.y, xi.y, xn));
+    }
+    xn = warp_sum(xn);
   }
-  xn = ds_block_sum(xn, scratch);
-  const double2 alpha = x[1];
-  double2 tau = make_double2(0.0, 0.0), scale = make_double2(0.0, 0.0);
-  double beta = alpha.x;
-  if (xn > 0.0 || alpha.y != 0.0) {
-    beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn))), alpha.x);
-    const double ib = 1.0 / beta;
-    tau = make_double2((beta - alpha.x) * ib, -alpha.y * ib);
-    const double dr = alpha.x - beta, di = alpha.y;  // scale = 1 / (alpha - beta)
-    const double ir2 = 1.0 / fma(dr, dr, di * di);
-    scale = make_double2(dr * ir2, -di * ir2);
+  if (lane == 0) scratch[warp] = xn;
+  __syncthreads();
+  if (warp == 0) {
+    xn = warp_sum(lane < kDsThreads / 32 ? scratch[lane] : 0.0);
+    const double2 alpha = x[1];
+    double2 tau = make_double2(0.0, 0.0), scale = make_double2(0.0, 0.0);
+    double beta = alpha.x;
+    if (xn > 0.0 || alpha.y != 0.0) {
+      beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, xn))), alpha.x);
+      const double ib = 1.0 / beta;
+      tau = make_double2((beta - alpha.x) * ib, -alpha.y * ib);
+      const double dr = alpha.x - beta, di = alpha.y;  // scale = 1 / (alpha - beta)
+      const double ir2 = 1.0 / fma(dr, dr, di * di);
+      scale = make_double2(dr * ir2, -di * ir2);
+    }
+    if (lane == 0) {
+      dvec[S.toff + k] = x[0].x;
+      evec[S.toff + k] = beta;
+      tauv[S.toff + k] = tau;
+      *tau_slot = tau;
+      *sc = scale;
+    }
   }
-  if (t == 0) {
-    dvec[S.toff + k] = x[0].x;
-    evec[S.toff + k] = beta;
-    tauv[S.toff + k] = tau;
-    *tau_slot = tau;
-  }
+  __syncthreads();
+  const double2 scale = *sc;
   double2* Ak = A + (long long)k * n;
   for (int i = k + 1 + t; i < n; i += kDsThreads) {
     const double2 vi = i == k + 1 ? make_double2(1.0, 0.0) : cmul(x[i - k], scale);
@@ -353,6 +368,10 @@ __device__ __forceinline__ void ds_reflector(int k, int n, const double2* x, dou
   }
 }
 
+// kGlobal: the owned lower columns stay in place in global memory (L2)
+// instead of the CTA's shared memory, for sectors too large for the cluster's
+// shared memory; the O(n) vector slots stay in shared memory either way.
+template <bool kGlobal>
 __global__ void __launch_bounds__(kDsThreads, 1)
     reduce_ds_kernel(double2* __restrict__ den, const Sector* __restrict__ secs, double* __restrict__ dvec,
                      double* __restrict__ evec, double2* __restrict__ tauv) {
@@ -367,23 +386,27 @@ __global__ void __launch_bounds__(kDsThreads, 1)
   double2* wb = sm + 2 * n;   // p, then w
   double2* pp = sm + 3 * n;   // this CTA's partial B v
   double2* ps = sm + 4 * n;   // tau (B v) of the rows i = r (mod C), summed over the cluster
-  double2* col = sm + 5 * n;  // the owned lower columns
-  __shared__ double2 s_tau[2], s_dot, s_a2;
+  double2* col = sm + 5 * n;  // the owned lower columns (packed; unused when kGlobal)
+  // element (i, j), i >= j, of an owned column whose packed offset is o
+  auto el = [&](long long o, int j, int i) -> double2& { return kGlobal ? A[(long long)j * n + i] : col[o + (i - j)]; };
+  __shared__ double2 s_tau[2], s_dot, s_a2, s_scale;
   __shared__ double red_d[kWarps];
   __shared__ double2 red_c[kWarps];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int nq = n > r ? (n - r + C - 1) / C : 0;
-  for (int q = 0; q < nq; ++q) {
-    const int j = q * C + r;
-    const long long o = ds_col_off(q, n, C, r);
-    for (int i = j + t; i < n; i += kDsThreads) col[o + (i - j)] = A[(long long)j * n + i];
+  if (!kGlobal) {
+    for (int q = 0; q < nq; ++q) {
+      const int j = q * C + r;
+      const long long o = ds_col_off(q, n, C, r);
+      for (int i = j + t; i < n; i += kDsThreads) col[o + (i - j)] = A[(long long)j * n + i];
+    }
   }
   __syncthreads();
   if (r == 0) {  // column 0
     if (n > 1) {
-      ds_reflector(0, n, col, vbuf, &s_tau[0], red_d, A, S, dvec, evec, tauv);
+      ds_reflector(0, n, &el(0, 0, 0), vbuf, &s_tau[0], &s_scale, red_d, A, S, dvec, evec, tauv);
     } else if (t == 0) {
-      dvec[S.toff] = col[0].x;
+      dvec[S.toff] = el(0, 0, 0).x;
       evec[S.toff] = 0.0;
       tauv[S.toff] = make_double2(0.0, 0.0);
     }
@@ -409,7 +432,7 @@ __global__ void __launch_bounds__(kDsThreads, 1)
       double2 acc = make_double2(0.0, 0.0);
       long long o = olo;
       for (int j = qlo * C + r; j <= i; j += C) {
-        acc = cfma(col[o + (i - j)], vb[j], acc);
+        acc = cfma(el(o, j, i), vb[j], acc);
         o += n - j;
       }
       pp[i] = acc;
@@ -419,7 +442,7 @@ __global__ void __launch_bounds__(kDsThreads, 1)
     for (int q = qlo + warp, j = (qlo + warp) * C + r; j < n; q += kWarps, j += kWarps * C) {
       const long long o = ds_col_off(q, n, C, r);
       double2 sum = make_double2(0.0, 0.0);
-      for (int i = j + 1 + lane; i < n; i += 32) sum = cfmac(col[o + (i - j)], vb[i], sum);
+      for (int i = j + 1 + lane; i < n; i += 32) sum = cfmac(el(o, j, i), vb[i], sum);
       sum = warp_sum2(sum);
       if (lane == 0) pp[j] = cadd(pp[j], sum);
     }
@@ -432,6 +455,7 @@ __global__ void __launch_bounds__(kDsThreads, 1)
       const uint32_t rp = ds_map(pp, src);
       double2 dot = make_double2(0.0, 0.0);
       for (int base = 0; base < nr; base += per) {  // the same trip count in every thread
+        if (base + (warp * 32) / C >= nr) continue;  // this warp has no rows in this pass (uniform per warp)
         const int ri = base + slot, i = i0 + ri * C;
         // every lane of a C-lane group takes part in its shuffles
         double2 val = ri < nr ? ds_ld2(rp + (uint32_t)(i * sizeof(double2))) : make_double2(0.0, 0.0);
@@ -445,16 +469,12 @@ __global__ void __launch_bounds__(kDsThreads, 1)
           dot = cfmac(p, vb[i], dot);  // conj(p_i) v_i
         }
       }
-      if (nr > 0) {  // uniform over the CTA
-        dot = warp_sum2(dot);
-        if (lane == 0) red_c[warp] = dot;
-        __syncthreads();
-        if (warp == 0) {
-          double2 sd = warp_sum2(lane < kWarps ? red_c[lane] : make_double2(0.0, 0.0));
-          if (lane == 0) s_dot = sd;
-        }
-      } else if (t == 0) {
-        s_dot = make_double2(0.0, 0.0);
+      if ((warp * 32) / C < nr) dot = warp_sum2(dot);  // warps that held rows
+      if (lane == 0) red_c[warp] = dot;
+      __syncthreads();
+      if (warp == 0) {
+        const double2 sd = warp_sum2(lane < kWarps ? red_c[lane] : make_double2(0.0, 0.0));
+        if (lane == 0) s_dot = sd;
       }
     }
     ds_sync();  // p and the partial dots are complete
@@ -477,12 +497,13 @@ __global__ void __launch_bounds__(kDsThreads, 1)
       // column, its diagonal
       const long long o = ds_col_off(nx / C, n, C, r);
       const double2 vj = vb[nx], wj = wb[nx];
-      for (int i = nx + t; i < n; i += kDsThreads) col[o + (i - nx)] = rank2(col[o + (i - nx)], vb[i], wb[i], vj, wj);
+      for (int i = nx + t; i < n; i += kDsThreads) el(o, nx, i) = rank2(el(o, nx, i), vb[i], wb[i], vj, wj);
       __syncthreads();
       if (nx + 1 < n) {
-        ds_reflector(nx, n, col + o, vbuf + (nx & 1) * n, &s_tau[nx & 1], red_d, A, S, dvec, evec, tauv);
+        ds_reflector(nx, n, &el(o, nx, nx), vbuf + (nx & 1) * n, &s_tau[nx & 1], &s_scale, red_d, A, S, dvec, evec,
+                     tauv);
       } else if (t == 0) {
-        dvec[S.toff + nx] = col[o].x;
+        dvec[S.toff + nx] = el(o, nx, nx).x;
         evec[S.toff + nx] = 0.0;
         tauv[S.toff + nx] = make_double2(0.0, 0.0);
       }
@@ -491,7 +512,7 @@ __global__ void __launch_bounds__(kDsThreads, 1)
       const double2 vi = vb[i], wi = wb[i];
       long long o = olo;
       for (int j = qlo * C + r; j <= i; j += C) {
-        if (j != nx || !own_next) col[o + (i - j)] = rank2(col[o + (i - j)], vi, wi, vb[j], wb[j]);
+        if (j != nx || !own_next) el(o, j, i) = rank2(el(o, j, i), vi, wi, vb[j], wb[j]);
         o += n - j;
       }
     }
@@ -982,81 +1003,30 @@ cudaError_t reduce(const Sector* d_secs, int nsec, int maxn, double2* den, doubl
 namespace {
 
 // dynamic shared memory of reduce_ds_kernel for sectors of at most n states:
-// the five vector slots and the packed lower columns of cluster rank 0 (the
-// most of any rank)
-size_t ds_smem_bytes(int n, int C) {
+// the five vector slots and, in shared memory, the packed lower columns of
+// cluster rank 0 (the most of any rank)
+size_t ds_smem_bytes(int n, int C, bool global_cols) {
   const int nq = (n + C - 1) / C;
-  return (size_t)(5LL * n + ds_col_off(nq, n, C, 0)) * sizeof(double2);
+  return (size_t)(5LL * n + (global_cols ? 0 : ds_col_off(nq, n, C, 0))) * sizeof(double2);
 }
 
-// dynamic shared memory one CTA of reduce_ds_kernel may use on this device
+template <bool kGlobal>
 size_t ds_smem_limit() {
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, reduce_ds_kernel) != cudaSuccess) return 0;
+  if (cudaFuncGetAttributes(&fa, reduce_ds_kernel<kGlobal>) != cudaSuccess) return 0;
   return optin > (int)fa.sharedSizeBytes ? (size_t)optin - fa.sharedSizeBytes : 0;
 }
 
-}  // namespace
-
-int ds_cluster_size() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 8;
-  static int cached[64] = {0};
-  if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
-  // 16 CTAs per cluster is beyond the portable size: used where the device
-  // can place such a cluster with the kernel's largest shared-memory use
-  int size = 8;
-  const size_t smem = ds_smem_limit();
-  if (smem > 0 &&
-      cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-      cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-          cudaSuccess) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kClusterMax, 1, 1);
-    cfg.blockDim = dim3(kDsThreads, 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterMax;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, reduce_ds_kernel, &cfg) == cudaSuccess && nclusters >= 1)
-      size = kClusterMax;
-  }
-  cudaGetLastError();  // a refused query leaves no error behind
-  if (dev >= 0 && dev < 64) cached[dev] = size;
-  return size;
-}
-
-int ds_max_n() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  static int cached[64] = {0};
-  if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
-  const int C = ds_cluster_size();
-  const size_t lim = ds_smem_limit();
-  int n = 0;
-  while (n < kMaxN && ds_smem_bytes(n + 1, C) <= lim) ++n;
-  cudaGetLastError();
-  if (dev >= 0 && dev < 64) cached[dev] = n;
-  return n;
-}
-
-cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, double2* den, double* d, double* e, double2* tau,
-                      cudaStream_t s) {
-  if (nsec <= 0) return cudaSuccess;
-  if (maxn > ds_max_n()) return cudaErrorInvalidValue;
-  const int C = ds_cluster_size();
-  const size_t smem = ds_smem_bytes(maxn, C);
-  cudaError_t e0 = cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <bool kGlobal>
+cudaError_t launch_ds(const Sector* d_secs, int nsec, size_t smem, int C, double2* den, double* d, double* e,
+                      double2* tau, cudaStream_t s) {
+  cudaError_t e0 = cudaFuncSetAttribute(reduce_ds_kernel<kGlobal>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem);
   if (e0 == cudaSuccess && C > 8)
-    e0 = cudaFuncSetAttribute(reduce_ds_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    e0 = cudaFuncSetAttribute(reduce_ds_kernel<kGlobal>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e0 != cudaSuccess) return e0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(nsec * C), 1, 1);
@@ -1070,7 +1040,67 @@ cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, double2* den, do
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, reduce_ds_kernel, den, d_secs, d, e, tau);
+  return cudaLaunchKernelEx(&cfg, reduce_ds_kernel<kGlobal>, den, d_secs, d, e, tau);
+}
+
+}  // namespace
+
+int ds_cluster_size() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 8;
+  static int cached[64] = {0};
+  if (dev >= 0 && dev < 64 && cached[dev]) return cached[dev];
+  // 16 CTAs per cluster is beyond the portable size: used where the device
+  // can place such a cluster with the kernel's largest shared-memory use
+  int size = 8;
+  const size_t smem = ds_smem_limit<false>();
+  if (smem > 0 &&
+      cudaFuncSetAttribute(reduce_ds_kernel<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(reduce_ds_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+          cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kClusterMax, 1, 1);
+    cfg.blockDim = dim3(kDsThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterMax;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, reduce_ds_kernel<false>, &cfg) == cudaSuccess && nclusters >= 1)
+      size = kClusterMax;
+  }
+  cudaGetLastError();  // a refused query leaves no error behind
+  if (dev >= 0 && dev < 64) cached[dev] = size;
+  return size;
+}
+
+int ds_max_n(bool global_cols) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  static int cached[2][64] = {};
+  if (dev >= 0 && dev < 64 && cached[global_cols][dev]) return cached[global_cols][dev];
+  const int C = ds_cluster_size();
+  const size_t lim = global_cols ? ds_smem_limit<true>() : ds_smem_limit<false>();
+  int n = 0;
+  while (n < kMaxN && ds_smem_bytes(n + 1, C, global_cols) <= lim) ++n;
+  cudaGetLastError();
+  if (dev >= 0 && dev < 64) cached[global_cols][dev] = n;
+  return n;
+}
+
+cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, bool global_cols, double2* den, double* d, double* e,
+                      double2* tau, cudaStream_t s) {
+  if (nsec <= 0) return cudaSuccess;
+  if (maxn > ds_max_n(global_cols)) return cudaErrorInvalidValue;
+  const int C = ds_cluster_size();
+  const size_t smem = ds_smem_bytes(maxn, C, global_cols);
+  return global_cols ? launch_ds<true>(d_secs, nsec, smem, C, den, d, e, tau, s)
+                     : launch_ds<false>(d_secs, nsec, smem, C, den, d, e, tau, s);
 }
 
 cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, const double* e, double* w,

@@ -67,13 +67,16 @@ struct PhaseItem {
 // tau; p (n per sector) and dots (kCluster per sector) are scratch
 cudaError_t reduce(const Sector* d_secs, int nsec, int maxn, double2* den, double* d, double* e, double2* tau,
                    double2* p, double2* dots, cudaStream_t s);
-// the same reduction with each sector held in the distributed shared memory of
-// a cluster of ds_cluster_size() CTAs (16 where the device can place such a
-// cluster, else 8): sectors of at most ds_max_n() states, maxn the largest
+// the same reduction on a cluster of ds_cluster_size() CTAs (16 where the
+// device can place such a cluster, else 8) with its vectors in distributed
+// shared memory and each sector's lower columns in the CTAs' shared memory
+// (global_cols false: sectors of at most ds_max_n(false) states) or in place
+// in global memory (global_cols true: at most ds_max_n(true)); maxn is the
+// largest sector of the launch
 int ds_cluster_size();
-int ds_max_n();
-cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, double2* den, double* d, double* e, double2* tau,
-                      cudaStream_t s);
+int ds_max_n(bool global_cols);
+cudaError_t reduce_ds(const Sector* d_secs, int nsec, int maxn, bool global_cols, double2* den, double* d, double* e,
+                      double2* tau, cudaStream_t s);
 // all eigenvalues of every T, ascending, by bisection
 cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, const double* e, double* w,
                    cudaStream_t s);
