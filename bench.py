@@ -82,6 +82,8 @@ def parse():
     p.add_argument("--window-m", type=int, default=2000, help="kept multiplets of the sweep window")
     p.add_argument("--window-steps", type=int, default=4, help="timed mid-chain steps per arm in the sweep window")
     p.add_argument("--window-L", type=int, default=32, help="cylinder length of the sweep window (N_e = 3.5 L)")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the c3 / c4 matvec measurements reported beside the headline line")
     p.add_argument("--eigensolver", default="own", choices=["own", "cusolver"],
                    help="density-matrix eigensolver of both arms: the library's own FP64 kernels (default) or "
                         "cuSOLVER zheevd above 32 states (comparison)")
@@ -410,6 +412,63 @@ def window_bench(dev, args):
     return out
 
 
+def config_matvec_bench(dev, name, steps, prec_name):
+    """The matvec of another configuration's mid-chain superblock (c3: t-J 4x48,
+    J = 0.4, phi = 1/6, N_e = 176, m = 4000; c4: Hubbard 6x24, phi = 1/3, U = 8,
+    N_e = 132, m = 6000; synthetic operators as for the headline workload):
+    split-precision matvecs/s by CUDA events over `steps` graph replays (L2
+    flushed before each), the FP64 GPU matvec rate over one product, and the
+    split product's error against FP64."""
+    import torch
+    from hofstadter_hubbard_tsc_gb300.superblock import Superblock
+    from hofstadter_hubbard_tsc_gb300 import _lib
+    a = argparse.Namespace(config=name, W=4, L=32, ne=112, m=2000)
+    t0 = time.perf_counter()
+    wl = make_workload(a)
+    gen_s = time.perf_counter() - t0
+    prec = PREC[prec_name]
+    dev.sync()
+    t0 = time.perf_counter()
+    sb = Superblock(dev, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo, precision=prec)
+    dev.sync()
+    plan_s = time.perf_counter() - t0
+    rng = np.random.default_rng(5)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    psi /= np.linalg.norm(psi)
+    sb.w_in.upload(psi)
+    stream = torch.cuda.ExternalStream(dev.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(pp, n):
+        for _ in range(2):
+            dev.check(dev.lib.hh_matvec_async(sb.plan, sb.w_in.h, sb.w_out.h, pp))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        with torch.cuda.stream(stream):
+            for e0, e1 in ev:
+                flush.zero_()
+                e0.record(stream)
+                dev.check(dev.lib.hh_matvec_async(sb.plan, sb.w_in.h, sb.w_out.h, pp))
+                e1.record(stream)
+        dev.check(dev.lib.hh_plan_check(sb.plan))
+        torch.cuda.synchronize()
+        return sum(e0.elapsed_time(e1) for e0, e1 in ev) / n
+
+    ms_split = timed(prec, steps)
+    hs = sb.w_out.download()
+    dev.check(dev.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
+    h64 = sb.w_out.download()
+    ms64 = timed(_lib.HH_PREC_FP64, 1)
+    out = {"config": dict(wl.describe(), **{"precision": prec_name}), "matvecs_per_s": 1e3 / ms_split,
+           "ms_per_matvec": ms_split, "steps": steps, "fp64_matvecs_per_s": 1e3 / ms64,
+           "split_vs_fp64_matvec": ms64 / ms_split,
+           "rel_err_vs_fp64_gpu": float(np.linalg.norm(hs - h64) / np.linalg.norm(h64)),
+           "workload_generation_s": round(gen_s, 2), "plan_build_s": round(plan_s, 3),
+           "timing": "CUDA events on the library stream, graph replays, L2 flushed before each"}
+    sb.free()
+    del flush
+    return out
+
+
 def run_reference(args, rank, ws, dist):
     if rank != 0:
         return
@@ -635,6 +694,8 @@ def main():
         line["sweep"] = sweep_bench(dev, args)
     if rank == 0 and not args.no_window and args.config == "c2":
         line["sweep_window"] = window_bench(dev, args)
+    if rank == 0 and not args.no_configs and args.config == "c2":
+        line["other_configs"] = {name: config_matvec_bench(dev, name, 5, args.precision) for name in ("c3", "c4")}
     if not args.no_energy_check:
         rs = np.random.default_rng(7)
         start = rs.normal(size=wl.sup.dim) + 1j * rs.normal(size=wl.sup.dim)

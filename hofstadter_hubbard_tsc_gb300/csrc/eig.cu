@@ -627,13 +627,16 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
     }
     const int q = R.tri_pos[k];
     for (int col = 0; col < nc; ++col) inv.push_back(tri::InvItem{q, n - nc + col, col, nc, zt});
-    // numerically degenerate kept eigenvalues: Gram-Schmidt before Newton-Schulz
+    // clusters of numerically degenerate kept eigenvalues (consecutive gaps
+    // below 1e-13 ||T||): Gram-Schmidt within each before Newton-Schulz
     const double* wk = R.w.data() + R.woff[k];
     const double tn = std::max(std::fabs(wk[0]), std::fabs(wk[n - 1]));
-    bool degenerate = false;
-    for (int j = n - nc; j + 1 < n; ++j)
-      if (wk[j + 1] - wk[j] <= 1e-13 * tn) degenerate = true;
-    if (degenerate) cgs.push_back(tri::CgsBlock{zt, n, nc});
+    for (int j0 = n - nc; j0 < n;) {
+      int j1 = j0 + 1;
+      while (j1 < n && wk[j1] - wk[j1 - 1] <= 1e-13 * tn) ++j1;
+      if (j1 - j0 > 1) cgs.push_back(tri::CgsBlock{zt, n, nc, j0 - (n - nc), j1 - (n - nc)});
+      j0 = j1;
+    }
     for (int c0 = 0; c0 < nc; c0 += tri::kBtCols)
       bt.push_back(tri::BtItem{q, c0, std::min(tri::kBtCols, nc - c0), nc, zt, xoff[k]});
     blks.push_back(Blk{zt, gt, n, nc});

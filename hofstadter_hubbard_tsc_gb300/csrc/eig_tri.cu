@@ -806,35 +806,36 @@ __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const 
 }
 
 // ------------------------------------------------------------------- cgs2
-// One CTA per block: each column, from the last (largest eigenvalue) to the
-// first, is orthogonalised against the ones already done, twice, and
-// normalised.
+// One CTA per cluster of numerically degenerate kept eigenvalues: each of its
+// columns, from the last (largest eigenvalue) to the first, is
+// orthogonalised against the cluster's columns already done, twice, and
+// normalised.  Inverse iteration leaves the vectors of a degenerate cluster
+// as independent but non-orthogonal combinations of its eigenspace; vectors
+// of eigenvalues further apart (relative gap above 1e-13) are orthogonal to
+// about eps / gap, which the Newton-Schulz steps that follow remove.  Each
+// coefficient is a CTA-wide dot product (shuffle trees), so a cluster of c
+// vectors costs O(c^2) short reductions.
 __global__ void cgs2_kernel(const CgsBlock* __restrict__ blocks, double* __restrict__ Z) {
   const CgsBlock b = blocks[blockIdx.x];
   double* Zb = Z + b.zoff;
   const int n = b.n, k = b.ldz;
-  extern __shared__ double coef[];  // k
   __shared__ double scratch[32];
-  for (int c = k - 1; c >= 0; --c) {
+  for (int c = b.c1 - 1; c >= b.c0; --c) {
     for (int pass = 0; pass < 2; ++pass) {
-      // coefficients against the finished columns c+1 .. k-1
-      for (int q = c + 1 + threadIdx.x; q < k; q += blockDim.x) {
+      for (int q = c + 1; q < b.c1; ++q) {
         double s = 0.0;
-        for (int i = 0; i < n; ++i) s = fma(Zb[(long long)i * k + q], Zb[(long long)i * k + c], s);
-        coef[q] = s;
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+          s = fma(Zb[(long long)i * k + q], Zb[(long long)i * k + c], s);
+        s = block_sum(s, scratch);
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+          Zb[(long long)i * k + c] = fma(-s, Zb[(long long)i * k + q], Zb[(long long)i * k + c]);
+        __syncthreads();
       }
-      __syncthreads();
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double s = Zb[(long long)i * k + c];
-        for (int q = c + 1; q < k; ++q) s = fma(-coef[q], Zb[(long long)i * k + q], s);
-        Zb[(long long)i * k + c] = s;
-      }
-      __syncthreads();
     }
     double s2 = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const double z = Zb[(long long)i * k + c];
-      s2 += z * z;
+      s2 = fma(z, z, s2);
     }
     s2 = block_sum(s2, scratch);
     const double r = s2 > 0.0 ? 1.0 / sqrt(s2) : 0.0;
@@ -1125,7 +1126,8 @@ cudaError_t inverse_iteration(const Sector* d_secs, const InvItem* d_items, int 
 
 cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, int maxk, double* Z, cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  cgs2_kernel<<<(unsigned)nblocks, 256, (size_t)maxk * sizeof(double), s>>>(d_blocks, Z);
+  (void)maxk;
+  cgs2_kernel<<<(unsigned)nblocks, 256, 0, s>>>(d_blocks, Z);
   return cudaGetLastError();
 }
 

@@ -51,10 +51,12 @@ struct BtItem {
   long long xoff;  // output: column-major n x ldz block (ld n), absolute element offset
 };
 
-// The Z block of a sector whose kept vectors go through Gram-Schmidt.
+// A cluster of numerically degenerate kept eigenvalues: columns [c0, c1) of a
+// sector's Z block go through Gram-Schmidt among themselves.
 struct CgsBlock {
   long long zoff;  // row-major n x ldz
   int n, ldz;
+  int c0, c1;
 };
 
 // A column range to put in the canonical phase.
@@ -83,8 +85,8 @@ cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, co
 // kept eigenvectors of T by inverse iteration (lu: 5 * maxn * nitems doubles)
 cudaError_t inverse_iteration(const Sector* d_secs, const InvItem* d_items, int nitems, int maxn, const double* d,
                               const double* e, const double* w, double* Z, double* lu, cudaStream_t s);
-// classical Gram-Schmidt twice over the columns of the Z blocks of the listed
-// sectors (numerically degenerate kept eigenvalues)
+// classical Gram-Schmidt twice within each listed cluster of columns
+// (numerically degenerate kept eigenvalues), one CTA per cluster
 cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, int maxk, double* Z, cudaStream_t s);
 // batched strided FP64 GEMMs, ntiles = total 64 x 64 tiles of the items
 cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s);

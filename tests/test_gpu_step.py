@@ -53,11 +53,14 @@ def test_density_truncate(device, side):
 
 @pytest.mark.parametrize("side", [0, 1])
 def test_density_truncate_sector_sizes(device, side):
-    """Sector sizes on both sides of the eigensolver's switch from its Jacobi
-    kernel to zheevd (32 states) and well past it, with a spectrum decaying over
-    many decades like a DMRG density matrix."""
+    """Sector sizes on both sides of each switch of the eigensolver: its
+    Jacobi kernel (up to 32 states), the cluster reduction with the sector in
+    shared memory (up to about 600) and with the sector in place in global
+    memory (700 here), with a spectrum decaying over many decades like a DMRG
+    density matrix."""
     from oracle.blocks import SSector, Super, WSub, Wave
-    dims = [(1, 2), (7, 9), (31, 12), (32, 40), (33, 50), (64, 60), (112, 120), (150, 160), (300, 280)]
+    dims = [(1, 2), (7, 9), (31, 12), (32, 40), (33, 50), (64, 60), (112, 120), (150, 160), (300, 280),
+            (512, 400), (700, 300)]
     rng = np.random.default_rng(21)
     subs = []
     for k, (a, b) in enumerate(dims):
