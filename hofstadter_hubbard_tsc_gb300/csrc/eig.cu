@@ -608,6 +608,7 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   cudaError_t e = cudaSuccess;
   std::vector<tri::InvItem> inv;
   std::vector<tri::CgsBlock> cgs;
+  std::vector<int2> clusters;
   std::vector<tri::BtItem> bt;
   std::vector<tri::PhaseItem> ph;
   struct Blk { long long zoff, goff; int n, k; };
@@ -631,12 +632,15 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
     // below 1e-13 ||T||): Gram-Schmidt within each before Newton-Schulz
     const double* wk = R.w.data() + R.woff[k];
     const double tn = std::max(std::fabs(wk[0]), std::fabs(wk[n - 1]));
-    for (int j0 = n - nc; j0 < n;) {
-      int j1 = j0 + 1;
-      while (j1 < n && wk[j1] - wk[j1 - 1] <= 1e-13 * tn) ++j1;
-      if (j1 - j0 > 1) cgs.push_back(tri::CgsBlock{zt, n, nc, j0 - (n - nc), j1 - (n - nc)});
-      j0 = j1;
+    const int cl_first = (int)clusters.size();
+    for (int j1 = n; j1 > n - nc;) {  // from the top down
+      int j0 = j1 - 1;
+      while (j0 > n - nc && wk[j0] - wk[j0 - 1] <= 1e-13 * tn) --j0;
+      if (j1 - j0 > 1) clusters.push_back(make_int2(j0 - (n - nc), j1 - (n - nc)));
+      j1 = j0;
     }
+    if ((int)clusters.size() > cl_first)
+      cgs.push_back(tri::CgsBlock{zt, n, nc, cl_first, (int)clusters.size() - cl_first});
     for (int c0 = 0; c0 < nc; c0 += tri::kBtCols)
       bt.push_back(tri::BtItem{q, c0, std::min(tri::kBtCols, nc - c0), nc, zt, xoff[k]});
     blks.push_back(Blk{zt, gt, n, nc});
@@ -685,6 +689,7 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
     c.take<tri::BtItem>(bt.size());
     c.take<tri::PhaseItem>(ph.size());
     c.take<tri::CgsBlock>(cgs.size());
+    c.take<int2>(clusters.size());
     need = c.off;
   }
   int st = reserve(ctx, &S->d_buf3, &S->cap3, need, "allocate eigenvector workspace");
@@ -699,6 +704,7 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   tri::BtItem* d_bt = c.take<tri::BtItem>(bt.size());
   tri::PhaseItem* d_ph = c.take<tri::PhaseItem>(ph.size());
   tri::CgsBlock* d_cgs = c.take<tri::CgsBlock>(cgs.size());
+  int2* d_clusters = c.take<int2>(clusters.size());
   auto up = [&](void* dst, const void* src, size_t bytes) {
     if (e == cudaSuccess && bytes > 0) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   };
@@ -707,10 +713,11 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   up(d_bt, bt.data(), bt.size() * sizeof(tri::BtItem));
   up(d_ph, ph.data(), ph.size() * sizeof(tri::PhaseItem));
   up(d_cgs, cgs.data(), cgs.size() * sizeof(tri::CgsBlock));
+  up(d_clusters, clusters.data(), clusters.size() * sizeof(int2));
   if (e != cudaSuccess) return cuda_check(ctx, e, "eigenvector work lists");
   if (nitems > 0) {
     e = tri::inverse_iteration(R.d_secs, d_inv, nitems, maxn, R.d_d, R.d_e, R.d_w, d_z, d_lu, s);
-    if (e == cudaSuccess) e = tri::cgs2(d_cgs, (int)cgs.size(), maxk, d_z, s);
+    if (e == cudaSuccess) e = tri::cgs2(d_cgs, (int)cgs.size(), d_clusters, maxk, d_z, s);
     for (int q = 0; q < 2 * kSteps && e == cudaSuccess; ++q) e = tri::gemm(d_gi[q], (int)gi[q].size(), ntiles[q], d_z, s);
     if (e == cudaSuccess) e = tri::backtransform(R.d_secs, d_bt, (int)bt.size(), R.A, R.d_tau, d_z + final_z, X, s);
     if (e != cudaSuccess) return cuda_check(ctx, e, "kept eigenvectors (inverse iteration)");

@@ -806,31 +806,43 @@ __global__ void inverse_iteration_kernel(const Sector* __restrict__ secs, const 
 }
 
 // ------------------------------------------------------------------- cgs2
-// One CTA per cluster of numerically degenerate kept eigenvalues: each of its
-// columns, from the last (largest eigenvalue) to the first, is
-// orthogonalised against the cluster's columns already done, twice, and
-// normalised.  Inverse iteration leaves the vectors of a degenerate cluster
-// as independent but non-orthogonal combinations of its eigenspace; vectors
-// of eigenvalues further apart (relative gap above 1e-13) are orthogonal to
-// about eps / gap, which the Newton-Schulz steps that follow remove.  Each
-// coefficient is a CTA-wide dot product (shuffle trees), so a cluster of c
-// vectors costs O(c^2) short reductions.
-__global__ void cgs2_kernel(const CgsBlock* __restrict__ blocks, double* __restrict__ Z) {
+// One CTA per sector block with clusters of numerically degenerate kept
+// eigenvalues: each column of each cluster, from the last (largest
+// eigenvalue) to the first, is orthogonalised against every column after it
+// in the block (the rest of its cluster and the larger eigenvalues'
+// columns), twice, and normalised; the block's clusters are taken from the
+// top down so that every column it projects against is final.  Inverse
+// iteration leaves the vectors of a degenerate cluster as independent but
+// non-orthogonal combinations of its eigenspace; vectors of eigenvalues
+// further apart (relative gap above 1e-13) are orthogonal to about
+// eps / gap, which the Newton-Schulz steps that follow remove.  Only the
+// clusters' columns are processed (the whole block, column by column, cost
+// tens of milliseconds per sector).
+__global__ void cgs2_kernel(const CgsBlock* __restrict__ blocks, const int2* __restrict__ clusters,
+                            double* __restrict__ Z) {
   const CgsBlock b = blocks[blockIdx.x];
   double* Zb = Z + b.zoff;
   const int n = b.n, k = b.ldz;
+  extern __shared__ double coef[];  // k
   __shared__ double scratch[32];
-  for (int c = b.c1 - 1; c >= b.c0; --c) {
+  for (int cl = 0; cl < b.ncl; ++cl) {
+  const int2 range = clusters[b.cl0 + cl];
+  for (int c = range.y - 1; c >= range.x; --c) {
     for (int pass = 0; pass < 2; ++pass) {
-      for (int q = c + 1; q < b.c1; ++q) {
+      // coefficients against the columns c+1 .. k-1, one per thread (rows of
+      // the row-major block are contiguous over q)
+      for (int q = c + 1 + threadIdx.x; q < k; q += blockDim.x) {
         double s = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-          s = fma(Zb[(long long)i * k + q], Zb[(long long)i * k + c], s);
-        s = block_sum(s, scratch);
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-          Zb[(long long)i * k + c] = fma(-s, Zb[(long long)i * k + q], Zb[(long long)i * k + c]);
-        __syncthreads();
+        for (int i = 0; i < n; ++i) s = fma(Zb[(long long)i * k + q], Zb[(long long)i * k + c], s);
+        coef[q] = s;
       }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = Zb[(long long)i * k + c];
+        for (int q = c + 1; q < k; ++q) s = fma(-coef[q], Zb[(long long)i * k + q], s);
+        Zb[(long long)i * k + c] = s;
+      }
+      __syncthreads();
     }
     double s2 = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -841,6 +853,7 @@ __global__ void cgs2_kernel(const CgsBlock* __restrict__ blocks, double* __restr
     const double r = s2 > 0.0 ? 1.0 / sqrt(s2) : 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) Zb[(long long)i * k + c] *= r;
     __syncthreads();
+  }
   }
 }
 
@@ -1124,10 +1137,10 @@ cudaError_t inverse_iteration(const Sector* d_secs, const InvItem* d_items, int 
   return cudaGetLastError();
 }
 
-cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, int maxk, double* Z, cudaStream_t s) {
+cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, const int2* d_clusters, int maxk, double* Z,
+                 cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
-  (void)maxk;
-  cgs2_kernel<<<(unsigned)nblocks, 256, 0, s>>>(d_blocks, Z);
+  cgs2_kernel<<<(unsigned)nblocks, 256, (size_t)maxk * sizeof(double), s>>>(d_blocks, d_clusters, Z);
   return cudaGetLastError();
 }
 

@@ -51,12 +51,14 @@ struct BtItem {
   long long xoff;  // output: column-major n x ldz block (ld n), absolute element offset
 };
 
-// A cluster of numerically degenerate kept eigenvalues: columns [c0, c1) of a
-// sector's Z block go through Gram-Schmidt among themselves.
+// The Z block of a sector with clusters of numerically degenerate kept
+// eigenvalues: the column ranges [c0, c1) in clusters[cl0, cl0 + ncl), last
+// (largest eigenvalues) first, go through Gram-Schmidt against every later
+// column of the block.
 struct CgsBlock {
   long long zoff;  // row-major n x ldz
   int n, ldz;
-  int c0, c1;
+  int cl0, ncl;
 };
 
 // A column range to put in the canonical phase.
@@ -85,9 +87,11 @@ cudaError_t bisect(const Sector* d_secs, int nsec, int maxn, const double* d, co
 // kept eigenvectors of T by inverse iteration (lu: 5 * maxn * nitems doubles)
 cudaError_t inverse_iteration(const Sector* d_secs, const InvItem* d_items, int nitems, int maxn, const double* d,
                               const double* e, const double* w, double* Z, double* lu, cudaStream_t s);
-// classical Gram-Schmidt twice within each listed cluster of columns
-// (numerically degenerate kept eigenvalues), one CTA per cluster
-cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, int maxk, double* Z, cudaStream_t s);
+// classical Gram-Schmidt twice of the clusters' columns (numerically
+// degenerate kept eigenvalues) against the later columns of their block, one
+// CTA per block; clusters holds (c0, c1) column ranges
+cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, const int2* d_clusters, int maxk, double* Z,
+                 cudaStream_t s);
 // batched strided FP64 GEMMs, ntiles = total 64 x 64 tiles of the items
 cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s);
 // X = Q Z into the truncation operator

@@ -729,12 +729,18 @@ static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision
   return cuda_check(ctx, e, "matvec");
 }
 
-// The vectors of a batch (waves of one layout holding nbatch vectors) are
-// multiplied one after another on the same plan (the tensor-core path as one
-// graph replay each); in and out must hold the same number of vectors.
+// The vectors of a batch (waves of one layout holding nbatch vectors): in
+// split precision one graph replay multiplies all of them (every stage one
+// launch over the whole batch, matvec_tc_batch); in FP64 they are multiplied
+// one after another on the same plan.  in and out must hold the same number
+// of vectors.
 static int matvec_batch(hh_plan* p, const hh_wave* in, hh_wave* out, int precision, bool check) {
   if (in->nelem != p->nelem || out->nelem != p->nelem || in == out || in->nbatch != out->nbatch)
     return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
+  if (precision != HH_PREC_FP64 && in->nbatch > 1) {
+    if (!split_of(precision)) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
+    return matvec_tc_batch(p, in->d, out->d, in->nbatch, check, split_of(precision));
+  }
   for (int b = 0; b < in->nbatch; ++b) {
     const bool last = b + 1 == in->nbatch;
     const int st = matvec_dev(p, in->d + (size_t)b * p->nelem, out->d + (size_t)b * p->nelem, precision,

@@ -230,6 +230,8 @@ struct hh_plan {
   hh_ctx* ctx = nullptr;
   std::vector<hh_contrib> contribs;
   hh_tc_plan tc;
+  hh_tc_plan tcb;  // the schedule of a batch of tcb_nb vectors (hh_matvec on a wave of several vectors)
+  int tcb_nb = 0;
   const hh_wave* layout = nullptr;
   long long nelem = 0;
   hh_gemm_list stage1, stage2;
@@ -287,6 +289,9 @@ void release_tc_plan(hh_plan* plan);
 // plan's error flag (p->tc.d_err) for the caller to read
 // split: BF16 parts per operand (3: BF16x6, 2: BF16x3)
 int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check = true, int split = 3);
+// nb vectors one after another in in / out, one launch per stage for all of
+// them (the batch schedule is built on first use and kept for that nb)
+int matvec_tc_batch(hh_plan* p, const double2* in, double2* out, int nb, bool check, int split);
 int tune_tc_plan(hh_plan* p, int reps, double* ms, int split);
 // BF16 parts per operand of a split precision, 0 for FP64 or an unknown code
 inline int split_of(int precision) {

@@ -112,17 +112,28 @@ void finish_tile(Tile& t, const Seg* segs) {
 
 }  // namespace tc
 
-void release_tc_plan(hh_plan* p) {
-  hh_tc_plan& t = p->tc;
+static void release_tc(hh_ctx* ctx, hh_tc_plan& t) {
   destroy_graph(t);
   void* ptrs[] = {t.d_op_img, t.d_x_img, t.d_t_img, t.d_op_tasks, t.d_x_tasks, t.d_tiles1,
                   t.d_tiles2, t.d_tiles2b, t.d_segs, t.d_csegs, t.d_err, t.d_io, t.d_x_blocks,
                   t.d_c_blocks, t.d_pieces};
-  for (void* q : ptrs) dev_free(p->ctx, q);
+  for (void* q : ptrs) dev_free(ctx, q);
   t = hh_tc_plan();
 }
 
-int build_tc_plan(hh_plan* p) {
+void release_tc_plan(hh_plan* p) {
+  release_tc(p->ctx, p->tc);
+  release_tc(p->ctx, p->tcb);
+  p->tcb_nb = 0;
+}
+
+// The schedule of nb vectors (a wave holding nb vectors one after another):
+// nb == 1 is the plan's own (p->tc); nb > 1 replicates every wave image,
+// T image and tile once per vector, the copies of a tile adjacent in every
+// order, so that ONE launch per stage multiplies the whole batch and the
+// copies of a tile, which read the same operator images, run side by side
+// and share those loads through L2.
+static int build_tc(hh_plan* p, hh_tc_plan& tp, int nb) {
   hh_ctx* ctx = p->ctx;
   const hh_wave* L = p->layout;
   // ---------------------------------------------------------------- images
@@ -437,6 +448,72 @@ int build_tc_plan(hh_plan* p) {
       (tl == &tiles1 ? mma1 : mma2) += f;
     }
 
+  // ------------------------------------------------------- batch copies
+  if (nb > 1) {
+    const long long xs = a_x.size, ts = a_t.size;  // per vector (multiples of 256 bytes)
+    constexpr long long kMask = (1LL << 60) - 1;
+    auto shift = [&](long long v, int b) {
+      const int arena = (int)((unsigned long long)v >> 60);
+      const long long o = v & kMask;
+      return arena == 1 ? tag(o + b * xs, 1) : arena == 2 ? tag(o + b * ts, 2) : v;
+    };
+    const int nsegs = (int)segs.size(), npieces = (int)pieces.size(), ncsegs = (int)csegs.size();
+    std::vector<tc::Seg> segs_b;
+    segs_b.reserve((size_t)nsegs * nb);
+    for (int b = 0; b < nb; ++b)
+      for (tc::Seg sg : segs) {
+        sg.a = shift(sg.a, b);
+        sg.b = shift(sg.b, b);
+        segs_b.push_back(sg);
+      }
+    std::vector<tc::TPiece> pieces_b;
+    for (int b = 0; b < nb; ++b)
+      for (tc::TPiece pc : pieces) {
+        pc.out = shift(pc.out, b);
+        pieces_b.push_back(pc);
+      }
+    std::vector<hh_seg> csegs_b;
+    for (int b = 0; b < nb; ++b)
+      for (hh_seg cs : csegs) {
+        cs.poff += (long long)b * p->nelem;
+        csegs_b.push_back(cs);
+      }
+    auto copies = [&](std::vector<tc::Tile>& tl) {
+      std::vector<tc::Tile> out;
+      out.reserve(tl.size() * nb);
+      for (const tc::Tile& x : tl)
+        for (int b = 0; b < nb; ++b) {
+          tc::Tile y = x;
+          y.seg0 += b * nsegs;
+          y.piece0 += b * npieces;
+          y.cseg0 += b * ncsegs;
+          if (y.mode == 0)
+            y.out += (long long)b * p->nelem;
+          else if (y.npiece == 0)
+            y.out = shift(y.out, b);
+          out.push_back(y);
+        }
+      tl.swap(out);
+    };
+    copies(tiles1);
+    copies(tiles2);
+    std::vector<tc::ImgTask> x_tasks_b;
+    for (int b = 0; b < nb; ++b)
+      for (tc::ImgTask tk : x_tasks) {
+        tk.src += (long long)b * p->nelem;
+        tk.dst += b * xs;
+        x_tasks_b.push_back(tk);
+      }
+    segs.swap(segs_b);
+    pieces.swap(pieces_b);
+    csegs.swap(csegs_b);
+    x_tasks.swap(x_tasks_b);
+    a_x.size = xs * nb;
+    a_t.size = ts * nb;
+    mma1 *= nb;
+    mma2 *= nb;
+  }
+
   // ------------------------------------------------------- tile order
   // Stage 1 (thousands of short tiles, at most kTileN wide) runs on the
   // 64-wide kernels (256 TMEM columns, two CTAs per SM; wider tiles, if any,
@@ -485,7 +562,7 @@ int build_tc_plan(hh_plan* p) {
   balance(tiles2b, n2n, tiles2b.size(), (size_t)sms);
 
   // --------------------------------------------------------------- device
-  hh_tc_plan& t = p->tc;
+  hh_tc_plan& t = tp;
   auto alloc = [&](void** ptr, size_t bytes) -> int {
     if (bytes == 0) bytes = 256;
     cudaError_t e = dev_alloc(ctx, ptr, bytes);
@@ -494,7 +571,7 @@ int build_tc_plan(hh_plan* p) {
   int st;
   if ((st = alloc(&t.d_op_img, a_op.size)) || (st = alloc(&t.d_x_img, a_x.size)) ||
       (st = alloc(&t.d_t_img, a_t.size))) {
-    release_tc_plan(p);
+    release_tc(ctx, tp);
     return st;
   }
   const long long base[3] = {(long long)(uintptr_t)t.d_op_img, (long long)(uintptr_t)t.d_x_img,
@@ -519,7 +596,7 @@ int build_tc_plan(hh_plan* p) {
   // when they cover the whole output wave no zeroing pass is needed
   long long covered = 0;
   for (const auto& x : tiles2) covered += (long long)x.mrem * x.nrem;
-  t.zero_out = covered != p->nelem;
+  t.zero_out = covered != (long long)nb * p->nelem;
   auto upload = [&](void** dptr, const void* src, size_t bytes) -> int {
     if ((st = alloc(dptr, bytes))) return st;
     if (bytes) {
@@ -539,7 +616,7 @@ int build_tc_plan(hh_plan* p) {
       (st = upload((void**)&t.d_segs, segs.data(), segs.size() * sizeof(tc::Seg))) ||
       (st = upload((void**)&t.d_csegs, csegs.data(), csegs.size() * sizeof(hh_seg))) ||
       (st = alloc((void**)&t.d_err, sizeof(int))) || (st = alloc((void**)&t.d_io, sizeof(tc::IoPtrs)))) {
-    release_tc_plan(p);
+    release_tc(ctx, tp);
     return st;
   }
   cudaMemsetAsync(t.d_err, 0, sizeof(int), ctx->stream);
@@ -560,7 +637,7 @@ int build_tc_plan(hh_plan* p) {
   const int n_op_blocks = tc_image_blocks(op_tasks.data(), (int)op_tasks.size(), op_blocks);
   int2* d_op_blocks = nullptr;
   if ((st = upload((void**)&d_op_blocks, op_blocks.data(), op_blocks.size() * sizeof(int2)))) {
-    release_tc_plan(p);
+    release_tc(ctx, tp);
     return st;
   }
   cudaError_t e = tc_build_images(t.d_op_tasks, t.n_op_tasks, nullptr, false, ctx->stream, nullptr, 3, d_op_blocks,
@@ -568,12 +645,14 @@ int build_tc_plan(hh_plan* p) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   dev_free(ctx, d_op_blocks);
   if (e != cudaSuccess) {
-    release_tc_plan(p);
+    release_tc(ctx, tp);
     return cuda_check(ctx, e, "build operator images");
   }
   t.ready = true;
   return HH_OK;
 }
+
+int build_tc_plan(hh_plan* p) { return build_tc(p, p->tc, 1); }
 
 // The launch sequence of one split-precision matvec: wave images, stage 1,
 // zeroed output (only when the stage-2 tiles leave elements uncovered), stage
@@ -581,9 +660,8 @@ int build_tc_plan(hh_plan* p) {
 // (graph capture).  (Copy terms folded into the stage-2 epilogue measured
 // slower, 0.232 against 0.205 ms at m = 2000: their loads sat on every
 // tile's critical path.)
-static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const tc::IoPtrs* io, cudaEvent_t* ev,
-                              int split) {
-  hh_tc_plan& t = p->tc;
+static cudaError_t enqueue_tc(hh_plan* p, hh_tc_plan& t, long long nelem, const double2* in, double2* out,
+                              const tc::IoPtrs* io, cudaEvent_t* ev, int split) {
   cudaStream_t s = p->ctx->stream;
   if (ev) cudaEventRecord(ev[0], s);
   cudaError_t e = tc_build_images(t.d_x_tasks, t.n_x_tasks, in, true, s, io, split, t.d_x_blocks, t.n_x_blocks);
@@ -594,7 +672,7 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
     e = tc_run_tiles(t.d_tiles1 + t.n_narrow1, t.n_tiles1 - t.n_narrow1, t.d_segs, out, t.d_err, t.persistent1, s,
                      io, 128, split, t.d_pieces);
   if (ev) cudaEventRecord(ev[2], s);
-  if (e == cudaSuccess && t.zero_out) e = tc_zero_out(out, p->nelem, s, io);
+  if (e == cudaSuccess && t.zero_out) e = tc_zero_out(out, nelem, s, io);
   const tc::Tile* tiles2 = t.persistent2 ? t.d_tiles2b : t.d_tiles2;
   if (e == cudaSuccess)
     e = tc_run_tiles(tiles2, t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s, io, 64, split);
@@ -607,19 +685,16 @@ static cudaError_t enqueue_tc(hh_plan* p, const double2* in, double2* out, const
   return e;
 }
 
-int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check, int split) {
+static int run_tc(hh_plan* p, hh_tc_plan& t, int nb, const double2* in, double2* out, float* ms, bool check,
+                  int split) {
   hh_ctx* ctx = p->ctx;
-  if (!p->tc.ready) {
-    int st = build_tc_plan(p);
-    if (st != HH_OK) return st;
-  }
-  hh_tc_plan& t = p->tc;
+  const long long nelem = (long long)nb * p->nelem;
   cudaError_t e = cudaSuccess;
   if (ms) {
     // eager launches with events between the stages
     cudaEvent_t ev[4];
     for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
-    e = enqueue_tc(p, in, out, nullptr, ev, split);
+    e = enqueue_tc(p, t, nelem, in, out, nullptr, ev, split);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
     if (e == cudaSuccess) {
       cudaEventElapsedTime(&ms[0], ev[0], ev[3]);
@@ -633,12 +708,12 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check
     // attributes); the graph is captured again at the new split next time
     destroy_graph(t);
     t.graph_split = split;
-    e = enqueue_tc(p, in, out, nullptr, nullptr, split);
+    e = enqueue_tc(p, t, nelem, in, out, nullptr, nullptr, split);
   } else {
     if (!t.graph_exec) {
       e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
-        cudaError_t eq = enqueue_tc(p, nullptr, nullptr, t.d_io, nullptr, split);
+        cudaError_t eq = enqueue_tc(p, t, nelem, nullptr, nullptr, t.d_io, nullptr, split);
         e = cudaStreamEndCapture(ctx->stream, &t.graph);
         if (e == cudaSuccess) e = eq;
       }
@@ -662,6 +737,28 @@ int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check
                                          std::to_string(herr) + ")");
   }
   return HH_OK;
+}
+
+int matvec_tc(hh_plan* p, const double2* in, double2* out, float* ms, bool check, int split) {
+  if (!p->tc.ready) {
+    int st = build_tc_plan(p);
+    if (st != HH_OK) return st;
+  }
+  return run_tc(p, p->tc, 1, in, out, ms, check, split);
+}
+
+int matvec_tc_batch(hh_plan* p, const double2* in, double2* out, int nb, bool check, int split) {
+  if (nb == 1) return matvec_tc(p, in, out, nullptr, check, split);
+  if (!p->tcb.ready || p->tcb_nb != nb) {
+    release_tc(p->ctx, p->tcb);
+    p->tcb_nb = 0;
+    int st = build_tc(p, p->tcb, nb);
+    if (st != HH_OK) return st;
+    p->tcb_nb = nb;
+    p->tcb.persistent1 = p->tc.persistent1;  // the launch choices tuned on the single-vector plan
+    p->tcb.persistent2 = p->tc.persistent2;
+  }
+  return run_tc(p, p->tcb, nb, in, out, nullptr, check, split);
 }
 
 // Times the launch variants of the tile GEMM (stage 1 / stage 2 on the
