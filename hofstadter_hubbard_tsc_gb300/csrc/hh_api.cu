@@ -823,14 +823,16 @@ int hh_plan_check(hh_plan_t* p) {
   hh_ctx* ctx = p->ctx;
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_check(ctx, e, "plan check");
-  if (!p->tc.ready) return HH_OK;
-  int herr = 0;
-  e = cudaMemcpy(&herr, p->tc.d_err, sizeof(int), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return cuda_check(ctx, e, "plan check");
-  if (herr) {
-    cudaMemset(p->tc.d_err, 0, sizeof(int));
-    return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
-                                         std::to_string(herr) + ")");
+  for (hh_tc_plan* t : {&p->tc, &p->tcb}) {  // the single-vector and the batch schedules
+    if (!t->ready) continue;
+    int herr = 0;
+    e = cudaMemcpy(&herr, t->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_check(ctx, e, "plan check");
+    if (herr) {
+      cudaMemset(t->d_err, 0, sizeof(int));
+      return fail(ctx, HH_ERR_TIMEOUT, "tensor-core matvec: a bounded mbarrier wait ran out (code " +
+                                           std::to_string(herr) + ")");
+    }
   }
   return HH_OK;
 }
