@@ -42,6 +42,7 @@ constexpr int kJacobiMaxN = 32;  // 32^2 complex doubles = 16 KiB of shared memo
 constexpr int kJacobiThreads = 256;
 constexpr int kJacobiMaxSweeps = 30;
 constexpr int kPool = 8;  // zheevd host threads, each with a stream and a solver handle
+constexpr int kBigCluster = 32;  // degenerate clusters this large go through Cholesky QR
 
 struct EigItem {
   long long off;   // n x n sector (column-major, ld n) in the density block
@@ -607,8 +608,15 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   cudaStream_t s = ctx->stream;
   cudaError_t e = cudaSuccess;
   std::vector<tri::InvItem> inv;
-  std::vector<tri::CgsBlock> cgs;
+  std::vector<tri::CgsBlock> cgs, cgs_low;
   std::vector<int2> clusters;
+  // clusters of at least kBigCluster columns (the null space of a
+  // rank-deficient sector, kept when kept_max exceeds its rank): the columns
+  // are projected off the later columns and orthonormalised by Cholesky QR,
+  // twice each, with the FP64 GEMM kernel; scratch W, G, R^{-1} at xoff
+  struct BigCl { long long zoff; int n, k, c0, c1; long long woff, goff, roff; };
+  std::vector<BigCl> bigs;
+  long long xtot = 0;
   std::vector<tri::BtItem> bt;
   std::vector<tri::PhaseItem> ph;
   struct Blk { long long zoff, goff; int n, k; };
@@ -632,15 +640,42 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
     // below 1e-13 ||T||): Gram-Schmidt within each before Newton-Schulz
     const double* wk = R.w.data() + R.woff[k];
     const double tn = std::max(std::fabs(wk[0]), std::fabs(wk[n - 1]));
-    const int cl_first = (int)clusters.size();
+    // clusters above the sector's large cluster (or all, without one) go
+    // through Gram-Schmidt before the large cluster's Cholesky QR, the ones
+    // below it after, so that every column a cluster is projected against
+    // is final
+    std::vector<int2> upper, lower;
+    bool big_here = false;
     for (int j1 = n; j1 > n - nc;) {  // from the top down
       int j0 = j1 - 1;
       while (j0 > n - nc && wk[j0] - wk[j0 - 1] <= 1e-13 * tn) --j0;
-      if (j1 - j0 > 1) clusters.push_back(make_int2(j0 - (n - nc), j1 - (n - nc)));
+      const int c0 = j0 - (n - nc), c1 = j1 - (n - nc), cw = c1 - c0;
+      // Cholesky QR (multi-SM GEMMs) instead of Gram-Schmidt for the topmost
+      // large cluster of a sector (a lower one would read columns that the
+      // same launches rewrite)
+      if (cw >= kBigCluster && !big_here) {
+        big_here = true;
+        BigCl b{zt, n, nc, c0, c1, 0, 0, 0};
+        b.woff = xtot;
+        xtot += (long long)(nc - c1) * cw;
+        b.goff = xtot;
+        xtot += (long long)cw * cw;
+        b.roff = xtot;
+        xtot += (long long)cw * cw;
+        bigs.push_back(b);
+      } else if (cw > 1) {
+        (big_here ? lower : upper).push_back(make_int2(c0, c1));
+      }
       j1 = j0;
     }
-    if ((int)clusters.size() > cl_first)
-      cgs.push_back(tri::CgsBlock{zt, n, nc, cl_first, (int)clusters.size() - cl_first});
+    if (!upper.empty()) {
+      cgs.push_back(tri::CgsBlock{zt, n, nc, (int)clusters.size(), (int)upper.size()});
+      clusters.insert(clusters.end(), upper.begin(), upper.end());
+    }
+    if (!lower.empty()) {
+      cgs_low.push_back(tri::CgsBlock{zt, n, nc, (int)clusters.size(), (int)lower.size()});
+      clusters.insert(clusters.end(), lower.begin(), lower.end());
+    }
     for (int c0 = 0; c0 < nc; c0 += tri::kBtCols)
       bt.push_back(tri::BtItem{q, c0, std::min(tri::kBtCols, nc - c0), nc, zt, xoff[k]});
     blks.push_back(Blk{zt, gt, n, nc});
@@ -678,17 +713,55 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
     }
   }
   const long long final_z = (kSteps % 2 == 1) ? zt : 0;
+  // Cholesky QR of the large clusters: item lists of its launches.  Z blocks
+  // are row-major (element (i, j) of a block at zoff + i k + j); T, the
+  // first pass's result, sits in the Newton-Schulz buffer's second half.
+  const long long xbase = 2 * zt + gt, tbase = zt;
+  std::vector<tri::GemmItem> projA, projB, gram1, app1, gram2, app2;
+  std::vector<tri::CholItem> chol;
+  int nt_projA = 0, nt_projB = 0, nt_gram1 = 0, nt_app1 = 0, nt_gram2 = 0, nt_app2 = 0;
+  auto item = [](std::vector<tri::GemmItem>& v, int& ntile, long long a, int a_r, int a_c, long long b, int b_r,
+                 int b_c, long long c, int c_r, int c_c, long long c0, int M, int N, int K, double alpha,
+                 double beta) {
+    if (M <= 0 || N <= 0 || K <= 0) return;
+    tri::GemmItem g{};
+    g.a = a; g.b = b; g.c = c; g.c0 = c0;
+    g.M = M; g.N = N; g.K = K;
+    g.a_r = a_r; g.a_c = a_c; g.b_r = b_r; g.b_c = b_c; g.c_r = c_r; g.c_c = c_c;
+    g.alpha = alpha; g.beta = beta;
+    g.tiles_n = (N + 63) / 64;
+    g.tile0 = ntile;
+    ntile += ((M + 63) / 64) * g.tiles_n;
+    v.push_back(g);
+  };
+  for (const BigCl& b : bigs) {
+    const int cw = b.c1 - b.c0, L = b.k - b.c1, k = b.k;
+    const long long zc = b.zoff + b.c0, zl = b.zoff + b.c1, w = xbase + b.woff, g = xbase + b.goff,
+                    r = xbase + b.roff, t = tbase + b.zoff + (long long)b.n * b.c0;
+    // W = Z_L^T Z_c, then Z_c -= Z_L W
+    item(projA, nt_projA, zl, 1, k, zc, k, 1, w, cw, 1, w, L, cw, b.n, 1.0, 0.0);
+    item(projB, nt_projB, zl, k, 1, w, cw, 1, zc, k, 1, zc, b.n, cw, L, -1.0, 1.0);
+    // G = Z_c^T Z_c, T = Z_c R^{-1}; G = T^T T, Z_c = T R^{-1}
+    item(gram1, nt_gram1, zc, 1, k, zc, k, 1, g, cw, 1, g, cw, cw, b.n, 1.0, 0.0);
+    item(app1, nt_app1, zc, k, 1, r, cw, 1, t, cw, 1, t, b.n, cw, cw, 1.0, 0.0);
+    item(gram2, nt_gram2, t, 1, cw, t, cw, 1, g, cw, 1, g, cw, cw, b.n, 1.0, 0.0);
+    item(app2, nt_app2, t, cw, 1, r, cw, 1, zc, k, 1, zc, b.n, cw, cw, 1.0, 0.0);
+    chol.push_back(tri::CholItem{g, r, cw, 0});
+  }
   const int nitems = (int)inv.size();
   size_t need = 0;
   {
     Carve c;
     c.take<tri::InvItem>(inv.size());
     c.take<double>((size_t)5 * maxn * std::max(1, nitems));
-    c.take<double>((size_t)(2 * zt + gt));
+    c.take<double>((size_t)(2 * zt + gt + xtot));
     for (auto& v : gi) c.take<tri::GemmItem>(v.size());
+    for (auto* v : {&projA, &projB, &gram1, &app1, &gram2, &app2}) c.take<tri::GemmItem>(v->size());
+    c.take<tri::CholItem>(chol.size());
     c.take<tri::BtItem>(bt.size());
     c.take<tri::PhaseItem>(ph.size());
     c.take<tri::CgsBlock>(cgs.size());
+    c.take<tri::CgsBlock>(cgs_low.size());
     c.take<int2>(clusters.size());
     need = c.off;
   }
@@ -698,26 +771,47 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   c.base = (char*)S->d_buf3;
   tri::InvItem* d_inv = c.take<tri::InvItem>(inv.size());
   double* d_lu = c.take<double>((size_t)5 * maxn * std::max(1, nitems));
-  double* d_z = c.take<double>((size_t)(2 * zt + gt));
+  double* d_z = c.take<double>((size_t)(2 * zt + gt + xtot));
   tri::GemmItem* d_gi[2 * kSteps];
   for (int q = 0; q < 2 * kSteps; ++q) d_gi[q] = c.take<tri::GemmItem>(gi[q].size());
+  std::vector<tri::GemmItem>* qr_lists[6] = {&projA, &projB, &gram1, &app1, &gram2, &app2};
+  tri::GemmItem* d_qr[6];
+  for (int q = 0; q < 6; ++q) d_qr[q] = c.take<tri::GemmItem>(qr_lists[q]->size());
+  tri::CholItem* d_chol = c.take<tri::CholItem>(chol.size());
   tri::BtItem* d_bt = c.take<tri::BtItem>(bt.size());
   tri::PhaseItem* d_ph = c.take<tri::PhaseItem>(ph.size());
   tri::CgsBlock* d_cgs = c.take<tri::CgsBlock>(cgs.size());
+  tri::CgsBlock* d_cgs_low = c.take<tri::CgsBlock>(cgs_low.size());
   int2* d_clusters = c.take<int2>(clusters.size());
   auto up = [&](void* dst, const void* src, size_t bytes) {
     if (e == cudaSuccess && bytes > 0) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   };
   up(d_inv, inv.data(), inv.size() * sizeof(tri::InvItem));
   for (int q = 0; q < 2 * kSteps; ++q) up(d_gi[q], gi[q].data(), gi[q].size() * sizeof(tri::GemmItem));
+  for (int q = 0; q < 6; ++q) up(d_qr[q], qr_lists[q]->data(), qr_lists[q]->size() * sizeof(tri::GemmItem));
+  up(d_chol, chol.data(), chol.size() * sizeof(tri::CholItem));
   up(d_bt, bt.data(), bt.size() * sizeof(tri::BtItem));
   up(d_ph, ph.data(), ph.size() * sizeof(tri::PhaseItem));
   up(d_cgs, cgs.data(), cgs.size() * sizeof(tri::CgsBlock));
+  up(d_cgs_low, cgs_low.data(), cgs_low.size() * sizeof(tri::CgsBlock));
   up(d_clusters, clusters.data(), clusters.size() * sizeof(int2));
   if (e != cudaSuccess) return cuda_check(ctx, e, "eigenvector work lists");
   if (nitems > 0) {
     e = tri::inverse_iteration(R.d_secs, d_inv, nitems, maxn, R.d_d, R.d_e, R.d_w, d_z, d_lu, s);
     if (e == cudaSuccess) e = tri::cgs2(d_cgs, (int)cgs.size(), d_clusters, maxk, d_z, s);
+    if (!bigs.empty()) {
+      for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+        e = tri::gemm(d_qr[0], (int)projA.size(), nt_projA, d_z, s);
+        if (e == cudaSuccess) e = tri::gemm(d_qr[1], (int)projB.size(), nt_projB, d_z, s);
+      }
+      if (e == cudaSuccess) e = tri::gemm(d_qr[2], (int)gram1.size(), nt_gram1, d_z, s);
+      if (e == cudaSuccess) e = tri::chol_inv(d_chol, (int)chol.size(), d_z, s);
+      if (e == cudaSuccess) e = tri::gemm(d_qr[3], (int)app1.size(), nt_app1, d_z, s);
+      if (e == cudaSuccess) e = tri::gemm(d_qr[4], (int)gram2.size(), nt_gram2, d_z, s);
+      if (e == cudaSuccess) e = tri::chol_inv(d_chol, (int)chol.size(), d_z, s);
+      if (e == cudaSuccess) e = tri::gemm(d_qr[5], (int)app2.size(), nt_app2, d_z, s);
+    }
+    if (e == cudaSuccess) e = tri::cgs2(d_cgs_low, (int)cgs_low.size(), d_clusters, maxk, d_z, s);
     for (int q = 0; q < 2 * kSteps && e == cudaSuccess; ++q) e = tri::gemm(d_gi[q], (int)gi[q].size(), ntiles[q], d_z, s);
     if (e == cudaSuccess) e = tri::backtransform(R.d_secs, d_bt, (int)bt.size(), R.A, R.d_tau, d_z + final_z, X, s);
     if (e != cudaSuccess) return cuda_check(ctx, e, "kept eigenvectors (inverse iteration)");

@@ -857,6 +857,64 @@ __global__ void cgs2_kernel(const CgsBlock* __restrict__ blocks, const int2* __r
   }
 }
 
+// --------------------------------------------------------------- chol_inv
+// One CTA per item: the upper Cholesky factor R of G + s I (in place in G's
+// upper triangle; s = 1e-14 trace(G) / c keeps a nearly singular Gram matrix
+// factorisable, the second Cholesky QR pass removes its effect), then
+// R^{-1} column by column (thread q solves R x = e_q backwards, four
+// independent partial sums against the FP64 latency).  Used by the Cholesky
+// QR of large clusters of degenerate kept eigenvalues (null spaces of
+// rank-deficient density matrices), where column-by-column Gram-Schmidt on
+// one CTA costs tens of milliseconds.
+__global__ void __launch_bounds__(512) chol_inv_kernel(const CholItem* __restrict__ items, double* __restrict__ buf) {
+  const CholItem it = items[blockIdx.x];
+  double* G = buf + it.g;
+  double* Ri = buf + it.r;
+  const int c = it.c;
+  __shared__ double s_shift, s_piv;
+  __shared__ double red[32];
+  double tr = 0.0;
+  for (int i = threadIdx.x; i < c; i += blockDim.x) tr += G[(long long)i * c + i];
+  tr = block_sum(tr, red);
+  if (threadIdx.x == 0) s_shift = 1e-14 * tr / (c > 0 ? c : 1) + DBL_MIN;
+  __syncthreads();
+  for (int i = threadIdx.x; i < c; i += blockDim.x) G[(long long)i * c + i] += s_shift;
+  __syncthreads();
+  for (int j = 0; j < c; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = G[(long long)j * c + j];
+      s_piv = sqrt(d > s_shift ? d : s_shift);
+    }
+    __syncthreads();
+    const double rjj = s_piv, inv = 1.0 / rjj;
+    for (int q = j + threadIdx.x; q < c; q += blockDim.x)
+      G[(long long)j * c + q] = q == j ? rjj : G[(long long)j * c + q] * inv;
+    __syncthreads();
+    const int m = c - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int p = j + 1 + e / m, q = j + 1 + e % m;
+      if (q >= p) G[(long long)p * c + q] = fma(-G[(long long)j * c + p], G[(long long)j * c + q], G[(long long)p * c + q]);
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < c; q += blockDim.x) {
+    for (int p = c - 1; p > q; --p) Ri[(long long)p * c + q] = 0.0;
+    Ri[(long long)q * c + q] = 1.0 / G[(long long)q * c + q];
+    for (int p = q - 1; p >= 0; --p) {
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int t = p + 1;
+      for (; t + 3 <= q; t += 4) {
+        a0 = fma(G[(long long)p * c + t], Ri[(long long)t * c + q], a0);
+        a1 = fma(G[(long long)p * c + t + 1], Ri[(long long)(t + 1) * c + q], a1);
+        a2 = fma(G[(long long)p * c + t + 2], Ri[(long long)(t + 2) * c + q], a2);
+        a3 = fma(G[(long long)p * c + t + 3], Ri[(long long)(t + 3) * c + q], a3);
+      }
+      for (; t <= q; ++t) a0 = fma(G[(long long)p * c + t], Ri[(long long)t * c + q], a0);
+      Ri[(long long)p * c + q] = -((a0 + a1) + (a2 + a3)) / G[(long long)p * c + p];
+    }
+  }
+}
+
 // ------------------------------------------------------------------- gemm
 constexpr int kTile = 64, kKc = 16, kGemmThreads = 256;
 
@@ -1141,6 +1199,12 @@ cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, const int2* d_clusters, 
                  cudaStream_t s) {
   if (nblocks <= 0) return cudaSuccess;
   cgs2_kernel<<<(unsigned)nblocks, 256, (size_t)maxk * sizeof(double), s>>>(d_blocks, d_clusters, Z);
+  return cudaGetLastError();
+}
+
+cudaError_t chol_inv(const CholItem* d_items, int nitems, double* buf, cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  chol_inv_kernel<<<(unsigned)nitems, 512, 0, s>>>(d_items, buf);
   return cudaGetLastError();
 }
 

@@ -61,6 +61,14 @@ struct CgsBlock {
   int cl0, ncl;
 };
 
+// One large cluster's Cholesky factor: G (c x c, row-major, symmetric) at g
+// becomes the upper factor R of G + s I (s = 1e-14 trace(G) / c); R^{-1} is
+// written at r (c x c, row-major).
+struct CholItem {
+  long long g, r;
+  int c, pad;
+};
+
 // A column range to put in the canonical phase.
 struct PhaseItem {
   long long off;   // first element of the first column
@@ -92,6 +100,9 @@ cudaError_t inverse_iteration(const Sector* d_secs, const InvItem* d_items, int 
 // CTA per block; clusters holds (c0, c1) column ranges
 cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, const int2* d_clusters, int maxk, double* Z,
                  cudaStream_t s);
+// R^{-1} of the Cholesky factor of each item's Gram matrix, one CTA per item
+// (orthonormalisation of large degenerate clusters by Cholesky QR)
+cudaError_t chol_inv(const CholItem* d_items, int nitems, double* buf, cudaStream_t s);
 // batched strided FP64 GEMMs, ntiles = total 64 x 64 tiles of the items
 cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s);
 // X = Q Z into the truncation operator

@@ -174,8 +174,10 @@ int hh_plan_stats(const hh_plan_t* p, double* counts);
 int hh_plan_free(hh_plan_t* p);
 
 /* model_wave (code/mat_vec.f90:3476): out = H in, device-resident waves;
- * waves holding nbatch vectors (hh_wave_create) are multiplied vector by
- * vector on the same plan (in and out must hold the same number).         */
+ * waves holding nbatch vectors (hh_wave_create; in and out must hold the
+ * same number): in split precision all of them in one batched replay (every
+ * stage one launch over the batch; the batch schedule is built on the first
+ * call for that nbatch and kept), in FP64 vector by vector.               */
 int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision);
 /* model_wave with host buffers: copies in, multiplies, copies out (device
  * buffers of the plan are reused between calls).                          */
