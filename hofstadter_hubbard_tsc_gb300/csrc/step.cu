@@ -434,20 +434,33 @@ extern "C" int hh_wave_transform(hh_ctx_t* ctx, int dir, const hh_basis_t* sys_b
       }
     }
   }
-  // stage 1: S = opA(A) old_region (M x Kb) per piece; stage 2: grouped by output rect
+  // stage 1: S = opA(A) old_region (M x Kb) per distinct (old sector, region,
+  // operator): the pieces that differ only in the new sector's spin (the
+  // nsd / ned loops above) share it; stage 2: grouped by output rect
   GemmRun G1, G2;
   long long scr = 0;
+  std::map<std::tuple<int, int, int, int, int, long long, int>, long long> s1_done;
   std::map<std::tuple<int, int, int, int, int>, std::vector<hh_seg>> rects;
   std::vector<std::tuple<int, int, int, int, int>> order;
   for (const Piece& q : P) {
     const hh_wsec& ow = old_wave->secs[q.i];
-    std::vector<hh_seg> s1{gemm_seg(q.a, HH_BASE_ABS, q.lda, q.opa, ow.off + (long long)q.icol * ow.sdim + q.irow,
-                                    HH_BASE_IN, ow.sdim, HH_OP_N, q.Ka)};
-    G1.add_rect(scr, HH_BASE_SCR, q.M, q.M, q.Kb, s1, 0);
+    const auto s1key = std::make_tuple(q.i, q.irow, q.icol, q.Ka, q.Kb, q.a, q.M);
+    long long soff;
+    auto found = s1_done.find(s1key);
+    if (found != s1_done.end()) {
+      soff = found->second;
+    } else {
+      std::vector<hh_seg> s1{gemm_seg(q.a, HH_BASE_ABS, q.lda, q.opa,
+                                      ow.off + (long long)q.icol * ow.sdim + q.irow, HH_BASE_IN, ow.sdim, HH_OP_N,
+                                      q.Ka)};
+      G1.add_rect(scr, HH_BASE_SCR, q.M, q.M, q.Kb, s1, 0);
+      soff = scr;
+      s1_done.emplace(s1key, soff);
+      scr += (long long)q.M * q.Kb;
+    }
     auto key = std::make_tuple(q.k, q.orow, q.ocol, q.M, q.N);
     if (!rects.count(key)) order.push_back(key);
-    rects[key].push_back(gemm_seg(scr, HH_BASE_SCR, q.M, HH_OP_N, q.b, HH_BASE_ABS, q.ldb, q.opb, q.Kb, q.c, 0.0));
-    scr += (long long)q.M * q.Kb;
+    rects[key].push_back(gemm_seg(soff, HH_BASE_SCR, q.M, HH_OP_N, q.b, HH_BASE_ABS, q.ldb, q.opb, q.Kb, q.c, 0.0));
   }
   for (const auto& key : order) {
     const auto& [k, orow, ocol, M, N] = key;
