@@ -307,9 +307,12 @@ def sweep_bench(dev, args):
                 d = GPUDMRG(dev, lat, 28, precision=prec, guess_hook=hook if name == "split" else None, **kw)
                 d.load(ckpt)
                 d.phase_s.clear()
+                import torch
+                torch.cuda.nvtx.range_push(f"sweep_{name}_m{m}")  # profiler filter for the timed sweep
                 t0 = time.perf_counter()
                 d.sweep()
                 dt = time.perf_counter() - t0
+                torch.cuda.nvtx.range_pop()
                 its = [r[3] for r in d.energies[-nstep:]]
                 out[name] = {"E0": d.energies[-1][2], "sweep_s": dt,
                              "lanczos_iterations": int(np.sum(its)), "lanzero": 1e-10,
