@@ -3,7 +3,7 @@
 // ascending.
 //
 // Default path (eig_values, then eig_vectors once the host has chosen the
-// kept states): sectors of up to kJacobiMaxN states are solved completely by
+// kept states): sectors of up to kJacobiOwnMaxN states are solved completely by
 // the Jacobi kernel below; larger ones go through the tridiagonal pipeline of
 // eig_tri.cu (cluster Householder reduction, bisection for every eigenvalue,
 // inverse iteration and back-transformation for the kept eigenvectors only).
@@ -39,6 +39,11 @@ namespace hh {
 namespace {
 
 constexpr int kJacobiMaxN = 32;  // 32^2 complex doubles = 16 KiB of shared memory
+// The own path hands sectors above 16 states to the tridiagonal pipeline: the
+// Jacobi kernel's per-round rotation parameters (a square root and divisions
+// in FP64) make a 32-state sector cost ~1.9 ms, against ~0.4 ms for the
+// cluster reduction (measured on the 2x16 ladder sweep at m = 256).
+constexpr int kJacobiOwnMaxN = 16;
 constexpr int kJacobiThreads = 256;
 constexpr int kJacobiMaxSweeps = 30;
 constexpr int kPool = 8;  // zheevd host threads, each with a stream and a solver handle
@@ -475,7 +480,7 @@ int eig_values(hh_ctx* ctx, double2* A, const std::vector<long long>& offs, cons
   std::vector<int> tri;
   for (size_t k = 0; k < ns; ++k) {
     const int n = dims[k];
-    const bool jac = n > 0 && n <= kJacobiMaxN && !force_tri;
+    const bool jac = n > 0 && n <= kJacobiOwnMaxN && !force_tri;
     items[k] = EigItem{offs[k], 0, nev, n, jac ? 1 : 0};
     R.woff[k] = nev;
     nev += n;

@@ -57,7 +57,7 @@ int hh_ctx_sync(hh_ctx_t* ctx);
 int hh_version(void);
 
 /* Eigensolver of the density-matrix sectors (hh_density_truncate), all FP64:
- * HH_EIG_OWN (default): the library's own kernels -- sectors of up to 32
+ * HH_EIG_OWN (default): the library's own kernels -- sectors of up to 16
  *   states by one-CTA Jacobi, larger ones by Householder reduction to a real
  *   tridiagonal on a thread-block cluster, bisection for every eigenvalue,
  *   and inverse iteration plus back-transformation for the kept

@@ -54,7 +54,7 @@ def test_density_truncate(device, side):
 @pytest.mark.parametrize("side", [0, 1])
 def test_density_truncate_sector_sizes(device, side):
     """Sector sizes on both sides of each switch of the eigensolver: its
-    Jacobi kernel (up to 32 states), the cluster reduction with the sector in
+    Jacobi kernel (up to 16 states), the cluster reduction with the sector in
     shared memory (up to about 600) and with the sector in place in global
     memory (700 here), with a spectrum decaying over many decades like a DMRG
     density matrix."""
