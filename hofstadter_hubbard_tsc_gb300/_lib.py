@@ -17,6 +17,7 @@ HH_ERR_TIMEOUT, HH_ERR_NUMERIC, HH_ERR_UNSUPPORTED = -5, -6, -7
 HH_PREC_FP64 = 0
 HH_PREC_BF16X6 = 1  # three BF16 parts, six products: ~2^-24 per product
 HH_PREC_BF16X3 = 2  # two BF16 parts, three products: ~2^-16 per product
+HH_PREC_FP32 = 3  # FP32 arithmetic: the wave transform's guess only (hh_ctx_set_transform_precision)
 HH_EIG_OWN, HH_EIG_CUSOLVER = 0, 1  # density-matrix eigensolver (hh_ctx_set_eigensolver)
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
@@ -66,6 +67,7 @@ SIGNATURES = {
     "hh_ctx_sync": (I, [P]),
     "hh_version": (I, []),
     "hh_ctx_set_eigensolver": (I, [P, I]),
+    "hh_ctx_set_transform_precision": (I, [P, I]),
     "hh_eig_selftest": (I, [P, I, DP, DP, DP]),
     "hh_block_create": (I, [P, I, I, I, I, IP, DP, PP]),
     "hh_block_zeros": (I, [P, I, I, I, I, IP, PP]),

@@ -9,6 +9,8 @@
 // in slot order by seg_reduce_kernel.
 #include "hh_internal.h"
 
+#include <type_traits>
+
 namespace hh {
 
 namespace {
@@ -29,6 +31,11 @@ __device__ __forceinline__ const double2* resolve(long long off, int base, const
   }
 }
 
+// F32: the same products with FP32 arithmetic (inputs rounded to FP32 as they
+// are staged, outputs widened to FP64): for results that only start an
+// iteration, where GB300's FP32 pipe (64 times the FP64 rate) is worth the
+// 2^-24 rounding.
+template <bool F32>
 __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __restrict__ tiles,
                                                           const hh_seg* __restrict__ segs,
                                                           const double2* __restrict__ bin,
@@ -36,8 +43,11 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
                                                           double2* __restrict__ bout,
                                                           double2* __restrict__ part,
                                                           long long sin, long long sscr, long long sout) {
-  __shared__ double2 Ps[TK][TM + 1];
-  __shared__ double2 Qs[TK][TN + 1];
+  using V = typename std::conditional<F32, float2, double2>::type;
+  using R = typename std::conditional<F32, float, double>::type;
+  auto narrow = [](double2 v) { V r; r.x = (R)v.x; r.y = (R)v.y; return r; };
+  __shared__ V Ps[TK][TM + 1];
+  __shared__ V Qs[TK][TN + 1];
   const hh_tile t = tiles[blockIdx.x];
   const int b = blockIdx.y;
   const double2* in = bin + (long long)b * sin;
@@ -46,11 +56,11 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int mrem = min(TM, t.M - t.m0), nrem = min(TN, t.N - t.n0);
-  double2 acc[4][4];
+  V acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+    for (int j = 0; j < 4; ++j) acc[i][j].x = acc[i][j].y = (R)0;
 
   for (int si = 0; si < t.nseg; ++si) {
     const hh_seg s = segs[t.seg0 + si];
@@ -65,8 +75,8 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
           if (r < mrem && q < nrem) {
             double2 v = P[(long long)(t.m0 + r) + (long long)(t.n0 + q) * s.ldp];
             double2 cv = cmul(c, v);
-            acc[i][j].x += cv.x;
-            acc[i][j].y += cv.y;
+            acc[i][j].x += (R)cv.x;
+            acc[i][j].y += (R)cv.y;
           }
         }
       continue;
@@ -90,7 +100,7 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
           }
           v = cmul(c, v);
         }
-        Ps[kk][m] = v;
+        Ps[kk][m] = narrow(v);
       }
 #pragma unroll
       for (int r = 0; r < (TN * TK) / NT; ++r) {
@@ -106,12 +116,12 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
             if (s.opQ == HH_OP_C) v.y = -v.y;
           }
         }
-        Qs[kk][n] = v;
+        Qs[kk][n] = narrow(v);
       }
       __syncthreads();
 #pragma unroll 4
       for (int kk = 0; kk < TK; ++kk) {
-        double2 a[4], bb[4];
+        V a[4], bb[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) a[i] = Ps[kk][ty * 4 + i];
 #pragma unroll
@@ -135,7 +145,7 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) S[(ty * 4 + i) + (tx * 4 + j) * TM] = acc[i][j];
+      for (int j = 0; j < 4; ++j) S[(ty * 4 + i) + (tx * 4 + j) * TM] = make_double2(acc[i][j].x, acc[i][j].y);
     return;
   }
   double2* O = (t.obase == HH_BASE_SCR) ? scr : out;
@@ -149,11 +159,11 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
         long long idx = (long long)(t.m0 + r) + (long long)(t.n0 + q) * t.ldo;
         if (t.accumulate) {
           double2 o = O[idx];
-          o.x += acc[i][j].x;
-          o.y += acc[i][j].y;
+          o.x += (double)acc[i][j].x;
+          o.y += (double)acc[i][j].y;
           O[idx] = o;
         } else {
-          O[idx] = acc[i][j];
+          O[idx] = make_double2(acc[i][j].x, acc[i][j].y);
         }
       }
     }
@@ -376,11 +386,16 @@ cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, c
 }
 
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
-                                     double2* base_out, cudaStream_t s) {
+                                     double2* base_out, cudaStream_t s, bool fp32) {
   if (L.n_work == 0) return cudaSuccess;
   // grid.x = work tiles; the 65535 limit applies to grid.y only
   dim3 grid((unsigned)L.n_work, 1);
-  seg_gemm_fp64_kernel<<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part, 0, 0, 0);
+  if (fp32)
+    seg_gemm_fp64_kernel<true><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part, 0, 0,
+                                                   0);
+  else
+    seg_gemm_fp64_kernel<false><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part, 0,
+                                                    0, 0);
   if (L.n_red > 0) seg_reduce_kernel<<<(unsigned)L.n_red, NT, 0, s>>>(L.d_reds, L.d_part, base_scr, base_out);
   return cudaGetLastError();
 }
@@ -390,7 +405,7 @@ cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, do
 // launch reserves no device memory for their code.
 cudaError_t preload_segment_gemm_fp64() {
   cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, seg_gemm_fp64_kernel);
+  cudaError_t e = cudaFuncGetAttributes(&a, seg_gemm_fp64_kernel<false>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, seg_reduce_kernel);
   return e;
 }

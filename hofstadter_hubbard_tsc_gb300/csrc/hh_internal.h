@@ -49,6 +49,9 @@ struct hh_ctx {
   // (HH_EIG_OWN or HH_EIG_CUSOLVER)
   void* eig = nullptr;
   int eig_solver = 0;
+  // arithmetic of hh_wave_transform's products: HH_PREC_FP64 (default) or
+  // HH_PREC_FP32 (the transformed wave only starts Lanczos)
+  int transform_precision = 0;
   // device address of the static scratch array of hh_matvec_noalloc, looked
   // up by hh_init in this context (noalloc.cu); null with a reason if that
   // lookup failed
@@ -259,7 +262,7 @@ int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what);
 void noalloc_setup(hh_ctx* ctx);
 // grouped segment GEMM (FP64); bases[4] = {abs(unused), in, scr, out}
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
-                                     double2* base_out, cudaStream_t s);
+                                     double2* base_out, cudaStream_t s, bool fp32 = false);
 // loads the segment GEMM kernels into the current context (gemm_fp64.cu)
 cudaError_t preload_segment_gemm_fp64();
 // wave vector kernels

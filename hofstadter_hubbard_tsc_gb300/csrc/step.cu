@@ -25,9 +25,9 @@ struct GemmRun {
   hh_gemm_list L;
   // queued on the context stream; the task list returns to the pool in
   // stream order, so nothing here waits for the device
-  int run(hh_ctx* ctx, double2* base_in, double2* base_scr, double2* base_out) {
+  int run(hh_ctx* ctx, double2* base_in, double2* base_scr, double2* base_out, bool fp32 = false) {
     L.upload(ctx);
-    cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream);
+    cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream, fp32);
     L.release();
     return cuda_check(ctx, e, "step GEMM");
   }
@@ -249,6 +249,12 @@ extern "C" int hh_density_truncate(hh_ctx_t* ctx, const hh_wave_t* psi, int side
 extern "C" int hh_ctx_set_eigensolver(hh_ctx_t* ctx, int solver) {
   if (!ctx || (solver != HH_EIG_OWN && solver != HH_EIG_CUSOLVER)) return HH_ERR_INVALID;
   ctx->eig_solver = solver;
+  return HH_OK;
+}
+
+extern "C" int hh_ctx_set_transform_precision(hh_ctx_t* ctx, int precision) {
+  if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32)) return HH_ERR_INVALID;
+  ctx->transform_precision = precision;
   return HH_OK;
 }
 
@@ -474,8 +480,9 @@ extern "C" int hh_wave_transform(hh_ctx_t* ctx, int dir, const hh_basis_t* sys_b
     dev_free(ctx, d_scr);
     return cuda_check(ctx, e, "wave transform scratch");
   }
-  int st = G1.run(ctx, old_wave->d, d_scr, new_wave->d);
-  if (!st) st = G2.run(ctx, old_wave->d, d_scr, new_wave->d);
+  const bool fp32 = ctx->transform_precision == HH_PREC_FP32;
+  int st = G1.run(ctx, old_wave->d, d_scr, new_wave->d, fp32);
+  if (!st) st = G2.run(ctx, old_wave->d, d_scr, new_wave->d, fp32);
   dev_free(ctx, d_scr);
   if (st) return st;
   return hh_wave_normalize(new_wave);

@@ -679,6 +679,7 @@ static cudaError_t enqueue_tc(hh_plan* p, hh_tc_plan& t, long long nelem, const 
   if (e == cudaSuccess)
     e = tc_run_tiles(tiles2 + t.n_narrow2, t.n_tiles2 - t.n_narrow2, t.d_segs, out, t.d_err, t.persistent2, s,
                      io, 128, split);
+  if (ev) cudaEventRecord(ev[4], s);
   if (e == cudaSuccess && t.n_c_blocks > 0)
     e = tc_copy_terms(t.d_tiles2, t.d_c_blocks, t.n_c_blocks, t.d_csegs, in, out, s, io);
   if (ev) cudaEventRecord(ev[3], s);
@@ -692,17 +693,17 @@ static int run_tc(hh_plan* p, hh_tc_plan& t, int nb, const double2* in, double2*
   cudaError_t e = cudaSuccess;
   if (ms) {
     // eager launches with events between the stages
-    cudaEvent_t ev[4];
-    for (int i = 0; i < 4; ++i) cudaEventCreate(&ev[i]);
+    cudaEvent_t ev[5];  // start, images done, stage 1 done, end, stage-2 tiles done
+    for (int i = 0; i < 5; ++i) cudaEventCreate(&ev[i]);
     e = enqueue_tc(p, t, nelem, in, out, nullptr, ev, split);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
     if (e == cudaSuccess) {
       cudaEventElapsedTime(&ms[0], ev[0], ev[3]);
       cudaEventElapsedTime(&ms[1], ev[1], ev[2]);
-      cudaEventElapsedTime(&ms[2], ev[2], ev[3]);
+      cudaEventElapsedTime(&ms[2], ev[2], ev[4]);
       cudaEventElapsedTime(&ms[3], ev[0], ev[1]);
     }
-    for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+    for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
   } else if (t.calls++ == 0 || split != t.graph_split) {
     // the first call at a split runs eagerly (and initialises the kernels'
     // attributes); the graph is captured again at the new split next time

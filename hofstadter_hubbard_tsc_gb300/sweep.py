@@ -234,6 +234,14 @@ class GPUDMRG:
         self.last_trunc = (ns, err, ent)
         return trun
 
+    def _wave_trans(self, direction, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave):
+        """wave_trans_LR / wave_trans_RL: in a split-precision run the
+        transformed guess (it only starts Lanczos) is formed with FP32
+        arithmetic, in an FP64 run with FP64 as in the reference."""
+        self.dev.check(self.dev.lib.hh_ctx_set_transform_precision(
+            self.dev.h, _lib.HH_PREC_FP64 if self.precision == _lib.HH_PREC_FP64 else _lib.HH_PREC_FP32))
+        wave_trans(self.dev, direction, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave)
+
     # ---------------------------------------------------------------- sweeps
     def warm_up(self):
         """warm_up_point(1, N/2) (code/warm_up.f90:1284-1491)."""
@@ -280,7 +288,7 @@ class GPUDMRG:
             self.guess_kind = "previous"
         elif self.wave is not None:
             wv = self._new_wave(sup)
-            wave_trans(self.dev, "LR", dsys_bs, self.env_bases[N - label][1], self.sys_truns[label],
+            self._wave_trans("LR", dsys_bs, self.env_bases[N - label][1], self.sys_truns[label],
                        self.env_truns[N - label - 1], self.wave[0], wv)
             self.guess_kind = "transformed"
         else:
@@ -301,7 +309,7 @@ class GPUDMRG:
             sup = self._super(sys_bs, env_bs, self.n_elec, 0)
             wv = self._new_wave(sup)
             with self._phase("transform"):
-                wave_trans(self.dev, "LR", dsys_bs, self.env_bases[N - label][1], strun,
+                self._wave_trans("LR", dsys_bs, self.env_bases[N - label][1], strun,
                            self.env_truns[N - label - 1], self.wave[0], wv)
             self.guess_kind = "transformed"
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)
@@ -327,7 +335,7 @@ class GPUDMRG:
             self.guess_kind = "previous"
         elif self.wave is not None:
             wv = self._new_wave(sup)
-            wave_trans(self.dev, "RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label],
+            self._wave_trans("RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label],
                        self.env_truns[N - label - 1], self.wave[0], wv)
             self.guess_kind = "transformed"
         else:
@@ -348,7 +356,7 @@ class GPUDMRG:
             geo = self.lat.geometry(sys.len, env.len)
             wv = self._new_wave(sup)
             with self._phase("transform"):
-                wave_trans(self.dev, "RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label], etrun,
+                self._wave_trans("RL", self.sys_bases[label + 1][1], denv_bs, self.sys_truns[label], etrun,
                            self.wave[0], wv)
             self.guess_kind = "transformed"
             self._solve(sys, env, sys_bs, env_bs, geo, sup, wv)

@@ -39,6 +39,9 @@ extern "C" {
                                  FP32 accumulate (tcgen05): ~2^-24 per product    */
 #define HH_PREC_BF16X3 2      /* two BF16 parts, three products (x0y0 + x0y1 +
                                  x1y0), FP32 accumulate: ~2^-16 per product       */
+#define HH_PREC_FP32 3        /* complex FP32 on the CUDA cores (the wave
+                                 transform's guess only, hh_ctx_set_transform_
+                                 precision)                                       */
 
 typedef struct hh_ctx hh_ctx_t;
 typedef struct hh_block hh_block_t;
@@ -67,6 +70,12 @@ int hh_version(void);
 #define HH_EIG_OWN 0
 #define HH_EIG_CUSOLVER 1
 int hh_ctx_set_eigensolver(hh_ctx_t* ctx, int solver);
+/* Arithmetic of hh_wave_transform's products: HH_PREC_FP64 (default, the
+ * reference's ZGEMM) or HH_PREC_FP32 (inputs rounded to FP32, FP32
+ * accumulation, FP64 result).  The transformed wave only starts the next
+ * Lanczos, so a split-precision sweep can take the 2^-24 rounding for
+ * GB300's FP32 rate (64x its FP64 rate).  No counterpart in the reference. */
+int hh_ctx_set_transform_precision(hh_ctx_t* ctx, int precision);
 /* Diagnostic: every eigenpair of one dense Hermitian matrix A (n x n,
  * column-major, interleaved complex) through the tridiagonal pipeline of
  * HH_EIG_OWN (whatever n): w ascending (n doubles), V the eigenvectors
@@ -183,8 +192,10 @@ int hh_matvec(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision);
  * buffers of the plan are reused between calls).                          */
 int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision);
 /* hh_matvec with CUDA events on the context stream around each stage;
- * ms[0] = whole matvec, ms[1] = stage 1 (left products), ms[2] = stage 2,
- * ms[3] = BF16 split of the input wave (split-precision path only).     */
+ * ms[0] = whole matvec, ms[1] = stage 1 (left products), ms[2] = stage 2
+ * (its tile kernel; the site-diagonal copy terms that follow are the rest of
+ * ms[0]), ms[3] = BF16 split of the input wave (split-precision path
+ * only).                                                                  */
 int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int precision, float* ms);
 
 /* hh_matvec (FP64) that allocates nothing during the call.  No counterpart

@@ -9,7 +9,7 @@ from oracle.density import get_density_matrix_sys, get_density_matrix_env, get_t
 from oracle.blocks import update_trun_ndia, update_trun_dia
 from oracle.lattice import Lattice
 from hofstadter_hubbard_tsc_gb300.device import DBlock, DBasis, DWave
-from hofstadter_hubbard_tsc_gb300 import step
+from hofstadter_hubbard_tsc_gb300 import _lib, step
 from tests import helpers as H
 
 pytestmark = pytest.mark.gpu
@@ -137,6 +137,15 @@ def test_wave_transform(device, monkeypatch):
         direction = "LR" if name.endswith("lr") else "RL"
         dold = _dwave(device, old)
         dnew = DWave(device, H.wave(new).layout(), new.sys_len, new.env_len)
-        step.wave_trans(device, direction, DBasis(device, H.basis(sbs)), DBasis(device, H.basis(ebs)),
-                        DBlock.upload(device, H.block(strun)), DBlock.upload(device, H.block(etrun)), dold, dnew)
+        args = (DBasis(device, H.basis(sbs)), DBasis(device, H.basis(ebs)), DBlock.upload(device, H.block(strun)),
+                DBlock.upload(device, H.block(etrun)), dold, dnew)
+        step.wave_trans(device, direction, *args)
         np.testing.assert_allclose(dnew.download(), H.wave(new).flat(), atol=1e-12)
+        # the FP32-arithmetic transform of split-precision runs (a Lanczos start
+        # vector): within FP32 rounding of the FP64 result, then back to FP64
+        device.check(device.lib.hh_ctx_set_transform_precision(device.h, _lib.HH_PREC_FP32))
+        step.wave_trans(device, direction, *args)
+        device.check(device.lib.hh_ctx_set_transform_precision(device.h, _lib.HH_PREC_FP64))
+        ref = H.wave(new).flat()
+        assert np.linalg.norm(dnew.download() - ref) <= 1e-6 * np.linalg.norm(ref)
+    assert device.lib.hh_ctx_set_transform_precision(device.h, _lib.HH_PREC_BF16X3) == -1
