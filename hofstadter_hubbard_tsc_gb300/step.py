@@ -5,6 +5,7 @@ import ctypes as C
 
 import numpy as np
 
+from . import _lib
 from .device import DBlock
 
 SYS, ENV = 0, 1
@@ -31,9 +32,14 @@ def update_trun(dev, op, trun, dia):
     return DBlock.from_handle(dev, h)
 
 
-def wave_trans(dev, direction, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave):
-    """wave_trans_LR (direction 'LR') / wave_trans_RL ('RL') into new_wave (normalised)."""
+def wave_trans(dev, direction, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave, precision=_lib.HH_PREC_FP64):
+    """wave_trans_LR (direction 'LR') / wave_trans_RL ('RL') into new_wave (normalised).
+
+    precision: HH_PREC_FP64 (the reference's arithmetic) or HH_PREC_FP32 (the
+    Lanczos start vector of a split-precision sweep); it is set on the context
+    for every call, so no earlier call's choice carries over."""
     d = 0 if direction == "LR" else 1
+    dev.check(dev.lib.hh_ctx_set_transform_precision(dev.h, int(precision)))
     dev.check(dev.lib.hh_wave_transform(dev.h, d, sys_bs.h, env_bs.h, sys_trun.h, env_trun.h, old_wave.h,
                                         new_wave.h))
     return new_wave

@@ -238,9 +238,8 @@ class GPUDMRG:
         """wave_trans_LR / wave_trans_RL: in a split-precision run the
         transformed guess (it only starts Lanczos) is formed with FP32
         arithmetic, in an FP64 run with FP64 as in the reference."""
-        self.dev.check(self.dev.lib.hh_ctx_set_transform_precision(
-            self.dev.h, _lib.HH_PREC_FP64 if self.precision == _lib.HH_PREC_FP64 else _lib.HH_PREC_FP32))
-        wave_trans(self.dev, direction, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave)
+        wave_trans(self.dev, direction, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave,
+                   _lib.HH_PREC_FP64 if self.precision == _lib.HH_PREC_FP64 else _lib.HH_PREC_FP32)
 
     # ---------------------------------------------------------------- sweeps
     def warm_up(self):

@@ -143,9 +143,7 @@ def test_wave_transform(device, monkeypatch):
         np.testing.assert_allclose(dnew.download(), H.wave(new).flat(), atol=1e-12)
         # the FP32-arithmetic transform of split-precision runs (a Lanczos start
         # vector): within FP32 rounding of the FP64 result, then back to FP64
-        device.check(device.lib.hh_ctx_set_transform_precision(device.h, _lib.HH_PREC_FP32))
-        step.wave_trans(device, direction, *args)
-        device.check(device.lib.hh_ctx_set_transform_precision(device.h, _lib.HH_PREC_FP64))
+        step.wave_trans(device, direction, *args, precision=_lib.HH_PREC_FP32)
         ref = H.wave(new).flat()
         assert np.linalg.norm(dnew.download() - ref) <= 1e-6 * np.linalg.norm(ref)
     assert device.lib.hh_ctx_set_transform_precision(device.h, _lib.HH_PREC_BF16X3) == -1
