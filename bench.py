@@ -551,7 +551,7 @@ def run_c5(args, local):
         t64 = time.perf_counter() - t0
         h64 = sb.w_out.download()
         errs[b] = float(np.linalg.norm(got[b] - h64) / np.linalg.norm(h64))
-    counts = np.zeros(20)
+    counts = np.zeros(_lib.HH_PLAN_STATS)
     dev.check(dev.lib.hh_plan_stats(sb.plan, counts.ctypes.data_as(C.POINTER(C.c_double))))
     peaks = measured_peaks()
     nprod = 6 if prec == _lib.HH_PREC_BF16X6 else 3
@@ -667,8 +667,9 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
     ms = (C.c_float * 4)()
 
-    # launch autotuner (split precision): stage 1 / stage 2 persistent or per tile
-    tune_ms, tune_choice = np.zeros(4), C.c_int(0)
+    # schedule autotuner (split precision): stage-2 tile shape x stage 1 / stage 2
+    # persistent or per tile
+    tune_ms, tune_choice = np.zeros(_lib.HH_TUNE_VARIANTS), C.c_int(0)
     t0 = time.perf_counter()
     dev.check(dev.lib.hh_plan_tune(sb.plan, prec, 3, tune_ms.ctypes.data_as(C.POINTER(C.c_double)),
                                    C.byref(tune_choice)))
@@ -745,7 +746,7 @@ def main():
     peaks = measured_peaks()
     stage = 1 if s1 >= s2 else 2
     t_stage = (s1 if stage == 1 else s2) / args.steps * 1e-3
-    counts = np.zeros(20)
+    counts = np.zeros(_lib.HH_PLAN_STATS)
     dev.check(dev.lib.hh_plan_stats(sb.plan, counts.ctypes.data_as(dp)))
     flops_stage = counts[8] if stage == 1 else counts[9]
     achieved = flops_stage / t_stage / 1e12
@@ -769,6 +770,16 @@ def main():
         issued = (counts[12] if stage == 1 else counts[13]) * (1.0 if prec == _lib.HH_PREC_BF16X6 else 0.5)
         roofline["bf16_flops_issued_per_launch"] = issued
         roofline["tensor_pipe_frac_of_measured_bf16"] = issued / t_stage / 1e12 / peaks["bf16_tflops"]
+        if stage == 2:
+            # the tile list's own MMA floor: its MMA cycles (max(45, width/2)
+            # per K = 16 MMA, measured) spread evenly over every SM's tensor core
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            mhz = (clk or {}).get("sm_mhz") or 2070.0
+            cyc = counts[22] * (2.0 if prec == _lib.HH_PREC_BF16X6 else 1.0)
+            floor_ms = cyc / sms / (mhz * 1e6) * 1e3
+            roofline["stage2_tiles"] = {"tiles": int(counts[20]), "stacked": int(counts[21]),
+                                        "tile_shape": int(counts[23]), "mma_cycle_floor_ms": floor_ms,
+                                        "kernel_over_floor": t_stage * 1e3 / floor_ms if floor_ms else None}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True,
@@ -781,7 +792,7 @@ def main():
                                              "matvec_launch": ("one CUDA-graph replay per step (hh_matvec_async)"
                                                                if prec != _lib.HH_PREC_FP64 else "eager"),
                                              "autotune": ({"variants_ms": [round(x, 4) for x in tune_ms],
-                                                           "variant_index": "2*stage1_persistent+stage2_persistent",
+                                                           "variant_index": "4*stage2_tile_shape+2*stage1_persistent+stage2_persistent",
                                                            "chosen": int(tune_choice.value), "tune_s": round(tune_s, 3)}
                                                           if prec != _lib.HH_PREC_FP64 else None),
                                              "ref_gflop_per_matvec": counts[0] / 1e9,

@@ -19,6 +19,8 @@ HH_PREC_BF16X6 = 1  # three BF16 parts, six products: ~2^-24 per product
 HH_PREC_BF16X3 = 2  # two BF16 parts, three products: ~2^-16 per product
 HH_PREC_FP32 = 3  # FP32 arithmetic: the wave transform's guess only (hh_ctx_set_transform_precision)
 HH_EIG_OWN, HH_EIG_CUSOLVER = 0, 1  # density-matrix eigensolver (hh_ctx_set_eigensolver)
+HH_TILE_SHAPES, HH_TUNE_VARIANTS = 4, 16  # stage-2 tile shapes / timings of hh_plan_tune
+HH_PLAN_STATS = 24  # doubles written by hh_plan_stats
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory",
           -4: "quantum number mismatch", -5: "bounded device wait timed out",
@@ -94,6 +96,7 @@ SIGNATURES = {
     "hh_matvec_host": (I, [P, DP, DP, I]),
     "hh_lanczos": (I, [P, P, D, I, I, DP, IP]),
     "hh_plan_tune": (I, [P, I, I, DP, IP]),
+    "hh_plan_set_tiles": (I, [P, I]),
     "hh_matvec_async": (I, [P, P, P, I]),
     "hh_plan_check": (I, [P]),
     "hh_matvec_timed": (I, [P, P, P, I, C.POINTER(C.c_float)]),

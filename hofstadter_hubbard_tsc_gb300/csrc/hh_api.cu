@@ -702,6 +702,10 @@ int hh_plan_stats(const hh_plan_t* p, double* c) {
           (p->tc.n_narrow2 > 0) + (p->tc.n_tiles2 > p->tc.n_narrow2);
   c[18] = (double)(p->stage1.n_work + p->stage2.n_work);
   c[19] = p->tc.persistent1 ? 1.0 : 0.0;
+  c[20] = (double)p->tc.n_tiles2;
+  c[21] = (double)p->tc.n_stacked2;
+  c[22] = p->tc.mma_cycles2;
+  c[23] = (double)p->tc_shape;
   return HH_OK;
 }
 
@@ -845,8 +849,18 @@ int hh_plan_tune(hh_plan_t* p, int precision, int reps, double* ms, int* choice)
   }
   if (!split_of(precision)) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
   int st = tune_tc_plan(p, reps, ms, split_of(precision));
-  if (st == HH_OK && choice) *choice = 2 * (int)p->tc.persistent1 + (int)p->tc.persistent2;
+  if (st == HH_OK && choice) *choice = 4 * p->tc_shape + 2 * (int)p->tc.persistent1 + (int)p->tc.persistent2;
   return st;
+}
+
+int hh_plan_set_tiles(hh_plan_t* p, int shape) {
+  if (!p || shape < 0 || shape >= HH_TILE_SHAPES) return HH_ERR_INVALID;
+  if (shape == p->tc_shape) return HH_OK;
+  cudaError_t e = cudaStreamSynchronize(p->ctx->stream);  // no replay of the old schedule in flight
+  if (e != cudaSuccess) return cuda_check(p->ctx, e, "hh_plan_set_tiles");
+  release_tc_plan(p);
+  p->tc_shape = shape;
+  return HH_OK;
 }
 
 int hh_host_alloc(long long bytes, void** ptr) {

@@ -227,6 +227,8 @@ struct hh_tc_plan {
   bool persistent1 = true, persistent2 = false;
   double bytes_op = 0, bytes_x = 0, bytes_t = 0;
   double mma_flops1 = 0, mma_flops2 = 0;  // tensor FLOPs issued (bf16), padding included
+  int n_stacked2 = 0;                     // stage-2 tiles of at most 64 rows (stacked MMAs)
+  double mma_cycles2 = 0;                 // stage-2 MMA cycles at BF16x3 (summed over tiles)
 };
 
 struct hh_plan {
@@ -235,6 +237,7 @@ struct hh_plan {
   hh_tc_plan tc;
   hh_tc_plan tcb;  // the schedule of a batch of tcb_nb vectors (hh_matvec on a wave of several vectors)
   int tcb_nb = 0;
+  int tc_shape = 0;  // row split of the stage-2 tiles (tc_plan.cpp; chosen by hh_plan_tune)
   const hh_wave* layout = nullptr;
   long long nelem = 0;
   hh_gemm_list stage1, stage2;

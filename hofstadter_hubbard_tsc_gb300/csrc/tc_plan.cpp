@@ -209,14 +209,20 @@ static int build_tc(hh_plan* p, hh_tc_plan& tp, int nb) {
   // (bits 60-61 of an address mark its arena: 0 operators, 1 wave, 2 T)
   auto tag = [](long long off, int arena) { return off | ((long long)arena << 60); };
   double mma1 = 0.0, mma2 = 0.0;
-  auto make_seg = [&](long long a, const ImgRef& ai, int m0, long long b, const ImgRef& bi, int n0, int ntile) {
+  // A rows [m0, m0 + mrows) (mrows <= 128, m0 a multiple of 8): a tile that
+  // reaches the end of its A image copies the image's padding too (a tile
+  // spanning the whole image then loads all planes of a chunk at once),
+  // others whole 8-row groups
+  auto make_seg = [&](long long a, const ImgRef& ai, int m0, long long b, const ImgRef& bi, int n0, int ntile,
+                      int mrows = 128) {
     tc::Seg s{};
     const int ar = rpad(ai.rows), br = rpad(bi.rows);
     s.a = a + (long long)(m0 / 8) * 256;
     s.b = b + (long long)(n0 / 8) * 256;
     s.a_plane = (long long)(ar / 8) * 256;
     s.b_plane = (long long)(br / 8) * 256;
-    s.a_bytes = std::min(128, ar - m0) * 32;
+    const int arows = m0 + mrows >= ai.rows ? ar - m0 : std::min(((mrows + 7) & ~7), ar - m0);
+    s.a_bytes = std::min(128, arows) * 32;
     s.b_bytes = std::min(ntile, br - n0) * 32;
     s.nkc = k16(ai.kc) / 16;
     return s;
@@ -377,14 +383,45 @@ static int build_tc(hh_plan* p, hh_tc_plan& tp, int nb) {
       it->second.push_back(ci);
     }
   }
+  // Tile shape of an output rectangle (hh_plan::tc_shape): 0, tiles of 128
+  // rows; 1, every rectangle in near-equal tiles of at most 64 rows (stacked:
+  // one MMA of width 2 ntile per part pair, 45-64 cycles for 64 rows, against
+  // four of width ntile, 4 x 45 cycles for 128 rows, at the price of one more
+  // read of the B panel per 64 rows); 2, tiles of 128 rows whose remainders
+  // of 65-127 rows go to two stacked tiles; 3, tiles of 128 rows and up to
+  // 128 columns (the 128-wide kernel, one CTA per SM: half the A reads per
+  // output, no second CTA to hide an epilogue).  Shapes 0-2 are at most 64
+  // wide.  The plan autotuner picks.
+  const int shape = p->tc_shape;
+  const int tn2 = shape == 3 ? 128 : kTileN;
+  auto row_split = [shape](int M) {
+    std::vector<std::pair<int, int>> r;  // (m0, rows)
+    auto stacked = [&r](int m0, int rows) {
+      const int nt = (rows + 63) / 64;
+      const int per = ((rows + nt - 1) / nt + 7) & ~7;
+      for (int a = 0; a < rows; a += per) r.emplace_back(m0 + a, std::min(per, rows - a));
+    };
+    if (shape == 1) {
+      stacked(0, M);
+      return r;
+    }
+    for (int m0 = 0; m0 < M; m0 += 128) {
+      const int rows = std::min(128, M - m0);
+      if (shape == 2 && rows > 64 && rows < 128)
+        stacked(m0, rows);
+      else
+        r.emplace_back(m0, rows);
+    }
+    return r;
+  };
   for (const auto& rk : order) {
     const auto& list = rects[rk];
     const hh_contrib& c0 = p->contribs[list[0]];
     const int M = c0.M, N = c0.N;
     const hh_wsec& w = L->secs[c0.k_out];
-    for (int m0 = 0; m0 < M; m0 += 128)
-      for (int n0 = 0; n0 < N; n0 += kTileN) {
-        const int ntile = k16(std::min(kTileN, N - n0));
+    for (const auto& [m0, mrows] : row_split(M))
+      for (int n0 = 0; n0 < N; n0 += tn2) {
+        const int ntile = k16(std::min(tn2, N - n0));
         tc::Tile tl{};
         tl.seg0 = (int)segs.size();
         tl.cseg0 = (int)csegs.size();
@@ -393,15 +430,15 @@ static int build_tc(hh_plan* p, hh_tc_plan& tp, int nb) {
           if (c.hasA && c.hasB) {
             const ImgRef& T = contrib_t[ci];
             ImgRef bi = op_img(c.B, 1, c.N, c.Kb, c.cre, c.cim);
-            segs.push_back(make_seg(tag(T.off, 2), T, m0, tag(bi.off, 0), bi, n0, ntile));
+            segs.push_back(make_seg(tag(T.off, 2), T, m0, tag(bi.off, 0), bi, n0, ntile, mrows));
           } else if (c.hasA) {
             ImgRef ai = op_img(c.A, 0, c.M, c.Ka, c.cre, c.cim);
             ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.Ka, c.N, 1);
-            segs.push_back(make_seg(tag(ai.off, 0), ai, m0, tag(xi.off, 1), xi, n0, ntile));
+            segs.push_back(make_seg(tag(ai.off, 0), ai, m0, tag(xi.off, 1), xi, n0, ntile, mrows));
           } else if (c.hasB) {
             ImgRef xi = x_img(c.i_in, c.irow, c.icol, c.M, c.Kb, 0);
             ImgRef bi = op_img(c.B, 1, c.N, c.Kb, c.cre, c.cim);
-            segs.push_back(make_seg(tag(xi.off, 1), xi, m0, tag(bi.off, 0), bi, n0, ntile));
+            segs.push_back(make_seg(tag(xi.off, 1), xi, m0, tag(bi.off, 0), bi, n0, ntile, mrows));
           } else {
             hh_seg cs{};
             const hh_wsec& wi = L->secs[c.i_in];
@@ -427,8 +464,8 @@ static int build_tc(hh_plan* p, hh_tc_plan& tp, int nb) {
         tl.ncseg = (int)csegs.size() - tl.cseg0;
         tl.mode = 0;
         tl.ntile = ntile;
-        tl.mrem = std::min(128, M - m0);
-        tl.nrem = std::min(kTileN, N - n0);
+        tl.mrem = mrows;
+        tl.nrem = std::min(tn2, N - n0);
         tl.out = w.off + (long long)(c0.ocol + n0) * w.sdim + c0.orow + m0;
         tl.ldo = w.sdim;
         tl.m0 = m0;
@@ -632,6 +669,15 @@ static int build_tc(hh_plan* p, hh_tc_plan& tp, int nb) {
   t.bytes_t = (double)a_t.size;
   t.mma_flops1 = mma1;
   t.mma_flops2 = mma2;
+  // stage-2 tile statistics: stacked tiles and the MMA cycles of the whole
+  // stage under the per-instruction cost max(45, width / 2) cycles per K = 16
+  // MMA (measured), SPLIT = 2 (three part pairs per chunk)
+  t.n_stacked2 = 0;
+  t.mma_cycles2 = 0.0;
+  for (const auto& x : tiles2) {
+    t.n_stacked2 += x.stack ? 1 : 0;
+    t.mma_cycles2 += 3.0 * x.nchunk * 256.0 * chunk_cost(x);
+  }
   // operator images are built once here (block list freed after the build)
   std::vector<int2> op_blocks;
   const int n_op_blocks = tc_image_blocks(op_tasks.data(), (int)op_tasks.size(), op_blocks);
@@ -762,17 +808,16 @@ int matvec_tc_batch(hh_plan* p, const double2* in, double2* out, int nb, bool ch
   return run_tc(p, p->tcb, nb, in, out, nullptr, check, split);
 }
 
-// Times the launch variants of the tile GEMM (stage 1 / stage 2 on the
+// Times the stage-2 tile shapes (0 - 3 of build_tc) and, for
+// each, the launch variants of the tile GEMM (stage 1 / stage 2 on the
 // persistent kernel or one CTA per tile) on this plan's own task lists, reps
-// timed runs each after one warm-up, and keeps the fastest; ms[v] receives
-// the mean time of variant v = 2 * persistent1 + persistent2.
+// timed runs each after one warm-up, and keeps the fastest; ms[4 s + v]
+// receives the mean time of shape s and variant v = 2 * persistent1 +
+// persistent2.  A shape is tried by rebuilding the plan's schedule (host
+// tiling and the operator images); the batched schedule, if any, is rebuilt
+// with the kept shape at its next use.
 int tune_tc_plan(hh_plan* p, int reps, double* ms, int split) {
   hh_ctx* ctx = p->ctx;
-  if (!p->tc.ready) {
-    int st = build_tc_plan(p);
-    if (st != HH_OK) return st;
-  }
-  hh_tc_plan& t = p->tc;
   const size_t bytes = (size_t)p->nelem * sizeof(double2);
   cudaError_t e = cudaSuccess;
   if (!p->d_host_in) e = dev_alloc(ctx, (void**)&p->d_host_in, bytes);
@@ -780,28 +825,47 @@ int tune_tc_plan(hh_plan* p, int reps, double* ms, int split) {
   if (e == cudaSuccess) e = cudaMemsetAsync(p->d_host_in, 0, bytes, ctx->stream);
   if (e != cudaSuccess) return cuda_check(ctx, e, "tune buffers");
   double best = 1e300;
-  int best_v = 2 * (int)t.persistent1 + (int)t.persistent2;
-  for (int v = 0; v < 4; ++v) {
-    t.persistent1 = (v >> 1) & 1;
-    t.persistent2 = v & 1;
-    double sum = 0.0;
-    for (int r = 0; r <= reps; ++r) {
-      float m[4];
-      int st = matvec_tc(p, p->d_host_in, p->d_host_out, m, true, split);
-      if (st) return st;
-      if (r > 0) sum += m[0];
+  int best_s = p->tc_shape, best_v = 2 * (int)p->tc.persistent1 + (int)p->tc.persistent2;
+  auto rebuild = [&](int shape) {
+    release_tc(ctx, p->tc);
+    p->tc_shape = shape;
+    return build_tc_plan(p);
+  };
+  for (int shape = 0; shape < HH_TILE_SHAPES; ++shape) {
+    if (shape != p->tc_shape || !p->tc.ready) {
+      int st = rebuild(shape);
+      if (st != HH_OK) return st;
     }
-    const double mean = reps > 0 ? sum / reps : 0.0;
-    if (ms) ms[v] = mean;
-    if (mean < best) {
-      best = mean;
-      best_v = v;
+    hh_tc_plan& t = p->tc;
+    for (int v = 0; v < 4; ++v) {
+      t.persistent1 = (v >> 1) & 1;
+      t.persistent2 = v & 1;
+      double sum = 0.0;
+      for (int r = 0; r <= reps; ++r) {
+        float m[4];
+        int st = matvec_tc(p, p->d_host_in, p->d_host_out, m, true, split);
+        if (st) return st;
+        if (r > 0) sum += m[0];
+      }
+      const double mean = reps > 0 ? sum / reps : 0.0;
+      if (ms) ms[4 * shape + v] = mean;
+      if (mean < best) {
+        best = mean;
+        best_s = shape;
+        best_v = v;
+      }
     }
   }
-  t.persistent1 = (best_v >> 1) & 1;
-  t.persistent2 = best_v & 1;
+  if (best_s != p->tc_shape) {
+    int st = rebuild(best_s);
+    if (st != HH_OK) return st;
+  }
+  p->tc.persistent1 = (best_v >> 1) & 1;
+  p->tc.persistent2 = best_v & 1;
   // the next graph is captured with the chosen kernels
-  destroy_graph(t);
+  destroy_graph(p->tc);
+  release_tc(ctx, p->tcb);
+  p->tcb_nb = 0;
   return HH_OK;
 }
 

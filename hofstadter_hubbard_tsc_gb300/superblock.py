@@ -247,7 +247,7 @@ class Superblock:
         return h
 
     def stats(self):
-        c = np.zeros(20)
+        c = np.zeros(_lib.HH_PLAN_STATS)
         self.dev.check(self.dev.lib.hh_plan_stats(self.plan, c.ctypes.data_as(C.POINTER(C.c_double))))
         keys = ["ref_flops", "exec_flops", "tiles", "segments", "stage1", "scratch_bytes", "op_bytes",
                 "wave_bytes", "exec_flops_s1", "exec_flops_s2", "ref_flops_first", "ref_flops_rest",

@@ -165,7 +165,7 @@ typedef struct {
 int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* env_bs,
                    const hh_wave_t* layout, int nterm, const hh_term_t* terms,
                    hh_plan_t** out);
-/* counts (16 doubles): [0] reference FLOPs per matvec (8MNK over the
+/* counts (HH_PLAN_STATS doubles): [0] reference FLOPs per matvec (8MNK over the
  * reference's ZGEMM calls + 8 per element of the axpy terms), [1] FLOPs this
  * plan executes, [2] output tiles, [3] segments, [4] stage-1 products,
  * [5] scratch bytes, [6] operator bytes, [7] wave bytes (in + out),
@@ -177,8 +177,12 @@ int hh_plan_create(hh_ctx_t* ctx, const hh_basis_t* sys_bs, const hh_basis_t* en
  * schedule has been built (first split-precision matvec), [16] kernel
  * launches of one FP64 matvec, [17] of one split-precision matvec (graph
  * replay included), [18] FP64 work tiles after balancing, [19] 1 when stage
- * 1 of the split-precision matvec runs on the persistent kernel.  counts
- * holds 20 doubles.                                                        */
+ * 1 of the split-precision matvec runs on the persistent kernel, [20]
+ * stage-2 tiles of the split-precision schedule, [21] those of at most 64
+ * rows (stacked MMAs), [22] the stage's MMA cycles at HH_PREC_BF16X3 summed
+ * over its tiles (a K = 16 MMA costs max(45, width / 2) SM cycles), [23] its
+ * tile shape (hh_plan_tune).  counts holds HH_PLAN_STATS = 24 doubles.      */
+#define HH_PLAN_STATS 24
 int hh_plan_stats(const hh_plan_t* p, double* counts);
 int hh_plan_free(hh_plan_t* p);
 
@@ -222,13 +226,23 @@ int hh_host_free(void* ptr);
  * ran out is reported by the next hh_plan_check, which waits for the stream. */
 int hh_matvec_async(hh_plan_t* plan, const hh_wave_t* in, hh_wave_t* out, int precision);
 int hh_plan_check(hh_plan_t* plan);
-/* Autotuner of the split-precision launch: times the four variants of the
- * tile GEMM (stage 1 / stage 2 on the persistent kernel or one CTA per tile)
- * on this plan at the given split precision, reps runs each after a
- * warm-up, and keeps the fastest for the plan's later matvecs.  ms (may be NULL) receives the four mean times
- * in ms, index 2 * stage1_persistent + stage2_persistent; *choice (may be
- * NULL) the kept index.  FP64 plans have nothing to tune (choice 0).      */
+/* Autotuner of the split-precision schedule: for each of the HH_TILE_SHAPES
+ * shapes of the stage-2 output tiles (0: 128 rows x 64 columns; 1: every
+ * output rectangle in near-equal tiles of at most 64 rows x 64 columns; 2:
+ * 128 x 64, remainders of 65-127 rows in two tiles of at most 64; 3: 128 x
+ * 128) it times the
+ * four launch variants of the tile GEMM (stage 1 / stage 2 on the persistent
+ * kernel or one CTA per tile) on this plan at the given split precision, reps
+ * runs each after a warm-up, and keeps the fastest shape and variant for the
+ * plan's later matvecs.  ms (may be NULL) receives HH_TUNE_VARIANTS mean
+ * times in ms, index 4 * shape + 2 * stage1_persistent + stage2_persistent;
+ * *choice (may be NULL) the kept index.  FP64 plans have nothing to tune
+ * (choice 0).  hh_plan_set_tiles fixes the shape without timing (the
+ * split-precision schedule is rebuilt at the next split matvec).          */
+#define HH_TILE_SHAPES 4
+#define HH_TUNE_VARIANTS 16
 int hh_plan_tune(hh_plan_t* plan, int precision, int reps, double* ms, int* choice);
+int hh_plan_set_tiles(hh_plan_t* plan, int shape);
 /* lanczos_memo_new (code/lanczos.f90:4-177), levels = 1.  psi is the start
  * vector on entry and the ground state on exit; lanzero is the breakdown and
  * convergence threshold; maxit <= 100 is loop_in.  With a split precision

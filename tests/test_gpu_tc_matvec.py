@@ -56,6 +56,40 @@ def test_tc_matvec_synthetic_m200(device, precision):
     sb.free()
 
 
+def test_tc_tile_shapes_and_tuner(device):
+    """Every stage-2 tile shape (128 x 64, near-equal stacked tiles of at most
+    64 rows, the mixed split, 128 x 128) gives the FP64 product within the
+    split precision's tolerance, eagerly and on graph replay; the autotuner
+    times every shape and launch variant and keeps one whose products agree."""
+    from hofstadter_hubbard_tsc_gb300.synth import Workload
+    wl = Workload(W=4, L=8, n_elec=28, m=300)
+    sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
+    rng = np.random.default_rng(11)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    sb.w_in.upload(psi)
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
+    ref = sb.w_out.download()
+    for shape in range(_lib.HH_TILE_SHAPES):
+        device.check(device.lib.hh_plan_set_tiles(sb.plan, shape))
+        for pr in SPLITS:
+            for _ in range(3):  # eager first call, then graph capture and replay
+                device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, pr))
+                got = sb.w_out.download()
+                assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < RTOL[pr], (shape, pr)
+    assert device.lib.hh_plan_set_tiles(sb.plan, _lib.HH_TILE_SHAPES) == -1
+    ms = np.zeros(_lib.HH_TUNE_VARIANTS)
+    choice = C.c_int(-1)
+    device.check(device.lib.hh_plan_tune(sb.plan, _lib.HH_PREC_BF16X3, 1, ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                         C.byref(choice)))
+    assert 0 <= choice.value < _lib.HH_TUNE_VARIANTS and np.all(ms > 0)
+    assert ms[choice.value] == ms.min()
+    for _ in range(2):
+        device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_BF16X3))
+        got = sb.w_out.download()
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < RTOL[_lib.HH_PREC_BF16X3]
+    sb.free()
+
+
 @pytest.mark.parametrize("precision", SPLITS)
 def test_tc_lanczos_energy(device, precision):
     lat, d = H.record_superblocks(2, 6, 10, 32)
