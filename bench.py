@@ -424,6 +424,7 @@ def config_matvec_bench(dev, name, steps, prec_name):
     split-precision matvecs/s by CUDA events over `steps` graph replays (L2
     flushed before each), the FP64 GPU matvec rate over one product, and the
     split product's error against FP64."""
+    import ctypes as C
     import torch
     from hofstadter_hubbard_tsc_gb300.superblock import Superblock
     from hofstadter_hubbard_tsc_gb300 import _lib
@@ -458,6 +459,13 @@ def config_matvec_bench(dev, name, steps, prec_name):
         torch.cuda.synchronize()
         return sum(e0.elapsed_time(e1) for e0, e1 in ev) / n
 
+    tune = None
+    if prec != _lib.HH_PREC_FP64:  # the schedule autotuner on this workload
+        tms, tch = np.zeros(_lib.HH_TUNE_VARIANTS), C.c_int(0)
+        t0 = time.perf_counter()
+        dev.check(dev.lib.hh_plan_tune(sb.plan, prec, 2, tms.ctypes.data_as(C.POINTER(C.c_double)), C.byref(tch)))
+        tune = {"variants_ms": [round(x, 4) for x in tms], "chosen": int(tch.value),
+                "tune_s": round(time.perf_counter() - t0, 3)}
     ms_split = timed(prec, steps)
     hs = sb.w_out.download()
     dev.check(dev.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
@@ -467,7 +475,7 @@ def config_matvec_bench(dev, name, steps, prec_name):
            "ms_per_matvec": ms_split, "steps": steps, "fp64_matvecs_per_s": 1e3 / ms64,
            "split_vs_fp64_matvec": ms64 / ms_split,
            "rel_err_vs_fp64_gpu": float(np.linalg.norm(hs - h64) / np.linalg.norm(h64)),
-           "workload_generation_s": round(gen_s, 2), "plan_build_s": round(plan_s, 3),
+           "workload_generation_s": round(gen_s, 2), "plan_build_s": round(plan_s, 3), "autotune": tune,
            "timing": "CUDA events on the library stream, graph replays, L2 flushed before each"}
     sb.free()
     del flush
