@@ -833,6 +833,22 @@ def main():
         t64 = sum(a.elapsed_time(b) for a, b in ev64) / n64
         line["fp64_gpu"] = {"value": 1e3 / t64, "unit": UNIT, "ms_per_step": t64, "steps": n64,
                             "split_vs_fp64_matvec": (1e3 / t64) and value / (1e3 / t64)}
+        # the double-float product (the split Lanczos's restart product):
+        # rate and error against FP64, same timing
+        dev.check(dev.lib.hh_matvec(sb.plan, w_in.h, w_out.h, _lib.HH_PREC_FP32X2))
+        hdf = w_out.download()
+        evd = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n64)]
+        with torch.cuda.stream(stream):
+            for a, b in evd:
+                flush.zero_()
+                a.record(stream)
+                dev.check(dev.lib.hh_matvec_async(sb.plan, w_in.h, w_out.h, _lib.HH_PREC_FP32X2))
+                b.record(stream)
+        dev.check(dev.lib.hh_plan_check(sb.plan))
+        tdf = sum(a.elapsed_time(b) for a, b in evd) / n64
+        line["fp32x2_gpu"] = {"value": 1e3 / tdf, "unit": UNIT, "ms_per_step": tdf, "steps": n64,
+                              "vs_fp64_gpu": t64 / tdf,
+                              "rel_err_vs_fp64_gpu": float(np.linalg.norm(hdf - h64) / np.linalg.norm(h64))}
     if prec != _lib.HH_PREC_FP64:
         # 8 vectors of the same workload in one graph replay (every stage one
         # launch over the batch) against the single-vector replays above

@@ -18,6 +18,7 @@ HH_PREC_FP64 = 0
 HH_PREC_BF16X6 = 1  # three BF16 parts, six products: ~2^-24 per product
 HH_PREC_BF16X3 = 2  # two BF16 parts, three products: ~2^-16 per product
 HH_PREC_FP32 = 3  # FP32 arithmetic: the wave transform's guess only (hh_ctx_set_transform_precision)
+HH_PREC_FP32X2 = 4  # double-float on the FP32 pipe (~2^-47): the split Lanczos's restart product
 HH_EIG_OWN, HH_EIG_CUSOLVER = 0, 1  # density-matrix eigensolver (hh_ctx_set_eigensolver)
 HH_TILE_SHAPES, HH_TUNE_VARIANTS = 4, 16  # stage-2 tile shapes / timings of hh_plan_tune
 HH_PLAN_STATS = 24  # doubles written by hh_plan_stats
@@ -70,6 +71,7 @@ SIGNATURES = {
     "hh_version": (I, []),
     "hh_ctx_set_eigensolver": (I, [P, I]),
     "hh_ctx_set_transform_precision": (I, [P, I]),
+    "hh_ctx_set_restart_precision": (I, [P, I]),
     "hh_eig_selftest": (I, [P, I, DP, DP, DP]),
     "hh_block_create": (I, [P, I, I, I, I, IP, DP, PP]),
     "hh_block_zeros": (I, [P, I, I, I, I, IP, PP]),

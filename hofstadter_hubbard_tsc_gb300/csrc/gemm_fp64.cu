@@ -31,11 +31,60 @@ __device__ __forceinline__ const double2* resolve(long long off, int base, const
   }
 }
 
-// F32: the same products with FP32 arithmetic (inputs rounded to FP32 as they
-// are staged, outputs widened to FP64): for results that only start an
-// iteration, where GB300's FP32 pipe (64 times the FP64 rate) is worth the
-// 2^-24 rounding.
-template <bool F32>
+// One complex number as two double-float parts: re = rh + rl, im = ih + il
+// (hi = the FP64 value rounded to FP32, lo = the FP32 rounding of the rest;
+// 48 significand bits).
+struct alignas(16) df2 {
+  float rh, rl, ih, il;
+};
+
+__device__ __forceinline__ df2 to_df(double2 v) {
+  df2 r;
+  r.rh = __double2float_rn(v.x);
+  r.rl = __double2float_rn(v.x - (double)r.rh);
+  r.ih = __double2float_rn(v.y);
+  r.il = __double2float_rn(v.y - (double)r.ih);
+  return r;
+}
+
+// (sh, sl) += (xh + xl)(yh + yl) in double-float: the leading product with
+// its exact rounding error (FMA residual, Dekker's TwoProduct), its addition
+// to sh with the exact rounding error (Knuth's TwoSum), the cross products
+// into sl; xl yl (2^-48 relative) is dropped.  The _rn intrinsics keep the
+// compiler from fusing or reordering the error-free steps.
+__device__ __forceinline__ void df_mac(float& sh, float& sl, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float pe = __fmaf_rn(xh, yh, -p);
+  const float s = __fadd_rn(sh, p);
+  const float bv = __fsub_rn(s, sh);
+  const float se = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+  sl = __fadd_rn(sl, __fadd_rn(se, pe));
+  sl = __fmaf_rn(xh, yl, sl);
+  sl = __fmaf_rn(xl, yh, sl);
+  sh = s;
+}
+
+// (sh, sl) += x for an FP64 x (copy terms)
+__device__ __forceinline__ void df_add(float& sh, float& sl, double x) {
+  const float xh = __double2float_rn(x);
+  const float xl = __double2float_rn(x - (double)xh);
+  const float s = __fadd_rn(sh, xh);
+  const float bv = __fsub_rn(s, sh);
+  const float se = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bv)), __fsub_rn(xh, bv));
+  sl = __fadd_rn(sl, __fadd_rn(se, xl));
+  sh = s;
+}
+
+// Arithmetic of the segment GEMM (ARITH):
+//  kArithFp64: FP64, as the reference;
+//  kArithFp32: inputs rounded to FP32 as they are staged, FP32 products and
+//    sums, outputs widened to FP64: for results that only start an iteration,
+//    where GB300's FP32 pipe (64 times the FP64 rate) is worth the 2^-24
+//    rounding;
+//  kArithDf: double-float (df2 operands, df_mac): about 2^-47 relative per
+//    operation, FP64-class products on the FP32 pipe (48 FP32 operations per
+//    complex multiply-add, against four FP64 FMAs at 1/64 of the rate).
+template <int ARITH>
 __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __restrict__ tiles,
                                                           const hh_seg* __restrict__ segs,
                                                           const double2* __restrict__ bin,
@@ -43,9 +92,19 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
                                                           double2* __restrict__ bout,
                                                           double2* __restrict__ part,
                                                           long long sin, long long sscr, long long sout) {
-  using V = typename std::conditional<F32, float2, double2>::type;
+  constexpr bool F32 = ARITH == kArithFp32, DF = ARITH == kArithDf;
+  using V = typename std::conditional<DF, df2, typename std::conditional<F32, float2, double2>::type>::type;
   using R = typename std::conditional<F32, float, double>::type;
-  auto narrow = [](double2 v) { V r; r.x = (R)v.x; r.y = (R)v.y; return r; };
+  auto narrow = [](double2 v) {
+    V r;
+    if constexpr (DF) {
+      r = to_df(v);
+    } else {
+      r.x = (R)v.x;
+      r.y = (R)v.y;
+    }
+    return r;
+  };
   __shared__ V Ps[TK][TM + 1];
   __shared__ V Qs[TK][TN + 1];
   const hh_tile t = tiles[blockIdx.x];
@@ -60,7 +119,12 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j].x = acc[i][j].y = (R)0;
+    for (int j = 0; j < 4; ++j) {
+      if constexpr (DF)
+        acc[i][j] = df2{0.f, 0.f, 0.f, 0.f};
+      else
+        acc[i][j].x = acc[i][j].y = (R)0;
+    }
 
   for (int si = 0; si < t.nseg; ++si) {
     const hh_seg s = segs[t.seg0 + si];
@@ -75,8 +139,13 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
           if (r < mrem && q < nrem) {
             double2 v = P[(long long)(t.m0 + r) + (long long)(t.n0 + q) * s.ldp];
             double2 cv = cmul(c, v);
-            acc[i][j].x += (R)cv.x;
-            acc[i][j].y += (R)cv.y;
+            if constexpr (DF) {
+              df_add(acc[i][j].rh, acc[i][j].rl, cv.x);
+              df_add(acc[i][j].ih, acc[i][j].il, cv.y);
+            } else {
+              acc[i][j].x += (R)cv.x;
+              acc[i][j].y += (R)cv.y;
+            }
           }
         }
       continue;
@@ -130,22 +199,37 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            acc[i][j].x = fma(a[i].x, bb[j].x, acc[i][j].x);
-            acc[i][j].x = fma(-a[i].y, bb[j].y, acc[i][j].x);
-            acc[i][j].y = fma(a[i].x, bb[j].y, acc[i][j].y);
-            acc[i][j].y = fma(a[i].y, bb[j].x, acc[i][j].y);
+            if constexpr (DF) {
+              df2& z = acc[i][j];
+              df_mac(z.rh, z.rl, a[i].rh, a[i].rl, bb[j].rh, bb[j].rl);
+              df_mac(z.rh, z.rl, -a[i].ih, -a[i].il, bb[j].ih, bb[j].il);
+              df_mac(z.ih, z.il, a[i].rh, a[i].rl, bb[j].ih, bb[j].il);
+              df_mac(z.ih, z.il, a[i].ih, a[i].il, bb[j].rh, bb[j].rl);
+            } else {
+              acc[i][j].x = fma(a[i].x, bb[j].x, acc[i][j].x);
+              acc[i][j].x = fma(-a[i].y, bb[j].y, acc[i][j].x);
+              acc[i][j].y = fma(a[i].x, bb[j].y, acc[i][j].y);
+              acc[i][j].y = fma(a[i].y, bb[j].x, acc[i][j].y);
+            }
           }
       }
       __syncthreads();
     }
   }
+  // the accumulator as FP64
+  auto wide = [](const V& z) {
+    if constexpr (DF)
+      return make_double2((double)z.rh + (double)z.rl, (double)z.ih + (double)z.il);
+    else
+      return make_double2((double)z.x, (double)z.y);
+  };
   if (t.part >= 0) {
     // partial sum of a split tile: the whole 64x64 slot, column-major
     double2* S = part + (long long)t.part * (TM * TN);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) S[(ty * 4 + i) + (tx * 4 + j) * TM] = make_double2(acc[i][j].x, acc[i][j].y);
+      for (int j = 0; j < 4; ++j) S[(ty * 4 + i) + (tx * 4 + j) * TM] = wide(acc[i][j]);
     return;
   }
   double2* O = (t.obase == HH_BASE_SCR) ? scr : out;
@@ -157,13 +241,14 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
       int r = ty * 4 + i, q = tx * 4 + j;
       if (r < mrem && q < nrem) {
         long long idx = (long long)(t.m0 + r) + (long long)(t.n0 + q) * t.ldo;
+        const double2 v = wide(acc[i][j]);
         if (t.accumulate) {
           double2 o = O[idx];
-          o.x += (double)acc[i][j].x;
-          o.y += (double)acc[i][j].y;
+          o.x += v.x;
+          o.y += v.y;
           O[idx] = o;
         } else {
-          O[idx] = make_double2(acc[i][j].x, acc[i][j].y);
+          O[idx] = v;
         }
       }
     }
@@ -386,16 +471,19 @@ cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, c
 }
 
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
-                                     double2* base_out, cudaStream_t s, bool fp32) {
+                                     double2* base_out, cudaStream_t s, int arith) {
   if (L.n_work == 0) return cudaSuccess;
   // grid.x = work tiles; the 65535 limit applies to grid.y only
   dim3 grid((unsigned)L.n_work, 1);
-  if (fp32)
-    seg_gemm_fp64_kernel<true><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part, 0, 0,
-                                                   0);
+  if (arith == kArithFp32)
+    seg_gemm_fp64_kernel<kArithFp32><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part,
+                                                         0, 0, 0);
+  else if (arith == kArithDf)
+    seg_gemm_fp64_kernel<kArithDf><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part,
+                                                       0, 0, 0);
   else
-    seg_gemm_fp64_kernel<false><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part, 0,
-                                                    0, 0);
+    seg_gemm_fp64_kernel<kArithFp64><<<grid, NT, 0, s>>>(L.d_tiles, L.d_segs, base_in, base_scr, base_out, L.d_part,
+                                                         0, 0, 0);
   if (L.n_red > 0) seg_reduce_kernel<<<(unsigned)L.n_red, NT, 0, s>>>(L.d_reds, L.d_part, base_scr, base_out);
   return cudaGetLastError();
 }
@@ -405,7 +493,7 @@ cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, do
 // launch reserves no device memory for their code.
 cudaError_t preload_segment_gemm_fp64() {
   cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, seg_gemm_fp64_kernel<false>);
+  cudaError_t e = cudaFuncGetAttributes(&a, seg_gemm_fp64_kernel<kArithFp64>);
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, seg_reduce_kernel);
   return e;
 }

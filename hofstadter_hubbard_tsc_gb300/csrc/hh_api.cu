@@ -725,11 +725,14 @@ int hh_plan_free(hh_plan_t* p) {
 
 static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision, bool check = true) {
   hh_ctx* ctx = p->ctx;
-  if (precision != HH_PREC_FP64 && !split_of(precision)) return fail(ctx, HH_ERR_INVALID, "unknown precision");
-  if (precision != HH_PREC_FP64) return matvec_tc(p, in, out, nullptr, check, split_of(precision));
+  const int arith = seg_arith_of(precision);
+  if (arith < 0 && !split_of(precision)) return fail(ctx, HH_ERR_INVALID, "unknown precision");
+  if (arith < 0) return matvec_tc(p, in, out, nullptr, check, split_of(precision));
   cudaError_t e = cudaMemsetAsync(out, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
-  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
-  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, const_cast<double2*>(in), p->d_scratch, out, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_segment_gemm_fp64(p->stage1, const_cast<double2*>(in), p->d_scratch, out, ctx->stream, arith);
+  if (e == cudaSuccess)
+    e = launch_segment_gemm_fp64(p->stage2, const_cast<double2*>(in), p->d_scratch, out, ctx->stream, arith);
   return cuda_check(ctx, e, "matvec");
 }
 
@@ -741,10 +744,8 @@ static int matvec_dev(hh_plan* p, const double2* in, double2* out, int precision
 static int matvec_batch(hh_plan* p, const hh_wave* in, hh_wave* out, int precision, bool check) {
   if (in->nelem != p->nelem || out->nelem != p->nelem || in == out || in->nbatch != out->nbatch)
     return fail(p->ctx, HH_ERR_INVALID, "matvec: wave layout does not match the plan (or in == out)");
-  if (precision != HH_PREC_FP64 && in->nbatch > 1) {
-    if (!split_of(precision)) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
+  if (split_of(precision) && in->nbatch > 1)
     return matvec_tc_batch(p, in->d, out->d, in->nbatch, check, split_of(precision));
-  }
   for (int b = 0; b < in->nbatch; ++b) {
     const bool last = b + 1 == in->nbatch;
     const int st = matvec_dev(p, in->d + (size_t)b * p->nelem, out->d + (size_t)b * p->nelem, precision,
@@ -774,7 +775,7 @@ int hh_matvec_host(hh_plan_t* p, const double* in, double* out, int precision) {
   if (e == cudaSuccess) st = matvec_dev(p, p->d_host_in, p->d_host_out, precision, false);
   int* h_err = reinterpret_cast<int*>(ctx->h_red + 8);
   *h_err = 0;
-  const bool tc = precision != HH_PREC_FP64 && p->tc.ready;
+  const bool tc = split_of(precision) && p->tc.ready;
   if (e == cudaSuccess && st == HH_OK)
     e = cudaMemcpyAsync(out, p->d_host_out, bytes, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess && st == HH_OK && tc)
@@ -794,7 +795,8 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
   if (!p || !in || !out || !ms || in == out || in->nelem != p->nelem || out->nelem != p->nelem)
     return HH_ERR_INVALID;
   hh_ctx* ctx = p->ctx;
-  if (precision != HH_PREC_FP64) {
+  const int arith = seg_arith_of(precision);
+  if (arith < 0) {
     if (!split_of(precision)) return fail(ctx, HH_ERR_INVALID, "unknown precision");
     return matvec_tc(p, in->d, out->d, ms, true, split_of(precision));
   }
@@ -802,9 +804,9 @@ int hh_matvec_timed(hh_plan_t* p, const hh_wave_t* in, hh_wave_t* out, int preci
   for (int i = 0; i < 3; ++i) cudaEventCreate(&ev[i]);
   cudaError_t e = cudaMemsetAsync(out->d, 0, (size_t)p->nelem * sizeof(double2), ctx->stream);
   cudaEventRecord(ev[0], ctx->stream);
-  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, in->d, p->d_scratch, out->d, ctx->stream);
+  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage1, in->d, p->d_scratch, out->d, ctx->stream, arith);
   cudaEventRecord(ev[1], ctx->stream);
-  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, in->d, p->d_scratch, out->d, ctx->stream);
+  if (e == cudaSuccess) e = launch_segment_gemm_fp64(p->stage2, in->d, p->d_scratch, out->d, ctx->stream, arith);
   cudaEventRecord(ev[2], ctx->stream);
   if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
   if (e == cudaSuccess) {
@@ -843,7 +845,7 @@ int hh_plan_check(hh_plan_t* p) {
 
 int hh_plan_tune(hh_plan_t* p, int precision, int reps, double* ms, int* choice) {
   if (!p || reps < 1) return HH_ERR_INVALID;
-  if (precision == HH_PREC_FP64) {  // one launch shape: nothing to choose
+  if (seg_arith_of(precision) >= 0) {  // one launch shape: nothing to choose
     if (choice) *choice = 0;
     return HH_OK;
   }
@@ -882,24 +884,25 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit, int precision, double* energy,
                int* iterations) {
   if (!p || !psi || !energy || psi->nelem != p->nelem || maxit < 1) return HH_ERR_INVALID;
-  if (precision == HH_PREC_FP64)
+  if (seg_arith_of(precision) >= 0)
     return lanczos_core(p, psi, lanzero, maxit, precision, precision, energy, iterations);
   if (!split_of(precision)) return fail(p->ctx, HH_ERR_INVALID, "unknown precision");
   // Split precision, two passes.  (1) Lanczos on the tensor-core matvec down
   // to its noise floor: Ritz value change <= max(lanzero, 1e-8).  (2) Lanczos
-  // restarted from that vector psi_m whose first product H psi_m is FP64 and
-  // whose later ones are split precision.  The FP64 residual H psi_m - a0 psi_m
+  // restarted from that vector psi_m whose first product H psi_m is
+  // FP64-class (double-float by default, ctx->restart_precision) and whose
+  // later ones are split precision.  The accurate residual H psi_m - a0 psi_m
   // starts the correction space and the Gram-Schmidt step keeps every later
   // vector orthogonal to psi_m and to it, so the tridiagonal's first row is
-  // FP64-exact; the split-precision entries enter the Ritz value weighted by
-  // the squares of the correction coefficients (about the vector error of
-  // psi_m, 1e-4), which takes the energy to FP64 accuracy at the cost of one
-  // FP64 matvec.
+  // accurate to the product's ~1e-14; the split-precision entries enter the
+  // Ritz value weighted by the squares of the correction coefficients (about
+  // the vector error of psi_m, 1e-4), which takes the energy to FP64
+  // accuracy at the cost of one FP64-class matvec.
   double e_mixed = 0.0;
   int it1 = 0, it2 = 0;
   int st = lanczos_core(p, psi, std::max(lanzero, 1e-8), maxit, precision, precision, &e_mixed, &it1);
   if (st) return st;
-  st = lanczos_core(p, psi, lanzero, maxit, HH_PREC_FP64, precision, energy, &it2);
+  st = lanczos_core(p, psi, lanzero, maxit, p->ctx->restart_precision, precision, energy, &it2);
   if (st) return st;
   if (iterations) *iterations = it1 + it2;
   return HH_OK;

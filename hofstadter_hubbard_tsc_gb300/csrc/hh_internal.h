@@ -52,6 +52,7 @@ struct hh_ctx {
   // arithmetic of hh_wave_transform's products: HH_PREC_FP64 (default) or
   // HH_PREC_FP32 (the transformed wave only starts Lanczos)
   int transform_precision = 0;
+  int restart_precision = HH_PREC_FP32X2;  // the split Lanczos's energy-setting product
   // device address of the static scratch array of hh_matvec_noalloc, looked
   // up by hh_init in this context (noalloc.cu); null with a reason if that
   // lookup failed
@@ -263,9 +264,11 @@ void dev_free(hh_ctx* ctx, void* p);
 int cuda_check(hh_ctx* ctx, cudaError_t e, const char* what);
 // looks up the static scratch of hh_matvec_noalloc for ctx->device (noalloc.cu)
 void noalloc_setup(hh_ctx* ctx);
-// grouped segment GEMM (FP64); bases[4] = {abs(unused), in, scr, out}
+// grouped segment GEMM; bases[4] = {abs(unused), in, scr, out}; arithmetic
+// FP64, FP32 or double-float (gemm_fp64.cu)
+enum { kArithFp64 = 0, kArithFp32 = 1, kArithDf = 2 };
 cudaError_t launch_segment_gemm_fp64(const hh_gemm_list& L, double2* base_in, double2* base_scr,
-                                     double2* base_out, cudaStream_t s, bool fp32 = false);
+                                     double2* base_out, cudaStream_t s, int arith = kArithFp64);
 // loads the segment GEMM kernels into the current context (gemm_fp64.cu)
 cudaError_t preload_segment_gemm_fp64();
 // wave vector kernels
@@ -302,6 +305,11 @@ int tune_tc_plan(hh_plan* p, int reps, double* ms, int split);
 // BF16 parts per operand of a split precision, 0 for FP64 or an unknown code
 inline int split_of(int precision) {
   return precision == HH_PREC_BF16X6 ? 3 : precision == HH_PREC_BF16X3 ? 2 : 0;
+}
+// the segment-GEMM arithmetic of an FP64-class matvec precision (FP64 or
+// double-float), -1 for the split precisions and unknown codes
+inline int seg_arith_of(int precision) {
+  return precision == HH_PREC_FP64 ? kArithFp64 : precision == HH_PREC_FP32X2 ? kArithDf : -1;
 }
 double w6j(int j1, int j2, int j3, int l1, int l2, int l3);
 double w3j(int j1, int j2, int j3, int m1, int m2, int m3);

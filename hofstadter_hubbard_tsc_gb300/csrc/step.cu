@@ -27,7 +27,7 @@ struct GemmRun {
   // stream order, so nothing here waits for the device
   int run(hh_ctx* ctx, double2* base_in, double2* base_scr, double2* base_out, bool fp32 = false) {
     L.upload(ctx);
-    cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream, fp32);
+    cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream, fp32 ? kArithFp32 : kArithFp64);
     L.release();
     return cuda_check(ctx, e, "step GEMM");
   }
@@ -255,6 +255,12 @@ extern "C" int hh_ctx_set_eigensolver(hh_ctx_t* ctx, int solver) {
 extern "C" int hh_ctx_set_transform_precision(hh_ctx_t* ctx, int precision) {
   if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32)) return HH_ERR_INVALID;
   ctx->transform_precision = precision;
+  return HH_OK;
+}
+
+extern "C" int hh_ctx_set_restart_precision(hh_ctx_t* ctx, int precision) {
+  if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32X2)) return HH_ERR_INVALID;
+  ctx->restart_precision = precision;
   return HH_OK;
 }
 

@@ -42,6 +42,11 @@ extern "C" {
 #define HH_PREC_FP32 3        /* complex FP32 on the CUDA cores (the wave
                                  transform's guess only, hh_ctx_set_transform_
                                  precision)                                       */
+#define HH_PREC_FP32X2 4      /* double-float on the FP32 pipe: every operand as
+                                 a sum of two floats (48 bits), exact products
+                                 by FMA residuals, sums by TwoSum: ~2^-47 per
+                                 operation, FP64-class (the split Lanczos's
+                                 restart product by default)                      */
 
 typedef struct hh_ctx hh_ctx_t;
 typedef struct hh_block hh_block_t;
@@ -76,6 +81,11 @@ int hh_ctx_set_eigensolver(hh_ctx_t* ctx, int solver);
  * Lanczos, so a split-precision sweep can take the 2^-24 rounding for
  * GB300's FP32 rate (64x its FP64 rate).  No counterpart in the reference. */
 int hh_ctx_set_transform_precision(hh_ctx_t* ctx, int precision);
+/* Arithmetic of the one product of the split-precision hh_lanczos that sets
+ * the energy to FP64 accuracy (the restart product, below): HH_PREC_FP32X2
+ * (default; double-float on the FP32 pipe, which GB300 runs at 64 times its
+ * FP64 rate) or HH_PREC_FP64.  No counterpart in the reference.           */
+int hh_ctx_set_restart_precision(hh_ctx_t* ctx, int precision);
 /* Diagnostic: every eigenpair of one dense Hermitian matrix A (n x n,
  * column-major, interleaved complex) through the tridiagonal pipeline of
  * HH_EIG_OWN (whatever n): w ascending (n doubles), V the eigenvectors
@@ -249,9 +259,11 @@ int hh_plan_set_tiles(hh_plan_t* plan, int shape);
  * (HH_PREC_BF16X6, HH_PREC_BF16X3) the
  * Krylov recurrence first runs on the split-precision matvec until the Ritz
  * value moves by <= max(lanzero, 1e-8); a second Lanczos restarted from that
- * vector takes its first product in FP64 and the rest in split precision and
- * converges to lanzero (one FP64 matvec per call); *iterations counts the
- * Krylov vectors of both passes.                                          */
+ * vector takes its first product in FP64-class arithmetic (double-float or
+ * FP64, hh_ctx_set_restart_precision) and the rest in split precision and
+ * converges to lanzero (one such product per call); *iterations counts the
+ * Krylov vectors of both passes.  HH_PREC_FP32X2 runs every product in
+ * double-float.                                                           */
 int hh_lanczos(hh_plan_t* p, hh_wave_t* psi, double lanzero, int maxit,
                int precision, double* energy, int* iterations);
 /* Fills a wave with uniform [0,1) real and imaginary parts from a seeded

@@ -103,3 +103,53 @@ def test_tc_lanczos_energy(device, precision):
     emx, _, _ = sb.lanczos_memo_new(start, 1e-8, precision=precision)
     assert abs(emx - e64) / abs(e64) < 1e-8, (emx, e64)
     sb.free()
+
+
+def test_fp32x2_matvec_and_restart(device):
+    """The double-float product (HH_PREC_FP32X2: FP64 operands as sums of two
+    floats, exact FMA residuals and TwoSum on the FP32 pipe) equals the FP64
+    product to FP64-class accuracy on oracle superblocks and a synthetic
+    m = 200 superblock; the split Lanczos with its restart product in
+    double-float (the default) or FP64 gives the FP64 energy, and a Lanczos run
+    wholly in double-float too."""
+    from hofstadter_hubbard_tsc_gb300.synth import Workload
+    lat, d = H.record_superblocks(2, 6, 10, 32)
+    plat = H.product_lattice(lat)
+    for idx, rec in enumerate(d.record[::3]):
+        sys, env, sys_bs, env_bs, geo, sup, _ = rec
+        sb = Superblock(device, H.model(sys), H.model(env), H.basis(sys_bs), H.basis(env_bs),
+                        H.superbasis(sup), plat.geometry(sys.len, env.len))
+        x = H.wave(H.random_wave(sup, idx))
+        a = sb.model_wave(x, precision=_lib.HH_PREC_FP64).flat()
+        b = sb.model_wave(x, precision=_lib.HH_PREC_FP32X2).flat()
+        assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-13, idx
+        sb.free()
+    wl = Workload(W=4, L=8, n_elec=28, m=200)
+    sb = Superblock(device, wl.sys, wl.env, wl.sys_bs, wl.env_bs, wl.sup, wl.geo)
+    rng = np.random.default_rng(4)
+    psi = rng.normal(size=wl.sup.dim) + 1j * rng.normal(size=wl.sup.dim)
+    sb.w_in.upload(psi)
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP64))
+    ref = sb.w_out.download()
+    device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP32X2))
+    got = sb.w_out.download()
+    err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert err < 1e-13, err
+    sb.free()
+
+    assert device.lib.hh_ctx_set_restart_precision(device.h, _lib.HH_PREC_BF16X3) == -1
+    rec = d.record[-3]
+    sys, env, sys_bs, env_bs, geo, sup, _ = rec
+    sb = Superblock(device, H.model(sys), H.model(env), H.basis(sys_bs), H.basis(env_bs),
+                    H.superbasis(sup), plat.geometry(sys.len, env.len))
+    e64, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_FP64)
+    edf, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_FP32X2)
+    assert abs(edf - e64) / abs(e64) < 1e-11, (edf, e64)
+    try:
+        for rp in (_lib.HH_PREC_FP64, _lib.HH_PREC_FP32X2):
+            device.check(device.lib.hh_ctx_set_restart_precision(device.h, rp))
+            emx, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_BF16X3)
+            assert abs(emx - e64) / abs(e64) < 1e-10, (rp, emx, e64)
+    finally:
+        device.check(device.lib.hh_ctx_set_restart_precision(device.h, _lib.HH_PREC_FP32X2))
+    sb.free()
