@@ -64,6 +64,15 @@ __device__ __forceinline__ void df_mac(float& sh, float& sl, float xh, float xl,
   sh = s;
 }
 
+// (sh, sl) <- the same value with |sl| <= ulp(sh) / 2 (TwoSum of the two):
+// keeps the rounding errors of the low accumulator at 2^-48 of the sum
+__device__ __forceinline__ void df_renorm(float& sh, float& sl) {
+  const float s = __fadd_rn(sh, sl);
+  const float bv = __fsub_rn(s, sh);
+  sl = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bv)), __fsub_rn(sl, bv));
+  sh = s;
+}
+
 // (sh, sl) += x for an FP64 x (copy terms)
 __device__ __forceinline__ void df_add(float& sh, float& sl, double x) {
   const float xh = __double2float_rn(x);
@@ -211,6 +220,15 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
               acc[i][j].y = fma(a[i].x, bb[j].y, acc[i][j].y);
               acc[i][j].y = fma(a[i].y, bb[j].x, acc[i][j].y);
             }
+          }
+      }
+      if constexpr (DF) {  // once per 16 k: the low parts stay small
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            df_renorm(acc[i][j].rh, acc[i][j].rl);
+            df_renorm(acc[i][j].ih, acc[i][j].il);
           }
       }
       __syncthreads();

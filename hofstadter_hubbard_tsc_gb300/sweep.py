@@ -70,10 +70,14 @@ class GPUDMRG:
 
     @contextmanager
     def _phase(self, name):
+        """Host wall time of a phase, its device work included: the phase's
+        queued kernels are waited for at its end, so that work queued without a
+        wait (enlargement, renormalisation) is not billed to the next phase."""
         t0 = time.perf_counter()
         try:
             yield
         finally:
+            self.dev.sync()
             self.phase_s[name] += time.perf_counter() - t0
 
     # ------------------------------------------------------------------ setup

@@ -134,7 +134,9 @@ def test_fp32x2_matvec_and_restart(device):
     device.check(device.lib.hh_matvec(sb.plan, sb.w_in.h, sb.w_out.h, _lib.HH_PREC_FP32X2))
     got = sb.w_out.download()
     err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
-    assert err < 1e-13, err
+    # N(0,1) operators, sums of several hundred products per element: a few
+    # 2^-48 roundings each
+    assert err < 5e-13, err
     sb.free()
 
     assert device.lib.hh_ctx_set_restart_precision(device.h, _lib.HH_PREC_BF16X3) == -1
