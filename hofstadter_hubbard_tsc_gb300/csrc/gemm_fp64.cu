@@ -94,7 +94,7 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, double x) {
 //    operation, FP64-class products on the FP32 pipe (48 FP32 operations per
 //    complex multiply-add, against four FP64 FMAs at 1/64 of the rate).
 template <int ARITH>
-__global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __restrict__ tiles,
+__global__ void __launch_bounds__(NT, ARITH == kArithDf ? 2 : 0) seg_gemm_fp64_kernel(const hh_tile* __restrict__ tiles,
                                                           const hh_seg* __restrict__ segs,
                                                           const double2* __restrict__ bin,
                                                           double2* __restrict__ bscr,
@@ -197,8 +197,30 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
         Qs[kk][n] = narrow(v);
       }
       __syncthreads();
+      if constexpr (DF) {
+        // B operands one at a time, no unrolling over k: the accumulators
+        // fill the registers of two CTAs per SM
+#pragma unroll 1
+        for (int kk = 0; kk < TK; ++kk) {
+          df2 a[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) a[i] = Ps[kk][ty * 4 + i];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const df2 q = Qs[kk][tx * 4 + j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              df2& z = acc[i][j];
+              df_mac(z.rh, z.rl, a[i].rh, a[i].rl, q.rh, q.rl);
+              df_mac(z.rh, z.rl, -a[i].ih, -a[i].il, q.ih, q.il);
+              df_mac(z.ih, z.il, a[i].rh, a[i].rl, q.ih, q.il);
+              df_mac(z.ih, z.il, a[i].ih, a[i].il, q.rh, q.rl);
+            }
+          }
+        }
+      }
 #pragma unroll 4
-      for (int kk = 0; kk < TK; ++kk) {
+      for (int kk = 0; kk < (DF ? 0 : TK); ++kk) {
         V a[4], bb[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) a[i] = Ps[kk][ty * 4 + i];
@@ -208,13 +230,7 @@ __global__ void __launch_bounds__(NT) seg_gemm_fp64_kernel(const hh_tile* __rest
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            if constexpr (DF) {
-              df2& z = acc[i][j];
-              df_mac(z.rh, z.rl, a[i].rh, a[i].rl, bb[j].rh, bb[j].rl);
-              df_mac(z.rh, z.rl, -a[i].ih, -a[i].il, bb[j].ih, bb[j].il);
-              df_mac(z.ih, z.il, a[i].rh, a[i].rl, bb[j].ih, bb[j].il);
-              df_mac(z.ih, z.il, a[i].ih, a[i].il, bb[j].rh, bb[j].rl);
-            } else {
+            if constexpr (!DF) {
               acc[i][j].x = fma(a[i].x, bb[j].x, acc[i][j].x);
               acc[i][j].x = fma(-a[i].y, bb[j].y, acc[i][j].x);
               acc[i][j].y = fma(a[i].x, bb[j].y, acc[i][j].y);

@@ -53,6 +53,7 @@ struct hh_ctx {
   // HH_PREC_FP32 (the transformed wave only starts Lanczos)
   int transform_precision = 0;
   int restart_precision = HH_PREC_FP32X2;  // the split Lanczos's energy-setting product
+  int renorm_precision = 0;                // hh_renormalize's products (FP64 or FP32X2)
   // device address of the static scratch array of hh_matvec_noalloc, looked
   // up by hh_init in this context (noalloc.cu); null with a reason if that
   // lookup failed

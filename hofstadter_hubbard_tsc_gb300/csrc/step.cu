@@ -25,9 +25,9 @@ struct GemmRun {
   hh_gemm_list L;
   // queued on the context stream; the task list returns to the pool in
   // stream order, so nothing here waits for the device
-  int run(hh_ctx* ctx, double2* base_in, double2* base_scr, double2* base_out, bool fp32 = false) {
+  int run(hh_ctx* ctx, double2* base_in, double2* base_scr, double2* base_out, int arith = kArithFp64) {
     L.upload(ctx);
-    cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream, fp32 ? kArithFp32 : kArithFp64);
+    cudaError_t e = launch_segment_gemm_fp64(L, base_in, base_scr, base_out, ctx->stream, arith);
     L.release();
     return cuda_check(ctx, e, "step GEMM");
   }
@@ -258,6 +258,12 @@ extern "C" int hh_ctx_set_transform_precision(hh_ctx_t* ctx, int precision) {
   return HH_OK;
 }
 
+extern "C" int hh_ctx_set_renormalize_precision(hh_ctx_t* ctx, int precision) {
+  if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32X2)) return HH_ERR_INVALID;
+  ctx->renorm_precision = precision;
+  return HH_OK;
+}
+
 extern "C" int hh_ctx_set_restart_precision(hh_ctx_t* ctx, int precision) {
   if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32X2)) return HH_ERR_INVALID;
   ctx->restart_precision = precision;
@@ -348,8 +354,9 @@ extern "C" int hh_renormalize(hh_ctx_t* ctx, const hh_block_t* ori, const hh_blo
     hh_block_free(eff);
     return cuda_check(ctx, e, "renormalise scratch");
   }
-  st = G1.run(ctx, nullptr, d_scr, eff->d);
-  if (!st) st = G2.run(ctx, nullptr, d_scr, eff->d);
+  const int arith = ctx->renorm_precision == HH_PREC_FP32X2 ? kArithDf : kArithFp64;
+  st = G1.run(ctx, nullptr, d_scr, eff->d, arith);
+  if (!st) st = G2.run(ctx, nullptr, d_scr, eff->d, arith);
   dev_free(ctx, d_scr);
   if (st) {
     hh_block_free(eff);
@@ -486,9 +493,9 @@ extern "C" int hh_wave_transform(hh_ctx_t* ctx, int dir, const hh_basis_t* sys_b
     dev_free(ctx, d_scr);
     return cuda_check(ctx, e, "wave transform scratch");
   }
-  const bool fp32 = ctx->transform_precision == HH_PREC_FP32;
-  int st = G1.run(ctx, old_wave->d, d_scr, new_wave->d, fp32);
-  if (!st) st = G2.run(ctx, old_wave->d, d_scr, new_wave->d, fp32);
+  const int arith = ctx->transform_precision == HH_PREC_FP32 ? kArithFp32 : kArithFp64;
+  int st = G1.run(ctx, old_wave->d, d_scr, new_wave->d, arith);
+  if (!st) st = G2.run(ctx, old_wave->d, d_scr, new_wave->d, arith);
   dev_free(ctx, d_scr);
   if (st) return st;
   return hh_wave_normalize(new_wave);

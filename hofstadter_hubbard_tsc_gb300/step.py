@@ -25,8 +25,13 @@ def density_truncate(dev, wave, side, kept_min, kept_max, trun_err):
     return DBlock.from_handle(dev, h), ns.value, err.value, ent.value, spec[:dim]
 
 
-def update_trun(dev, op, trun, dia):
-    """update_trun_dia (dia=True) / update_trun_ndia: T^H O T."""
+def update_trun(dev, op, trun, dia, precision=_lib.HH_PREC_FP64):
+    """update_trun_dia (dia=True) / update_trun_ndia: T^H O T.
+
+    precision: HH_PREC_FP64 (the reference's arithmetic) or HH_PREC_FP32X2
+    (double-float, the block operators of a split-precision sweep); set on
+    the context for every call."""
+    dev.check(dev.lib.hh_ctx_set_renormalize_precision(dev.h, int(precision)))
     h = C.c_void_p()
     dev.check(dev.lib.hh_renormalize(dev.h, op.h, trun.h, 1 if dia else 0, C.byref(h)))
     return DBlock.from_handle(dev, h)

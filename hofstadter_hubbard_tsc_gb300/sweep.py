@@ -68,6 +68,13 @@ class GPUDMRG:
         self.guess_kind = "random"     # how the next Lanczos start vector was made
         self.phase_s = defaultdict(float)   # host wall seconds per phase of a step
 
+    @property
+    def _block_precision(self):
+        """Arithmetic of the block renormalisations T^H O T: FP64 in an FP64
+        run (the reference's), double-float (FP64-class, on the FP32 pipe) in
+        a split-precision run."""
+        return _lib.HH_PREC_FP64 if self.precision == _lib.HH_PREC_FP64 else _lib.HH_PREC_FP32X2
+
     @contextmanager
     def _phase(self, name):
         """Host wall time of a phase, its device work included: the phase's
@@ -198,11 +205,11 @@ class GPUDMRG:
             for ii in range(1, nleg1 + 1):
                 dst = pre.sub.setdefault(ii, {})
                 for nm in names:
-                    dst[nm] = update_trun(dev, next_sub[ii][nm], trun, dia=(ij == 5))
+                    dst[nm] = update_trun(dev, next_sub[ii][nm], trun, dia=(ij == 5), precision=self._block_precision)
         for ii in list(pre.sub.keys()):
             if ii > lat.nleg11.get(L + 1, 0):
                 del pre.sub[ii]
-        pre.ham = update_trun(dev, next_ham, trun, dia=True)
+        pre.ham = update_trun(dev, next_ham, trun, dia=True, precision=self._block_precision)
         pre.len = L + 1
         return pre
 

@@ -86,6 +86,12 @@ int hh_ctx_set_transform_precision(hh_ctx_t* ctx, int precision);
  * (default; double-float on the FP32 pipe, which GB300 runs at 64 times its
  * FP64 rate) or HH_PREC_FP64.  No counterpart in the reference.           */
 int hh_ctx_set_restart_precision(hh_ctx_t* ctx, int precision);
+/* Arithmetic of hh_renormalize's products T^H O T: HH_PREC_FP64 (default,
+ * the reference's ZGEMM pair) or HH_PREC_FP32X2 (double-float on the FP32
+ * pipe, ~2^-47 per operation: the block operators of a split-precision sweep
+ * stay FP64-class at about a third of the FP64 time).  No counterpart in the
+ * reference.                                                              */
+int hh_ctx_set_renormalize_precision(hh_ctx_t* ctx, int precision);
 /* Diagnostic: every eigenpair of one dense Hermitian matrix A (n x n,
  * column-major, interleaved complex) through the tridiagonal pipeline of
  * HH_EIG_OWN (whatever n): w ascending (n doubles), V the eigenvectors

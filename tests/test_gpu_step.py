@@ -117,6 +117,16 @@ def test_renormalize(device):
                    [(s.num_up, s.num_down, s.down_dif, s.row_dim, s.sdim) for s in got.subs]
             for a, b in zip(ref.subs, got.subs):
                 np.testing.assert_allclose(b.mat, a.mat, atol=1e-11)
+            # double-float products (the block operators of split-precision
+            # sweeps): FP64-class, then the context back at FP64
+            gdf = step.update_trun(device, DBlock.upload(device, H.block(blk)), d_trun, dia,
+                                   precision=_lib.HH_PREC_FP32X2).download()
+            for a, b in zip(ref.subs, gdf.subs):
+                np.testing.assert_allclose(b.mat, a.mat, atol=1e-11)
+            again = step.update_trun(device, DBlock.upload(device, H.block(blk)), d_trun, dia).download()
+            for a, b in zip(got.subs, again.subs):
+                np.testing.assert_array_equal(a.mat, b.mat)
+    assert device.lib.hh_ctx_set_renormalize_precision(device.h, _lib.HH_PREC_BF16X3) == -1
 
 
 def test_wave_transform(device, monkeypatch):
