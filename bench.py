@@ -345,7 +345,10 @@ def window_bench(dev, args):
     copy and runs the same K steps of left_to_right (code/warm_up.f90:1495-1671),
     each from the transformed guess of the step before, timed on the host with
     the device synchronised on both sides.  The corrector has no earlier sweep
-    to learn from here, so it records and stays on the plain guess."""
+    to learn from here, so it records and stays on the plain guess.  Riding on
+    the FP64 arm, untimed, every step's superblock is also solved by the split
+    Lanczos from the same start vector (the precisions compared on one
+    superblock and kept basis, step by step)."""
     from hofstadter_hubbard_tsc_gb300 import _lib
     from hofstadter_hubbard_tsc_gb300.device import DWave
     from hofstadter_hubbard_tsc_gb300.lattice import SquareLattice
@@ -376,6 +379,29 @@ def window_bench(dev, args):
 
     snap = (dict(d.sys_models), dict(d.env_models), dict(d.sys_truns), dict(d.env_truns), dict(d.sys_bases),
             dict(d.env_bases), copy_wave(d.wave), len(d.energies))
+
+    class SameSuperblock:
+        """Rides on the FP64 arm (its time is taken out of that arm's): every
+        step's superblock is solved a second time by the split-precision
+        Lanczos from the same start vector, so each step compares the two
+        precisions on one superblock and one kept basis."""
+
+        def __init__(self):
+            self.start, self.E, self.seconds = None, [], 0.0
+
+        def __call__(self, dmrg, sb, psi, when):
+            t0 = time.perf_counter()
+            if when == "before":
+                self.start = DWave(dev, psi.layout, psi.sys_len, psi.env_len)
+                dev.check(dev.lib.hh_wave_copy(self.start.h, psi.h))
+            else:
+                e, _ = sb.lanczos_device(self.start, dmrg.lanzero, dmrg.maxit, precision=split)
+                self.E.append(e)
+                self.start.free()
+            dev.sync()
+            self.seconds += time.perf_counter() - t0
+
+    same = SameSuperblock()
     out = {"config": f"hubbard-cylinder-4x{L}-phi0.25-U8-Ne{ne}-m{m}-midchain-window", "steps": K,
            "lanzero": 1e-10, "split_precision": args.precision if args.precision != "fp64" else "bf16x3",
            "start": f"infinite-system warm-up to the middle + 1 left-to-right step in split precision "
@@ -389,13 +415,16 @@ def window_bench(dev, args):
         d.wave = copy_wave(snap[6])
         del d.energies[snap[7]:]
         d.precision = prec
-        d.guess_hook = hook if name == "split" else None
+        d.guess_hook = hook if name == "split" else same
         d.phase_s.clear()
         dev.sync()
         t0 = time.perf_counter()
         d.left_to_right(N // 2, N // 2 + K)
         dev.sync()
         dt = time.perf_counter() - t0
+        if name == "fp64":  # the same-superblock solves are not the FP64 arm's work
+            dt -= same.seconds
+            d.phase_s.pop("guess", None)
         steps = d.energies[-K:]
         out[name] = {"window_s": dt, "s_per_step": dt / K, "E0": [e[2] for e in steps],
                      "lanczos_iterations": [int(e[3]) for e in steps],
@@ -410,6 +439,10 @@ def window_bench(dev, args):
     # precision); later steps follow each arm's own truncations, whose kept
     # bases move with the converged vector within the Lanczos tolerance
     out["rel_dE_first_step"] = out["rel_dE_per_step"][0]
+    # every step's FP64 superblock solved again in split precision, same start
+    out["rel_dE_same_superblock_per_step"] = (np.abs(np.array(same.E) - e64) / np.abs(e64)).tolist()
+    out["rel_dE_same_superblock"] = float(np.max(out["rel_dE_same_superblock_per_step"]))
+    out["same_superblock_check_s"] = round(same.seconds, 3)
     out["sweep_speedup_split_vs_fp64"] = out["fp64"]["window_s"] / out["split"]["window_s"]
     hook.free()
     d.sys_models = d.env_models = d.sys_truns = d.env_truns = d.sys_bases = d.env_bases = {}
