@@ -38,12 +38,30 @@ struct alignas(16) df2 {
   float rh, rl, ih, il;
 };
 
+// x = h + l to 2^-47: h is x's leading 24 significand bits (truncated), l
+// the remaining 29 rounded to a float.  Built from the bit pattern on the
+// integer and FP32 pipes (GB300 converts FP64 on its FP64 pipe, at 1/64 of
+// the FP32 rate) wherever both parts are normal floats, |x| in [2^-74,
+// 2^127]; elsewhere (zero, tiny or huge values) by FP64 conversions.
+__device__ __forceinline__ void split_f64(double x, float& h, float& l) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((u >> 52) & 0x7FF);
+  if (e >= 949 && e <= 1150) {
+    const unsigned sign = (unsigned)(u >> 63) << 31;
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
+    const float r = __fmul_rn(__uint2float_rn((unsigned)(m & 0x1FFFFFFFu)), __uint_as_float((unsigned)(e - 948) << 23));
+    l = __uint_as_float(__float_as_uint(r) | sign);
+  } else {
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+  }
+}
+
 __device__ __forceinline__ df2 to_df(double2 v) {
   df2 r;
-  r.rh = __double2float_rn(v.x);
-  r.rl = __double2float_rn(v.x - (double)r.rh);
-  r.ih = __double2float_rn(v.y);
-  r.il = __double2float_rn(v.y - (double)r.ih);
+  split_f64(v.x, r.rh, r.rl);
+  split_f64(v.y, r.ih, r.il);
   return r;
 }
 
@@ -71,6 +89,19 @@ __device__ __forceinline__ void df_renorm(float& sh, float& sl) {
   const float bv = __fsub_rn(s, sh);
   sl = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bv)), __fsub_rn(sl, bv));
   sh = s;
+}
+
+// c v for double-float complex numbers (the segment coefficient on a staged
+// operand), renormalised
+__device__ __forceinline__ df2 df_cmul(const df2& c, const df2& v) {
+  df2 r{0.f, 0.f, 0.f, 0.f};
+  df_mac(r.rh, r.rl, c.rh, c.rl, v.rh, v.rl);
+  df_mac(r.rh, r.rl, -c.ih, -c.il, v.ih, v.il);
+  df_mac(r.ih, r.il, c.rh, c.rl, v.ih, v.il);
+  df_mac(r.ih, r.il, c.ih, c.il, v.rh, v.rl);
+  df_renorm(r.rh, r.rl);
+  df_renorm(r.ih, r.il);
+  return r;
 }
 
 // (sh, sl) += x for an FP64 x (copy terms)
@@ -160,6 +191,10 @@ __global__ void __launch_bounds__(NT, ARITH == kArithDf ? 2 : 0) seg_gemm_fp64_k
       continue;
     }
     const double2* Q = resolve(s.qoff, s.qbase, in, scr, out);
+    // double-float: the coefficient applied after the split (FP32 pipe)
+    const bool c_one = s.cre == 1.0 && s.cim == 0.0;
+    df2 c_df{0.f, 0.f, 0.f, 0.f};
+    if constexpr (DF) c_df = to_df(c);
     for (int k0 = 0; k0 < s.K; k0 += TK) {
       const int krem = min(TK, s.K - k0);
       // stage the P tile (TM x TK), scaled by the segment coefficient
@@ -176,9 +211,12 @@ __global__ void __launch_bounds__(NT, ARITH == kArithDf ? 2 : 0) seg_gemm_fp64_k
             v = P[(long long)(k0 + kk) + (long long)(t.m0 + m) * s.ldp];
             if (s.opP == HH_OP_C) v.y = -v.y;
           }
-          v = cmul(c, v);
+          if constexpr (!DF) v = cmul(c, v);
         }
-        Ps[kk][m] = narrow(v);
+        if constexpr (DF)
+          Ps[kk][m] = c_one ? to_df(v) : df_cmul(c_df, to_df(v));
+        else
+          Ps[kk][m] = narrow(v);
       }
 #pragma unroll
       for (int r = 0; r < (TN * TK) / NT; ++r) {
