@@ -696,7 +696,8 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   int ntiles[2 * kSteps] = {};
   for (int stp = 0; stp < kSteps; ++stp) {
     const long long zin = (stp % 2 == 0) ? 0 : zt, zout = (stp % 2 == 0) ? zt : 0, g0 = 2 * zt;
-    for (const Blk& b : blks) {
+    for (size_t bi = 0; bi < blks.size(); ++bi) {
+      const Blk& b = blks[bi];
       tri::GemmItem G{};
       G.a = zin + b.zoff; G.b = zin + b.zoff; G.c = g0 + b.goff; G.c0 = G.c;
       G.M = b.k; G.N = b.k; G.K = b.n;
@@ -704,6 +705,8 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
       G.alpha = 1.0; G.beta = 0.0;
       G.tiles_n = (b.k + 63) / 64;
       G.tile0 = ntiles[2 * stp];
+      G.gate = (int)bi + 1;
+      G.step = stp;
       ntiles[2 * stp] += ((b.k + 63) / 64) * G.tiles_n;
       gi[2 * stp].push_back(G);
       tri::GemmItem H{};
@@ -713,11 +716,17 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
       H.alpha = -0.5; H.beta = 1.5;
       H.tiles_n = (b.k + 63) / 64;
       H.tile0 = ntiles[2 * stp + 1];
+      H.gate = (int)bi + 1;
+      H.step = stp;
       ntiles[2 * stp + 1] += ((b.n + 63) / 64) * H.tiles_n;
       gi[2 * stp + 1].push_back(H);
     }
   }
   const long long final_z = (kSteps % 2 == 1) ? zt : 0;
+  // after the first step's Gram matrices: the steps each block needs (a
+  // skipped step copies its Z, so the result stays at final_z)
+  std::vector<tri::NsBlock> nsb;
+  for (const Blk& b : blks) nsb.push_back(tri::NsBlock{2 * zt + b.goff, b.k, 0});
   // Cholesky QR of the large clusters: item lists of its launches.  Z blocks
   // are row-major (element (i, j) of a block at zoff + i k + j); T, the
   // first pass's result, sits in the Newton-Schulz buffer's second half.
@@ -768,6 +777,8 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
     c.take<tri::CgsBlock>(cgs.size());
     c.take<tri::CgsBlock>(cgs_low.size());
     c.take<int2>(clusters.size());
+    c.take<tri::NsBlock>(nsb.size());
+    c.take<int>(nsb.size());
     need = c.off;
   }
   int st = reserve(ctx, &S->d_buf3, &S->cap3, need, "allocate eigenvector workspace");
@@ -788,6 +799,8 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   tri::CgsBlock* d_cgs = c.take<tri::CgsBlock>(cgs.size());
   tri::CgsBlock* d_cgs_low = c.take<tri::CgsBlock>(cgs_low.size());
   int2* d_clusters = c.take<int2>(clusters.size());
+  tri::NsBlock* d_nsb = c.take<tri::NsBlock>(nsb.size());
+  int* d_need = c.take<int>(nsb.size());
   auto up = [&](void* dst, const void* src, size_t bytes) {
     if (e == cudaSuccess && bytes > 0) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
   };
@@ -800,6 +813,7 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
   up(d_cgs, cgs.data(), cgs.size() * sizeof(tri::CgsBlock));
   up(d_cgs_low, cgs_low.data(), cgs_low.size() * sizeof(tri::CgsBlock));
   up(d_clusters, clusters.data(), clusters.size() * sizeof(int2));
+  up(d_nsb, nsb.data(), nsb.size() * sizeof(tri::NsBlock));
   if (e != cudaSuccess) return cuda_check(ctx, e, "eigenvector work lists");
   if (nitems > 0) {
     e = tri::inverse_iteration(R.d_secs, d_inv, nitems, maxn, R.d_d, R.d_e, R.d_w, d_z, d_lu, s);
@@ -817,7 +831,10 @@ int eig_vectors(hh_ctx* ctx, const std::vector<int>& ncol, double2* X, const std
       if (e == cudaSuccess) e = tri::gemm(d_qr[5], (int)app2.size(), nt_app2, d_z, s);
     }
     if (e == cudaSuccess) e = tri::cgs2(d_cgs_low, (int)cgs_low.size(), d_clusters, maxk, d_z, s);
-    for (int q = 0; q < 2 * kSteps && e == cudaSuccess; ++q) e = tri::gemm(d_gi[q], (int)gi[q].size(), ntiles[q], d_z, s);
+    for (int q = 0; q < 2 * kSteps && e == cudaSuccess; ++q) {
+      e = tri::gemm(d_gi[q], (int)gi[q].size(), ntiles[q], d_z, s, q == 0 ? nullptr : d_need);
+      if (q == 0 && e == cudaSuccess) e = tri::ns_gate(d_nsb, (int)nsb.size(), d_z, d_need, s);
+    }
     if (e == cudaSuccess) e = tri::backtransform(R.d_secs, d_bt, (int)bt.size(), R.A, R.d_tau, d_z + final_z, X, s);
     if (e != cudaSuccess) return cuda_check(ctx, e, "kept eigenvectors (inverse iteration)");
   }

@@ -919,7 +919,8 @@ __global__ void __launch_bounds__(512) chol_inv_kernel(const CholItem* __restric
 constexpr int kTile = 64, kKc = 16, kGemmThreads = 256;
 
 __global__ void __launch_bounds__(kGemmThreads)
-    gemm_kernel(const GemmItem* __restrict__ items, int nitems, double* __restrict__ buf) {
+    gemm_kernel(const GemmItem* __restrict__ items, int nitems, double* __restrict__ buf,
+                const int* __restrict__ need) {
   // the item owning this tile (items sorted by tile0)
   int lo = 0, hi = nitems - 1;
   while (lo < hi) {
@@ -932,6 +933,16 @@ __global__ void __launch_bounds__(kGemmThreads)
   const GemmItem G = items[lo];
   const int tile = blockIdx.x - G.tile0;
   const int m0 = (tile / G.tiles_n) * kTile, n0 = (tile % G.tiles_n) * kTile;
+  if (need && G.gate > 0 && G.step >= need[G.gate - 1]) {  // a Newton-Schulz step this block skips
+    if (G.beta != 0.0)
+      for (int x = threadIdx.x; x < kTile * kTile; x += kGemmThreads) {
+        const int gi = m0 + x / kTile, gj = n0 + x % kTile;
+        if (gi < G.M && gj < G.N)
+          buf[G.c + (long long)gi * G.c_r + (long long)gj * G.c_c] =
+              buf[G.c0 + (long long)gi * G.c_r + (long long)gj * G.c_c];
+      }
+    return;
+  }
   __shared__ double As[kKc][kTile + 1];
   __shared__ double Bs[kKc][kTile + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // 4 x 4 outputs per thread
@@ -972,6 +983,31 @@ __global__ void __launch_bounds__(kGemmThreads)
         buf[G.c + (long long)gi * G.c_r + (long long)gj * G.c_c] = v;
       }
     }
+}
+
+// need[b] from delta = max |G_b - I| (one CTA per block; NaN counts as large)
+__global__ void __launch_bounds__(256) ns_gate_kernel(const NsBlock* __restrict__ blocks, const double* __restrict__ buf,
+                                                      int* __restrict__ need) {
+  const NsBlock B = blocks[blockIdx.x];
+  const double* G = buf + B.goff;
+  double d = 0.0;
+  const long long kk = (long long)B.k * B.k;
+  for (long long x = threadIdx.x; x < kk; x += blockDim.x) {
+    const double v = fabs(G[x] - ((x / B.k == x % B.k) ? 1.0 : 0.0));
+    d = (v > d || v != v) ? v : d;  // a NaN propagates
+  }
+  __shared__ double sh[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    const double w = __shfl_xor_sync(0xffffffffu, d, o);
+    d = (w > d || w != w) ? w : d;
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int q = 0; q < 8; ++q) m = (sh[q] > m || sh[q] != sh[q]) ? sh[q] : m;
+    need[blockIdx.x] = (m <= 1e-8) ? 1 : (m <= 1e-4) ? 2 : 3;
+  }
 }
 
 // ---------------------------------------------------------- backtransform
@@ -1208,9 +1244,15 @@ cudaError_t chol_inv(const CholItem* d_items, int nitems, double* buf, cudaStrea
   return cudaGetLastError();
 }
 
-cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s) {
+cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s, const int* need) {
   if (nitems <= 0 || ntiles <= 0) return cudaSuccess;
-  gemm_kernel<<<(unsigned)ntiles, kGemmThreads, 0, s>>>(d_items, nitems, buf);
+  gemm_kernel<<<(unsigned)ntiles, kGemmThreads, 0, s>>>(d_items, nitems, buf, need);
+  return cudaGetLastError();
+}
+
+cudaError_t ns_gate(const NsBlock* d_blocks, int nblocks, const double* buf, int* need, cudaStream_t s) {
+  if (nblocks <= 0) return cudaSuccess;
+  ns_gate_kernel<<<(unsigned)nblocks, 256, 0, s>>>(d_blocks, buf, need);
   return cudaGetLastError();
 }
 

@@ -40,6 +40,16 @@ struct GemmItem {
   double alpha, beta;
   int tiles_n;     // tiles along N
   int tile0;       // first tile of this item in the launch
+  int gate;        // Newton-Schulz items: 1 + their block (0: always run)
+  int step;        // ... and their step: skipped when step >= need[gate - 1]; a
+                   // skipped item with beta != 0 copies C0 to C instead
+};
+
+// The Gram matrix of one Newton-Schulz block (k x k at goff) after its first
+// step's G = Z^T Z.
+struct NsBlock {
+  long long goff;
+  int k, pad;
 };
 
 // Back-transformation X = Q Z of kBtCols columns of one sector.
@@ -103,8 +113,14 @@ cudaError_t cgs2(const CgsBlock* d_blocks, int nblocks, const int2* d_clusters, 
 // R^{-1} of the Cholesky factor of each item's Gram matrix, one CTA per item
 // (orthonormalisation of large degenerate clusters by Cholesky QR)
 cudaError_t chol_inv(const CholItem* d_items, int nitems, double* buf, cudaStream_t s);
-// batched strided FP64 GEMMs, ntiles = total 64 x 64 tiles of the items
-cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s);
+// batched strided FP64 GEMMs, ntiles = total 64 x 64 tiles of the items;
+// need (may be null) gates the Newton-Schulz items
+cudaError_t gemm(const GemmItem* d_items, int nitems, int ntiles, double* buf, cudaStream_t s,
+                 const int* need = nullptr);
+// Newton-Schulz steps each block needs, from delta = max |G - I| of its first
+// Gram matrix: the error after a step is about (3/4) delta^2, so 1 step for
+// delta <= 1e-8, 2 for delta <= 1e-4, else 3
+cudaError_t ns_gate(const NsBlock* d_blocks, int nblocks, const double* buf, int* need, cudaStream_t s);
 // X = Q Z into the truncation operator
 cudaError_t backtransform(const Sector* d_secs, const BtItem* d_items, int nitems, const double2* den,
                           const double2* tau, const double* Z, double2* X, cudaStream_t s);
