@@ -73,6 +73,7 @@ SIGNATURES = {
     "hh_ctx_set_transform_precision": (I, [P, I]),
     "hh_ctx_set_restart_precision": (I, [P, I]),
     "hh_ctx_set_renormalize_precision": (I, [P, I]),
+    "hh_ctx_set_krylov_storage": (I, [P, I]),
     "hh_eig_selftest": (I, [P, I, DP, DP, DP]),
     "hh_block_create": (I, [P, I, I, I, I, IP, DP, PP]),
     "hh_block_zeros": (I, [P, I, I, I, I, IP, PP]),

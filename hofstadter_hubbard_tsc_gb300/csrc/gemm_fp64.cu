@@ -435,7 +435,13 @@ __global__ void scale_kernel(double2* y, double a, long long n) {
 
 // Re<V_j, w> for j < k: one pass over w; partial sums per CTA, k <= 128.
 constexpr int KMAX = 128;
-__global__ void krylov_dots_kernel(const double2* V, int k, long long ld, const double2* w, long long n,
+// (V holds double2 or float2 vectors: the split Lanczos's first pass keeps
+// its Krylov basis in FP32, products and sums in FP64)
+__device__ __forceinline__ double2 widen(double2 v) { return v; }
+__device__ __forceinline__ double2 widen(float2 v) { return make_double2(v.x, v.y); }
+
+template <class VT>
+__global__ void krylov_dots_kernel(const VT* V, int k, long long ld, const double2* w, long long n,
                                    double* part) {
   __shared__ double sh[KMAX][RB / 32 + 1];
   double acc[8];
@@ -448,7 +454,7 @@ __global__ void krylov_dots_kernel(const double2* V, int k, long long ld, const 
 #pragma unroll
       for (int j = 0; j < 8; ++j)
         if (j < jn) {
-          double2 v = V[(long long)(j0 + j) * ld + i];
+          const double2 v = widen(V[(long long)(j0 + j) * ld + i]);
           acc[j] = fma(v.x, x.x, acc[j]);
           acc[j] = fma(v.y, x.y, acc[j]);
         }
@@ -484,7 +490,8 @@ __global__ void krylov_reduce_kernel(const double* part, int nblk, int k, double
 }
 
 // w -= sum_j c_j V_j  (sign = -1) or out = sum_j c_j V_j (sign = 0)
-__global__ void krylov_axpy_kernel(const double2* V, int k, long long ld, double2* w, long long n,
+template <class VT>
+__global__ void krylov_axpy_kernel(const VT* V, int k, long long ld, double2* w, long long n,
                                    const double* coef, int overwrite) {
   __shared__ double c[KMAX];
   for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = coef[j];
@@ -492,7 +499,7 @@ __global__ void krylov_axpy_kernel(const double2* V, int k, long long ld, double
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double2 s = make_double2(0.0, 0.0);
     for (int j = 0; j < k; ++j) {
-      double2 v = V[(long long)j * ld + i];
+      const double2 v = widen(V[(long long)j * ld + i]);
       s.x = fma(c[j], v.x, s.x);
       s.y = fma(c[j], v.y, s.y);
     }
@@ -504,6 +511,30 @@ __global__ void krylov_axpy_kernel(const double2* V, int k, long long ld, double
       o.y -= s.y;
       w[i] = o;
     }
+  }
+}
+
+// v = FP32 rounding of w, and the partial sums of <v|v> per CTA (sum_kernel
+// finishes them): a new Krylov vector stored in FP32 with the norm of what
+// was stored
+__global__ void store_f32_kernel(const double2* __restrict__ w, float2* __restrict__ v, long long n,
+                                 double* __restrict__ part) {
+  __shared__ double sh[RB / 32];
+  double s = 0.0;
+  for (long long i = blockIdx.x * (long long)RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB) {
+    const double2 x = w[i];
+    const float2 f = make_float2(__double2float_rn(x.x), __double2float_rn(x.y));
+    v[i] = f;
+    s = fma((double)f.x, (double)f.x, s);
+    s = fma((double)f.y, (double)f.y, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < RB / 32 ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
   }
 }
 
@@ -613,28 +644,52 @@ cudaError_t wave_scale(double2* y, double a, long long n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t krylov_dots(const double2* V, int k, long long ld, const double2* w, long long n, double* d_out,
+template <class VT>
+cudaError_t krylov_dots(const VT* V, int k, long long ld, const double2* w, long long n, double* d_out,
                         cudaStream_t s) {
   // d_out: [0, KMAX) results, then nblk*KMAX partials
   if (k > KMAX) return cudaErrorInvalidValue;
   int g = grid_for(n, RB);
   if (g > 512) g = 512;
-  krylov_dots_kernel<<<g, RB, 0, s>>>(V, k, ld, w, n, d_out + KMAX);
+  krylov_dots_kernel<VT><<<g, RB, 0, s>>>(V, k, ld, w, n, d_out + KMAX);
   krylov_reduce_kernel<<<k, 256, 0, s>>>(d_out + KMAX, g, k, d_out);
   return cudaGetLastError();
 }
 
-cudaError_t krylov_update(const double2* V, int k, long long ld, double2* w, long long n, const double* d_coef,
+template <class VT>
+cudaError_t krylov_update(const VT* V, int k, long long ld, double2* w, long long n, const double* d_coef,
                           cudaStream_t s) {
   if (k > KMAX) return cudaErrorInvalidValue;
-  krylov_axpy_kernel<<<grid_for(n, 256), 256, 0, s>>>(V, k, ld, w, n, d_coef, 0);
+  krylov_axpy_kernel<VT><<<grid_for(n, 256), 256, 0, s>>>(V, k, ld, w, n, d_coef, 0);
   return cudaGetLastError();
 }
 
-cudaError_t krylov_combine(const double2* V, int k, long long ld, double2* out, long long n, const double* d_coef,
+template <class VT>
+cudaError_t krylov_combine(const VT* V, int k, long long ld, double2* out, long long n, const double* d_coef,
                            cudaStream_t s) {
   if (k > KMAX) return cudaErrorInvalidValue;
-  krylov_axpy_kernel<<<grid_for(n, 256), 256, 0, s>>>(V, k, ld, out, n, d_coef, 1);
+  krylov_axpy_kernel<VT><<<grid_for(n, 256), 256, 0, s>>>(V, k, ld, out, n, d_coef, 1);
+  return cudaGetLastError();
+}
+
+template cudaError_t krylov_dots<double2>(const double2*, int, long long, const double2*, long long, double*,
+                                          cudaStream_t);
+template cudaError_t krylov_dots<float2>(const float2*, int, long long, const double2*, long long, double*,
+                                         cudaStream_t);
+template cudaError_t krylov_update<double2>(const double2*, int, long long, double2*, long long, const double*,
+                                            cudaStream_t);
+template cudaError_t krylov_update<float2>(const float2*, int, long long, double2*, long long, const double*,
+                                           cudaStream_t);
+template cudaError_t krylov_combine<double2>(const double2*, int, long long, double2*, long long, const double*,
+                                             cudaStream_t);
+template cudaError_t krylov_combine<float2>(const float2*, int, long long, double2*, long long, const double*,
+                                            cudaStream_t);
+
+cudaError_t krylov_store_f32(const double2* w, float2* v, long long n, double* vv, double* part, cudaStream_t s) {
+  int g = grid_for(n, RB);
+  if (g > 1024) g = 1024;
+  store_f32_kernel<<<g, RB, 0, s>>>(w, v, n, part);
+  sum_kernel<<<1, RB, 0, s>>>(part, g, vv);
   return cudaGetLastError();
 }
 

@@ -918,13 +918,21 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
   if (maxit > 100) maxit = 100;  // loop_in (code/lanczos.f90:14)
   const long long n = p->nelem;
   const int slots = maxit + 1;
-  if (p->krylov_cap < slots) {
+  // The split first pass (its products split precision from the start) keeps
+  // its Krylov basis in FP32, half the bytes of the Gram-Schmidt passes: its
+  // products carry ~1e-5 relative error and it stops at a 1e-8 Ritz change,
+  // and the restart pass (FP64 basis) fixes the energy.  The three newest
+  // vectors stay FP64 (the recurrence and the products use them), at the
+  // start of the same buffer.
+  const bool f32 = split_of(first_precision) && ctx->krylov_f32;
+  const int cap = std::max(slots, 3 + (slots + 1) / 2);  // in FP64 vectors
+  if (p->krylov_cap < cap) {
     dev_free(ctx, p->d_krylov);
     p->d_krylov = nullptr;
     p->krylov_cap = 0;
-    cudaError_t e = dev_alloc(ctx, (void**)&p->d_krylov, (size_t)slots * n * sizeof(double2));
+    cudaError_t e = dev_alloc(ctx, (void**)&p->d_krylov, (size_t)cap * n * sizeof(double2));
     if (e != cudaSuccess) return cuda_check(ctx, e, "cudaMalloc(Krylov basis)");
-    p->krylov_cap = slots;
+    p->krylov_cap = cap;
   }
   // d_red: [0, KRY) Gram-Schmidt coefficients and partials, then the scalars
   constexpr size_t KRY = 128 + 600 * 128;
@@ -965,40 +973,61 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
     return HH_OK;
   };
   std::vector<double> alpha, beta;
-  cudaError_t e = cudaMemcpyAsync(slot(0), psi->d, n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess) e = dot_into(slot(0), slot(0), d_w2);
+  // cur = v_{last-1}, prev = v_{last-2}, w = the product, then the next
+  // vector: basis slots (FP64 basis), or three rotating FP64 vectors beside
+  // the FP32 basis V32
+  float2* V32 = reinterpret_cast<float2*>(V + 3 * n);
+  double2* cur = f32 ? V : slot(0);
+  double2* prev = f32 ? V + 2 * n : nullptr;
+  double2* w = f32 ? V + n : slot(1);
+  // <v_j|v_j> of a new basis vector (and its FP32 copy)
+  auto store = [&](const double2* v, int j) {
+    return f32 ? krylov_store_f32(v, V32 + (size_t)j * n, n, d_vv + j, d_part, s) : dot_into(v, v, d_vv + j);
+  };
+  cudaError_t e = cudaMemcpyAsync(cur, psi->d, n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = dot_into(cur, cur, d_w2);
   if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos start");
   if ((st = fetch({d_w2}))) return st;
   if (!(ctx->h_red[0] > 0.0)) return fail(ctx, HH_ERR_NUMERIC, "Lanczos start vector is zero");
-  e = wave_scale_rsqrt_dev(slot(0), d_w2, nullptr, n, s);
-  if (e == cudaSuccess) e = dot_into(slot(0), slot(0), d_vv + 0);
+  e = wave_scale_rsqrt_dev(cur, d_w2, nullptr, n, s);
+  if (e == cudaSuccess) e = store(cur, 0);
   if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos start");
   int last = 1;
-  if ((st = matvec_dev(p, slot(0), slot(1), first_precision, false))) return st;
-  if ((e = dot_into(slot(0), slot(1), d_alpha + 0)) != cudaSuccess) return cuda_check(ctx, e, "Lanczos alpha");
+  if ((st = matvec_dev(p, cur, w, first_precision, false))) return st;
+  if ((e = dot_into(cur, w, d_alpha + 0)) != cudaSuccess) return cuda_check(ctx, e, "Lanczos alpha");
   if ((st = fetch({d_alpha}))) return st;
   alpha.push_back(ctx->h_red[0]);
   double ritz = alpha[0];
   while (last < maxit) {
-    double2* w = slot(last);
     // three-term recurrence (code/lanczos.f90:65-75)
-    e = wave_axpy_dev(w, slot(last - 1), d_alpha + (last - 1), -1.0, n, s);
-    if (e == cudaSuccess && last >= 2) e = wave_axpy_dev(w, slot(last - 2), d_beta + (last - 2), -1.0, n, s);
+    e = wave_axpy_dev(w, cur, d_alpha + (last - 1), -1.0, n, s);
+    if (e == cudaSuccess && last >= 2) e = wave_axpy_dev(w, prev, d_beta + (last - 2), -1.0, n, s);
     // beta = ||w||, w /= beta
     if (e == cudaSuccess) e = dot_into(w, w, d_beta2 + (last - 1));
     if (e == cudaSuccess) e = wave_scale_rsqrt_dev(w, d_beta2 + (last - 1), d_beta + (last - 1), n, s);
     // Gram-Schmidt against all previous vectors, real inner product
     // (Gram_Schmidt_process, code/space_info.f90:1176-1214)
-    if (e == cudaSuccess) e = krylov_dots(V, last, n, w, n, ctx->d_red, s);
+    if (e == cudaSuccess) e = f32 ? krylov_dots(V32, last, n, w, n, ctx->d_red, s) : krylov_dots(V, last, n, w, n, ctx->d_red, s);
     if (e == cudaSuccess) e = divide_dev(ctx->d_red, d_vv, last, s);
-    if (e == cudaSuccess) e = krylov_update(V, last, n, w, n, ctx->d_red, s);
+    if (e == cudaSuccess)
+      e = f32 ? krylov_update(V32, last, n, w, n, ctx->d_red, s) : krylov_update(V, last, n, w, n, ctx->d_red, s);
     if (e == cudaSuccess) e = dot_into(w, w, d_w2);
     if (e == cudaSuccess) e = wave_scale_rsqrt_dev(w, d_w2, nullptr, n, s);
-    if (e == cudaSuccess) e = dot_into(w, w, d_vv + last);
+    if (e == cudaSuccess) e = store(w, last);
     if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos recurrence");
     ++last;
-    if ((st = matvec_dev(p, slot(last - 1), slot(last), precision, false))) return st;
-    if ((e = dot_into(slot(last - 1), slot(last), d_alpha + (last - 1))) != cudaSuccess)
+    if (f32) {
+      double2* t = prev;
+      prev = cur;
+      cur = w;
+      w = t;
+    } else {
+      prev = cur;
+      cur = w;
+      w = slot(last);
+    }
+    if ((st = matvec_dev(p, cur, w, precision, false))) return st;
+    if ((e = dot_into(cur, w, d_alpha + (last - 1))) != cudaSuccess)
       return cuda_check(ctx, e, "Lanczos alpha");
     if ((st = fetch({d_beta2 + (last - 2), d_alpha + (last - 1)}))) return st;
     const double b = std::sqrt(ctx->h_red[0]);
@@ -1023,7 +1052,8 @@ static int lanczos_core(hh_plan* p, hh_wave* psi, double lanzero, int maxit, int
   if ((st = tridiag_lowest(last, alpha.data(), beta.data(), &e0, z.data())))
     return fail(ctx, st, "tridiagonal eigensolver did not converge");
   e = cudaMemcpyAsync(ctx->d_red, z.data(), last * sizeof(double), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = krylov_combine(V, last, n, psi->d, n, ctx->d_red, s);
+  if (e == cudaSuccess)
+    e = f32 ? krylov_combine(V32, last, n, psi->d, n, ctx->d_red, s) : krylov_combine(V, last, n, psi->d, n, ctx->d_red, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_check(ctx, e, "Lanczos final combination");
   if ((st = hh_wave_normalize(psi))) return st;

@@ -54,6 +54,7 @@ struct hh_ctx {
   int transform_precision = 0;
   int restart_precision = HH_PREC_FP32X2;  // the split Lanczos's energy-setting product
   int renorm_precision = 0;                // hh_renormalize's products (FP64 or FP32X2)
+  bool krylov_f32 = true;                  // FP32 Krylov basis in the split Lanczos's first pass
   // device address of the static scratch array of hh_matvec_noalloc, looked
   // up by hh_init in this context (noalloc.cu); null with a reason if that
   // lookup failed
@@ -285,12 +286,19 @@ cudaError_t divide_dev(double* c, const double* d, int k, cudaStream_t s);
 cudaError_t wave_axpy(double2* y, const double2* x, double a, long long n, cudaStream_t s);
 cudaError_t wave_scale(double2* y, double a, long long n, cudaStream_t s);
 cudaError_t wave_fill_random(double2* w, long long n, unsigned long long seed, cudaStream_t s);
-cudaError_t krylov_dots(const double2* V, int k, long long ld, const double2* w, long long n,
+// Krylov bases of double2 (FP64) or float2 (the split Lanczos's first pass)
+// vectors; products and sums in FP64
+template <class VT>
+cudaError_t krylov_dots(const VT* V, int k, long long ld, const double2* w, long long n,
                         double* d_out, cudaStream_t s);
-cudaError_t krylov_update(const double2* V, int k, long long ld, double2* w, long long n,
+template <class VT>
+cudaError_t krylov_update(const VT* V, int k, long long ld, double2* w, long long n,
                           const double* d_coef, cudaStream_t s);
-cudaError_t krylov_combine(const double2* V, int k, long long ld, double2* out, long long n,
+template <class VT>
+cudaError_t krylov_combine(const VT* V, int k, long long ld, double2* out, long long n,
                            const double* d_coef, cudaStream_t s);
+// v = FP32 rounding of w, *vv = <v|v> (part: >= 1024 partials)
+cudaError_t krylov_store_f32(const double2* w, float2* v, long long n, double* vv, double* part, cudaStream_t s);
 int build_plan(hh_ctx* ctx, const hh_basis* sb, const hh_basis* eb, const hh_wave* layout,
                int nterm, const hh_term_t* terms, hh_plan* plan);
 int build_tc_plan(hh_plan* plan);

@@ -264,6 +264,12 @@ extern "C" int hh_ctx_set_renormalize_precision(hh_ctx_t* ctx, int precision) {
   return HH_OK;
 }
 
+extern "C" int hh_ctx_set_krylov_storage(hh_ctx_t* ctx, int precision) {
+  if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32)) return HH_ERR_INVALID;
+  ctx->krylov_f32 = precision == HH_PREC_FP32;
+  return HH_OK;
+}
+
 extern "C" int hh_ctx_set_restart_precision(hh_ctx_t* ctx, int precision) {
   if (!ctx || (precision != HH_PREC_FP64 && precision != HH_PREC_FP32X2)) return HH_ERR_INVALID;
   ctx->restart_precision = precision;

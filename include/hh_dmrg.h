@@ -92,6 +92,11 @@ int hh_ctx_set_restart_precision(hh_ctx_t* ctx, int precision);
  * stay FP64-class at about a third of the FP64 time).  No counterpart in the
  * reference.                                                              */
 int hh_ctx_set_renormalize_precision(hh_ctx_t* ctx, int precision);
+/* Storage of the Krylov basis in the first pass of the split-precision
+ * hh_lanczos: HH_PREC_FP32 (default; half the bytes of its Gram-Schmidt
+ * passes, far below the split products' own error) or HH_PREC_FP64.  The
+ * restart pass keeps an FP64 basis.  No counterpart in the reference.     */
+int hh_ctx_set_krylov_storage(hh_ctx_t* ctx, int precision);
 /* Diagnostic: every eigenpair of one dense Hermitian matrix A (n x n,
  * column-major, interleaved complex) through the tridiagonal pipeline of
  * HH_EIG_OWN (whatever n): w ascending (n doubles), V the eigenvectors

@@ -149,9 +149,13 @@ def test_fp32x2_matvec_and_restart(device):
     assert abs(edf - e64) / abs(e64) < 1e-11, (edf, e64)
     try:
         for rp in (_lib.HH_PREC_FP64, _lib.HH_PREC_FP32X2):
-            device.check(device.lib.hh_ctx_set_restart_precision(device.h, rp))
-            emx, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_BF16X3)
-            assert abs(emx - e64) / abs(e64) < 1e-10, (rp, emx, e64)
+            for ks in (_lib.HH_PREC_FP64, _lib.HH_PREC_FP32):  # first pass's Krylov basis
+                device.check(device.lib.hh_ctx_set_restart_precision(device.h, rp))
+                device.check(device.lib.hh_ctx_set_krylov_storage(device.h, ks))
+                emx, _, _ = sb.lanczos_memo_new(H.wave(H.random_wave(sup, 9)), 1e-10, precision=_lib.HH_PREC_BF16X3)
+                assert abs(emx - e64) / abs(e64) < 1e-10, (rp, ks, emx, e64)
     finally:
         device.check(device.lib.hh_ctx_set_restart_precision(device.h, _lib.HH_PREC_FP32X2))
+        device.check(device.lib.hh_ctx_set_krylov_storage(device.h, _lib.HH_PREC_FP32))
+    assert device.lib.hh_ctx_set_krylov_storage(device.h, _lib.HH_PREC_BF16X3) == -1
     sb.free()
