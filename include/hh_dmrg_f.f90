@@ -43,7 +43,8 @@ module hh_dmrg_f
   use pubdata
   implicit none
 
-  integer(c_int), parameter :: HH_PREC_FP64 = 0, HH_PREC_BF16X6 = 1, HH_PREC_BF16X3 = 2
+  integer(c_int), parameter :: HH_PREC_FP64 = 0, HH_PREC_BF16X6 = 1, HH_PREC_BF16X3 = 2, &
+       HH_PREC_FP32 = 3, HH_PREC_FP32X2 = 4
   integer(c_int), parameter :: HH_BLOCK_VEC_DIA = 1, HH_VEC_BLOCK_DIA = 2, HH_SITE_VEC_SITE_DIA = 3, &
        HH_SITE_VEC_SITE_NDIA = 4, HH_BLOCK_SITE_VEC_NDIA = 5, HH_VEC_BLOCK_SITE_NDIA = 6, &
        HH_BLOCK_VEC_SITE_NDIA = 7, HH_SITE_VEC_BLOCK_NDIA = 8, HH_BLOCK_VEC_BLOCK_NDIA = 9, &
@@ -198,6 +199,20 @@ module hh_dmrg_f
       type(c_ptr), value :: ctx, sys_bs, env_bs, sys_trun, env_trun, old_wave, new_wave
       integer(c_int), value :: dir
     end function hh_wave_transform
+    ! arithmetic of the split hh_lanczos's restart product and of hh_renormalize
+    ! (HH_PREC_FP32X2: double-float, FP64-class, on the FP32 pipe)
+    integer(c_int) function hh_ctx_set_restart_precision(ctx, precision) &
+         bind(C, name="hh_ctx_set_restart_precision")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: precision
+    end function hh_ctx_set_restart_precision
+    integer(c_int) function hh_ctx_set_renormalize_precision(ctx, precision) &
+         bind(C, name="hh_ctx_set_renormalize_precision")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: precision
+    end function hh_ctx_set_renormalize_precision
     integer(c_long) function c_strlen(s) bind(C, name="strlen")
       import :: c_long, c_ptr
       type(c_ptr), value :: s
