@@ -435,33 +435,48 @@ __global__ void scale_kernel(double2* y, double a, long long n) {
 
 // Re<V_j, w> for j < k: one pass over w; partial sums per CTA, k <= 128.
 constexpr int KMAX = 128;
-// (V holds double2 or float2 vectors: the split Lanczos's first pass keeps
-// its Krylov basis in FP32, products and sums in FP64)
-__device__ __forceinline__ double2 widen(double2 v) { return v; }
-__device__ __forceinline__ double2 widen(float2 v) { return make_double2(v.x, v.y); }
-
+// V holds double2 vectors, or float2 ones (the split Lanczos's first pass
+// keeps its Krylov basis in FP32).  With float2 vectors the products run in
+// double-float on the FP32 pipe (df_mac; the FP64 operand split once per
+// element by split_f64): an FP64 FMA costs GB300 as much issue as some 80
+// FP32 operations, and these kernels make two per element and vector.
 template <class VT>
 __global__ void krylov_dots_kernel(const VT* V, int k, long long ld, const double2* w, long long n,
                                    double* part) {
+  constexpr bool F32V = std::is_same<VT, float2>::value;
   __shared__ double sh[KMAX][RB / 32 + 1];
   double acc[8];
+  float dh[8], dl[8];
   for (int j0 = 0; j0 < k; j0 += 8) {
     int jn = min(8, k - j0);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] = 0.0;
+    for (int j = 0; j < 8; ++j) acc[j] = 0.0, dh[j] = dl[j] = 0.f;
     for (long long i = blockIdx.x * (long long)RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB) {
       double2 x = w[i];
+      if constexpr (F32V) {
+        float xh, xl, yh, yl;
+        split_f64(x.x, xh, xl);
+        split_f64(x.y, yh, yl);
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        if (j < jn) {
-          const double2 v = widen(V[(long long)(j0 + j) * ld + i]);
-          acc[j] = fma(v.x, x.x, acc[j]);
-          acc[j] = fma(v.y, x.y, acc[j]);
-        }
+        for (int j = 0; j < 8; ++j)
+          if (j < jn) {
+            const float2 v = reinterpret_cast<const float2*>(V)[(long long)(j0 + j) * ld + i];
+            df_mac(dh[j], dl[j], v.x, 0.f, xh, xl);
+            df_mac(dh[j], dl[j], v.y, 0.f, yh, yl);
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (j < jn) {
+            const double2 v = reinterpret_cast<const double2*>(V)[(long long)(j0 + j) * ld + i];
+            acc[j] = fma(v.x, x.x, acc[j]);
+            acc[j] = fma(v.y, x.y, acc[j]);
+          }
+      }
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      double s = acc[j];
+      double s = F32V ? (double)dh[j] + (double)dl[j] : acc[j];
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if ((threadIdx.x & 31) == 0 && j < jn) sh[j0 + j][threadIdx.x >> 5] = s;
     }
@@ -493,15 +508,30 @@ __global__ void krylov_reduce_kernel(const double* part, int nblk, int k, double
 template <class VT>
 __global__ void krylov_axpy_kernel(const VT* V, int k, long long ld, double2* w, long long n,
                                    const double* coef, int overwrite) {
+  constexpr bool F32V = std::is_same<VT, float2>::value;
   __shared__ double c[KMAX];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = coef[j];
+  __shared__ float ch[KMAX], cl[KMAX];  // float2 vectors: the coefficients split once
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    c[j] = coef[j];
+    if constexpr (F32V) split_f64(coef[j], ch[j], cl[j]);
+  }
   __syncthreads();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double2 s = make_double2(0.0, 0.0);
-    for (int j = 0; j < k; ++j) {
-      const double2 v = widen(V[(long long)j * ld + i]);
-      s.x = fma(c[j], v.x, s.x);
-      s.y = fma(c[j], v.y, s.y);
+    if constexpr (F32V) {
+      float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
+      for (int j = 0; j < k; ++j) {
+        const float2 v = reinterpret_cast<const float2*>(V)[(long long)j * ld + i];
+        df_mac(xh, xl, ch[j], cl[j], v.x, 0.f);
+        df_mac(yh, yl, ch[j], cl[j], v.y, 0.f);
+      }
+      s = make_double2((double)xh + (double)xl, (double)yh + (double)yl);
+    } else {
+      for (int j = 0; j < k; ++j) {
+        const double2 v = reinterpret_cast<const double2*>(V)[(long long)j * ld + i];
+        s.x = fma(c[j], v.x, s.x);
+        s.y = fma(c[j], v.y, s.y);
+      }
     }
     if (overwrite) {
       w[i] = s;
