@@ -42,7 +42,7 @@ struct alignas(16) df2 {
 // the remaining 29 rounded to a float.  Built from the bit pattern on the
 // integer and FP32 pipes (GB300 converts FP64 on its FP64 pipe, at 1/64 of
 // the FP32 rate) wherever both parts are normal floats, |x| in [2^-74,
-// 2^127]; elsewhere (zero, tiny or huge values) by FP64 conversions.
+// 2^127], and for zero; elsewhere (tiny or huge values) by FP64 conversions.
 __device__ __forceinline__ void split_f64(double x, float& h, float& l) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const int e = (int)((u >> 52) & 0x7FF);
@@ -52,6 +52,9 @@ __device__ __forceinline__ void split_f64(double x, float& h, float& l) {
     h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
     const float r = __fmul_rn(__uint2float_rn((unsigned)(m & 0x1FFFFFFFu)), __uint_as_float((unsigned)(e - 948) << 23));
     l = __uint_as_float(__float_as_uint(r) | sign);
+  } else if (e == 0) {  // zero (the padding of partial tiles) or an FP64 subnormal, below every float
+    h = 0.f;
+    l = 0.f;
   } else {
     h = __double2float_rn(x);
     l = __double2float_rn(x - (double)h);
