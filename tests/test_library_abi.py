@@ -52,3 +52,22 @@ def test_null_handles_are_rejected(lib_path):
         checked += 1
     assert checked > 40
     assert lib.hh_host_free(None) == 0
+
+
+def test_header_constants_match_binding():
+    """Every numeric #define of include/hh_dmrg.h that the Python binding also
+    names has the same value there (precision codes, error codes, array sizes
+    of hh_plan_stats and hh_plan_tune)."""
+    txt = open(os.path.join(ROOT, "include", "hh_dmrg.h")).read()
+    defines = {}
+    for name, val in re.findall(r"#define\s+(HH_[A-Z0-9_]+)\s+\(?(-?\d+)\)?", txt):
+        defines[name] = int(val)
+    assert len(defines) > 15
+    shared = [n for n in defines if hasattr(_lib, n)]
+    for n in ("HH_PREC_FP64", "HH_PREC_BF16X6", "HH_PREC_BF16X3", "HH_PREC_FP32", "HH_PREC_FP32X2",
+              "HH_TILE_SHAPES", "HH_TUNE_VARIANTS", "HH_PLAN_STATS", "HH_EIG_OWN", "HH_EIG_CUSOLVER",
+              "HH_ERR_INVALID", "HH_ERR_TIMEOUT"):
+        assert n in shared, n
+    bad = {n: (defines[n], getattr(_lib, n)) for n in shared if defines[n] != getattr(_lib, n)}
+    assert not bad, bad
+    assert defines["HH_TUNE_VARIANTS"] == 4 * defines["HH_TILE_SHAPES"]
