@@ -890,10 +890,13 @@ __global__ void __launch_bounds__(512) chol_inv_kernel(const CholItem* __restric
     for (int q = j + threadIdx.x; q < c; q += blockDim.x)
       G[(long long)j * c + q] = q == j ? rjj : G[(long long)j * c + q] * inv;
     __syncthreads();
-    const int m = c - j - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int p = j + 1 + e / m, q = j + 1 + e % m;
-      if (q >= p) G[(long long)p * c + q] = fma(-G[(long long)j * c + p], G[(long long)j * c + q], G[(long long)p * c + q]);
+    // trailing update of the upper triangle: rows p over the warps, columns
+    // q >= p over the lanes (coalesced, no index division, no lower half)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int p = j + 1 + warp; p < c; p += nwarp) {
+      const double gjp = G[(long long)j * c + p];
+      for (int q = p + lane; q < c; q += 32)
+        G[(long long)p * c + q] = fma(-gjp, G[(long long)j * c + q], G[(long long)p * c + q]);
     }
     __syncthreads();
   }
